@@ -1,0 +1,279 @@
+"""GB300-native AccFFT single-GPU 3-D FFT path: Python binding of the C ABI.
+
+The native library (accfft_gb300/lib/libaccfft_gb300.so, built by
+``accfft_gb300.build``) implements AccFFT's single-rank GPU transforms and
+spectral operators with hand-written sm_103a kernels.  This module binds its
+C ABI (include/accfft_gb300.h) with ctypes and accepts either raw device
+pointers (int) or CUDA torch tensors.  There is no fallback: if the library
+is missing, ``lib()`` raises.
+
+Mirrors AccFFT's API (include/accfft_gpu.h, include/accfft_gpuf.h,
+include/accfft_operators_gpu.h in the reference):
+
+    plan = PlanR2C((N0, N1, N2), "float32")         # accfft_plan_dft_3d_r2c_gpuf
+    plan.r2c(u, u_hat)                              # accfft_execute_r2c_gpuf
+    plan.c2r(u_hat, u2)                             # accfft_execute_c2r_gpuf
+    plan.laplace(lap_u, u)                          # accfft_laplace_gpuf
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import re
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "lib", "libaccfft_gb300.so")
+API_LIB_PATH = os.path.join(HERE, "lib", "libaccfft_gpu.so")
+HEADER = os.path.join(os.path.dirname(HERE), "include", "accfft_gb300.h")
+
+ACCFFT_FORWARD = -1
+ACCFFT_BACKWARD = +1
+ACCFFT_ESTIMATE = 1
+ACCFFT_MEASURE = 2
+
+OK, EINVAL, EUNSUPPORTED, ECUDA, ENOTBAKED, EOVERFLOW = range(6)
+
+_lib = None
+
+
+class AccfftError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"accfft_gb300 error {code}: {msg}")
+        self.code = code
+
+
+def header_symbols() -> list[str]:
+    """Names of every function declared in include/accfft_gb300.h."""
+    txt = open(HEADER).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(accfft_c_\w+)\s*\(", txt)))
+
+
+def lib() -> ctypes.CDLL:
+    """Load the native library (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(f"{LIB_PATH} is missing: run `python -m accfft_gb300.build` first")
+    L = ctypes.CDLL(LIB_PATH)
+    vp, ip, dp = ctypes.c_void_p, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double)
+    ll, i, u = ctypes.c_longlong, ctypes.c_int, ctypes.c_uint
+    sig = {
+        "accfft_c_last_error": ([], ctypes.c_char_p),
+        "accfft_c_version": ([], i),
+        "accfft_c_length_supported": ([i], i),
+        "accfft_c_kernel_launches": ([], ctypes.c_ulonglong),
+        "accfft_c_dfft_get_local_size": ([i, i, i, ip, ip, i], ll),
+        "accfft_c_local_size_dft_r2c": ([ip, ip, ip, ip, ip, i], ll),
+        "accfft_c_local_size_dft_c2c": ([ip, ip, ip, ip, ip, i], ll),
+        "accfft_c_plan_dft_3d_r2c_gpu": ([ip, vp, vp, u], vp),
+        "accfft_c_plan_dft_3d_r2c_gpuf": ([ip, vp, vp, u], vp),
+        "accfft_c_plan_dft_3d_c2c_gpu": ([ip, vp, vp, u], vp),
+        "accfft_c_plan_dft_3d_c2c_gpuf": ([ip, vp, vp, u], vp),
+        "accfft_c_destroy_plan": ([vp], None),
+        "accfft_c_plan_info": ([vp, ip, ip, ip, ip, ctypes.POINTER(ll)], i),
+        "accfft_c_set_stream": ([vp, vp, i], i),
+        "accfft_c_execute_r2c_gpu": ([vp, vp, vp, dp, u], i),
+        "accfft_c_execute_c2r_gpu": ([vp, vp, vp, dp, u], i),
+        "accfft_c_execute_gpu": ([vp, i, vp, vp, dp, u], i),
+        "accfft_c_execute_c2c_gpu": ([vp, i, vp, vp, dp, u], i),
+        "accfft_c_execute_r2c_gpuf": ([vp, vp, vp, dp, u], i),
+        "accfft_c_execute_c2r_gpuf": ([vp, vp, vp, dp, u], i),
+        "accfft_c_execute_gpuf": ([vp, i, vp, vp, dp, u], i),
+        "accfft_c_execute_c2c_gpuf": ([vp, i, vp, vp, dp, u], i),
+        "accfft_c_execute_r2c_axis": ([vp, i, vp, vp, dp], i),
+        "accfft_c_execute_c2r_axis": ([vp, i, vp, vp, dp], i),
+        "accfft_c_grad": ([vp, vp, vp, vp, vp, u, dp], i),
+        "accfft_c_grad_slow": ([vp, vp, vp, vp, vp, u, dp], i),
+        "accfft_c_laplace": ([vp, vp, vp, dp], i),
+        "accfft_c_divergence": ([vp, vp, vp, vp, vp, dp], i),
+        "accfft_c_divergence_slow": ([vp, vp, vp, vp, vp, dp], i),
+        "accfft_c_biharmonic": ([vp, vp, vp, dp], i),
+        "accfft_c_inv_laplace": ([vp, vp, vp, dp], i),
+        "accfft_c_inv_biharmonic": ([vp, vp, vp, dp], i),
+    }
+    for name, (args, res) in sig.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = res
+    _lib = L
+    return L
+
+
+def last_error() -> str:
+    return lib().accfft_c_last_error().decode()
+
+
+def kernel_launches() -> int:
+    return int(lib().accfft_c_kernel_launches())
+
+
+def _check(rc: int):
+    if rc != OK:
+        raise AccfftError(rc, last_error())
+
+
+def _ints(vals):
+    return (ctypes.c_int * len(vals))(*vals)
+
+
+def _ptr(x) -> int | None:
+    """Device address of a CUDA tensor, an int pointer, or None."""
+    if x is None:
+        return None
+    if isinstance(x, int):
+        return x
+    if hasattr(x, "data_ptr"):
+        if not x.is_cuda:
+            raise ValueError("expected a CUDA tensor")
+        if not x.is_contiguous():
+            raise ValueError("expected a contiguous tensor")
+        return x.data_ptr()
+    raise TypeError(f"cannot take a device pointer of {type(x).__name__}")
+
+
+def local_size_r2c(n, real_bytes=8):
+    """accfft_local_size_dft_r2c_gpu[f] (src/accfft_common.cpp:98-192) at P = 1."""
+    isz, ist, osz, ost = (ctypes.c_int * 3)(), (ctypes.c_int * 3)(), (ctypes.c_int * 3)(), (ctypes.c_int * 3)()
+    amax = lib().accfft_c_local_size_dft_r2c(_ints(n), isz, ist, osz, ost, real_bytes)
+    return int(amax), tuple(isz), tuple(ist), tuple(osz), tuple(ost)
+
+
+def local_size_c2c(n, real_bytes=8):
+    """accfft_local_size_dft_c2c_gpu[f] (src/accfft_common.cpp:203-256) at P = 1."""
+    isz, ist, osz, ost = (ctypes.c_int * 3)(), (ctypes.c_int * 3)(), (ctypes.c_int * 3)(), (ctypes.c_int * 3)()
+    amax = lib().accfft_c_local_size_dft_c2c(_ints(n), isz, ist, osz, ost, real_bytes)
+    return int(amax), tuple(isz), tuple(ist), tuple(osz), tuple(ost)
+
+
+class _Plan:
+    kind = 0
+
+    def __init__(self, n, dtype="float32", data=None, data_out=None, flags=ACCFFT_MEASURE):
+        self.n = tuple(int(v) for v in n)
+        self.dtype = str(dtype).replace("torch.", "")
+        if self.dtype not in ("float32", "float64"):
+            raise ValueError("dtype must be float32 or float64")
+        self.dbl = self.dtype == "float64"
+        L = lib()
+        fn = {(1, False): L.accfft_c_plan_dft_3d_r2c_gpuf, (1, True): L.accfft_c_plan_dft_3d_r2c_gpu,
+              (2, False): L.accfft_c_plan_dft_3d_c2c_gpuf, (2, True): L.accfft_c_plan_dft_3d_c2c_gpu}[
+            (self.kind, self.dbl)]
+        d, o = _ptr(data), _ptr(data_out)
+        self._h = fn(_ints(self.n), d, o, flags)
+        if not self._h:
+            raise AccfftError(EINVAL, last_error())
+        kind, dbl, inplace = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        amax = ctypes.c_longlong()
+        _check(L.accfft_c_plan_info(self._h, None, ctypes.byref(kind), ctypes.byref(dbl), ctypes.byref(inplace),
+                                    ctypes.byref(amax)))
+        self.inplace = bool(inplace.value)
+        self.alloc_max = int(amax.value)
+
+    @property
+    def handle(self):
+        return self._h
+
+    def set_stream(self, stream, blocking=False):
+        """Enqueue on a CUDA stream (cudaStream_t as int, or a torch.cuda.Stream)."""
+        s = getattr(stream, "cuda_stream", stream)
+        _check(lib().accfft_c_set_stream(self._h, s, 1 if blocking else 0))
+
+    def destroy(self):
+        if getattr(self, "_h", None):
+            lib().accfft_c_destroy_plan(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass
+
+    @staticmethod
+    def _timer(timer):
+        if timer is None:
+            return None, None
+        buf = (ctypes.c_double * 5)(*timer[:5])
+        return buf, ctypes.cast(buf, ctypes.POINTER(ctypes.c_double))
+
+    @staticmethod
+    def _timer_back(buf, timer):
+        if buf is not None:
+            for k in range(5):
+                timer[k] = buf[k]
+
+
+class PlanR2C(_Plan):
+    """accfft_plan_dft_3d_r2c_gpu / _gpuf: real [N0][N1][N2] <-> complex [N0][N1][N2/2+1]."""
+    kind = 1
+
+    def r2c(self, data, data_out, xyz=7, timer=None):
+        buf, tp = self._timer(timer)
+        f = lib().accfft_c_execute_r2c_gpu if self.dbl else lib().accfft_c_execute_r2c_gpuf
+        _check(f(self._h, _ptr(data), _ptr(data_out), tp, xyz))
+        self._timer_back(buf, timer)
+
+    def c2r(self, data, data_out, xyz=7, timer=None):
+        buf, tp = self._timer(timer)
+        f = lib().accfft_c_execute_c2r_gpu if self.dbl else lib().accfft_c_execute_c2r_gpuf
+        _check(f(self._h, _ptr(data), _ptr(data_out), tp, xyz))
+        self._timer_back(buf, timer)
+
+    def execute(self, direction, data, data_out, xyz=7, timer=None):
+        buf, tp = self._timer(timer)
+        f = lib().accfft_c_execute_gpu if self.dbl else lib().accfft_c_execute_gpuf
+        _check(f(self._h, direction, _ptr(data), _ptr(data_out), tp, xyz))
+        self._timer_back(buf, timer)
+
+    def r2c_axis(self, axis, data, data_out, timer=None):
+        buf, tp = self._timer(timer)
+        _check(lib().accfft_c_execute_r2c_axis(self._h, axis, _ptr(data), _ptr(data_out), tp))
+        self._timer_back(buf, timer)
+
+    def c2r_axis(self, axis, data, data_out, timer=None):
+        buf, tp = self._timer(timer)
+        _check(lib().accfft_c_execute_c2r_axis(self._h, axis, _ptr(data), _ptr(data_out), tp))
+        self._timer_back(buf, timer)
+
+    # ---- operators (accfft_operators_gpu.h)
+    def grad(self, ax, ay, az, a, xyz=7, timer=None, slow=False):
+        buf, tp = self._timer(timer)
+        f = lib().accfft_c_grad_slow if slow else lib().accfft_c_grad
+        _check(f(self._h, _ptr(ax), _ptr(ay), _ptr(az), _ptr(a), xyz, tp))
+        self._timer_back(buf, timer)
+
+    def divergence(self, div, ax, ay, az, timer=None, slow=False):
+        buf, tp = self._timer(timer)
+        f = lib().accfft_c_divergence_slow if slow else lib().accfft_c_divergence
+        _check(f(self._h, _ptr(div), _ptr(ax), _ptr(ay), _ptr(az), tp))
+        self._timer_back(buf, timer)
+
+    def _op(self, name, out, a, timer):
+        buf, tp = self._timer(timer)
+        _check(getattr(lib(), "accfft_c_" + name)(self._h, _ptr(out), _ptr(a), tp))
+        self._timer_back(buf, timer)
+
+    def laplace(self, out, a, timer=None):
+        self._op("laplace", out, a, timer)
+
+    def biharmonic(self, out, a, timer=None):
+        self._op("biharmonic", out, a, timer)
+
+    def inv_laplace(self, out, a, timer=None):
+        self._op("inv_laplace", out, a, timer)
+
+    def inv_biharmonic(self, out, a, timer=None):
+        self._op("inv_biharmonic", out, a, timer)
+
+
+class PlanC2C(_Plan):
+    """accfft_plan_dft_3d_c2c_gpu / _gpuf: complex [N0][N1][N2] (interleaved)."""
+    kind = 2
+
+    def c2c(self, direction, data, data_out, xyz=7, timer=None):
+        buf, tp = self._timer(timer)
+        f = lib().accfft_c_execute_c2c_gpu if self.dbl else lib().accfft_c_execute_c2c_gpuf
+        _check(f(self._h, direction, _ptr(data), _ptr(data_out), tp, xyz))
+        self._timer_back(buf, timer)

@@ -1,0 +1,53 @@
+// Kernel argument blocks passed by value from the host plan layer to the
+// pass kernels.  Plain C++: shared by nvcc and host compilers.
+#pragma once
+
+namespace afg {
+
+enum SymKind {
+  SYM_NONE = 0,
+  SYM_LAPLACE = 1,      // -(wx^2+wy^2+wz^2) * scale
+  SYM_BIHARM = 2,       // (wx^2+wy^2+wz^2)^2 * scale
+  SYM_INVLAP = 3,       // scale / -(wx^2+wy^2+wz^2), 0 where the sum is 0
+  SYM_INVBIHARM = 4,    // scale / (kx^2+ky^2+kz^2)^2 without Nyquist folding, 1 where 0
+  SYM_GRADX = 5,        // i * wx * scale   (3-D spectrum)
+  SYM_GRADY = 6,
+  SYM_GRADZ = 7,
+  SYM_DERIV1 = 8,       // i * w(p) * scale (1-D symbol along the pass axis)
+  SYM_DERIV2 = 9        // -w(p)^2 * scale
+};
+
+struct SymArgs {
+  int kind;
+  int n0, n1, n2;   // grid sizes used to fold indices into wave numbers
+  int h2;           // spectrum columns per y row (N2/2+1 for r2c spectra)
+  int axis_len;     // line length for the 1-D symbols
+  double scale;
+};
+
+struct StridedArgs {
+  const void* in;
+  void* out;
+  const void* acc;          // optional addend, laid out like out (MODE 1)
+  const void* tw;           // stage twiddles of the line length
+  long long ncols;          // columns over all slabs
+  long long cps;            // columns per slab
+  long long in_slab, in_line;
+  long long out_slab, out_line;
+  int inverse;              // MODE 0: conjugate on load and store
+  SymArgs sym;              // MODE 1
+};
+
+struct ContigArgs {
+  const void* in;
+  void* out;
+  const void* acc;          // optional addend (k_zsym), laid out like out
+  const void* tw;           // stage twiddles of the line length
+  const void* tw_post;      // r2c split twiddles w_{2M}^k, k = 0..M
+  long long nlines;
+  long long in_dist, out_dist;   // in elements of the array's own type
+  int inverse;
+  SymArgs sym;
+};
+
+}  // namespace afg

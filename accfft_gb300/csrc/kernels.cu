@@ -1,0 +1,104 @@
+// One translation unit per (precision, kernel kind, length group): the build
+// compiles this file with -DAFG_PREC=<0|1> -DAFG_KIND=<0..4> -DAFG_GROUP=<0|1>
+// so the template instantiations spread over parallel nvcc processes.
+//   AFG_PREC 0 = float, 1 = double
+//   AFG_KIND 0 = strided (MODE 0 and 1), 1 = zc2c, 2 = zr2c, 3 = zc2r, 4 = zsym
+#include "passes.cuh"
+#include "launch.h"
+
+#if !defined(AFG_PREC) || !defined(AFG_KIND) || !defined(AFG_GROUP)
+#error "AFG_PREC, AFG_KIND and AFG_GROUP must be defined"
+#endif
+
+#if AFG_PREC == 0
+typedef float Real;
+#define AFG_P f32
+#else
+typedef double Real;
+#define AFG_P f64
+#endif
+#if AFG_GROUP == 0
+#define AFG_G g0
+#define AFG_LIST AFG_LENGTHS_G0
+#else
+#define AFG_G g1
+#define AFG_LIST AFG_LENGTHS_G1
+#endif
+#if AFG_KIND == 0
+#define AFG_K launch_strided
+#elif AFG_KIND == 1
+#define AFG_K launch_zc2c
+#elif AFG_KIND == 2
+#define AFG_K launch_zr2c
+#elif AFG_KIND == 3
+#define AFG_K launch_zc2r
+#else
+#define AFG_K launch_zsym
+#endif
+#define AFG_CAT4_(a, b, c) a##_##b##_##c
+#define AFG_CAT4(a, b, c) AFG_CAT4_(a, b, c)
+#define AFG_NAME AFG_CAT4(AFG_K, AFG_P, AFG_G)
+
+namespace afg {
+
+template <typename K>
+static void prepare(K kernel, size_t smem) {
+  // per-instantiation one-time opt-in to large dynamic shared memory
+  static bool done = false;
+  if (!done) {
+    if (smem > 48 * 1024) cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    done = true;
+  }
+}
+
+#if AFG_KIND == 0
+template <int L, int MODE>
+static void run_strided(const StridedArgs& a, cudaStream_t s) {
+  typedef StridedShape<Real, L> SH;
+  auto k = k_strided<Real, L, MODE>;
+  prepare(k, SH::smem);
+  unsigned grid = unsigned((a.ncols + SH::TC - 1) / SH::TC);
+  k<<<grid, SH::threads, SH::smem, s>>>(a);
+  count_launch();
+}
+bool AFG_NAME(int L, int mode, const StridedArgs& a, cudaStream_t s) {
+  switch (L) {
+#define AFG_CASE(n) \
+  case n:                          \
+    if (mode) run_strided<n, 1>(a, s); \
+    else run_strided<n, 0>(a, s);  \
+    return true;
+    AFG_LIST(AFG_CASE)
+#undef AFG_CASE
+    default: return false;
+  }
+}
+#else
+template <int L>
+static void run_contig(const ContigArgs& a, cudaStream_t s) {
+  typedef ContigShape<Real, L> SH;
+#if AFG_KIND == 1
+  auto k = k_zc2c<Real, L>;
+#elif AFG_KIND == 2
+  auto k = k_zr2c<Real, L>;
+#elif AFG_KIND == 3
+  auto k = k_zc2r<Real, L>;
+#else
+  auto k = k_zsym<Real, L>;
+#endif
+  prepare(k, SH::smem);
+  unsigned grid = unsigned((a.nlines + SH::TL - 1) / SH::TL);
+  k<<<grid, SH::threads, SH::smem, s>>>(a);
+  count_launch();
+}
+bool AFG_NAME(int L, const ContigArgs& a, cudaStream_t s) {
+  switch (L) {
+#define AFG_CASE(n) case n: run_contig<n>(a, s); return true;
+    AFG_LIST(AFG_CASE)
+#undef AFG_CASE
+    default: return false;
+  }
+}
+#endif
+
+}  // namespace afg

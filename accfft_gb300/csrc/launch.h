@@ -1,0 +1,43 @@
+// Host-side entry points into the pass kernels.  Each launcher returns false
+// when the line length has no compiled kernel; the plan layer checks every
+// axis against afg_length_supported() before it accepts a size.
+#pragma once
+#include <cuda_runtime.h>
+#include "args.h"
+
+// Lengths with compiled line kernels (complex line length L for c2c axes,
+// half length M = N2/2 for the real z axis), split in two groups so the
+// instantiations compile in parallel translation units.
+#define AFG_LENGTHS_G0(X) \
+  X(1) X(2) X(3) X(4) X(5) X(6) X(8) X(9) X(10) X(12) X(16) X(20) X(24) X(25) X(32) X(40) X(48) \
+  X(64) X(80) X(90) X(96) X(100) X(128)
+#define AFG_LENGTHS_G1(X) X(160) X(180) X(192) X(200) X(256) X(384) X(512) X(768) X(1024)
+
+namespace afg {
+
+bool length_supported(int L);
+
+// Per-translation-unit launchers, one per (kernel kind, precision, length
+// group); the ungrouped launchers below dispatch over all of them.
+#define AFG_DECL_LAUNCHERS(P, G) \
+  bool launch_strided_##P##_##G(int L, int mode, const StridedArgs& a, cudaStream_t s); \
+  bool launch_zc2c_##P##_##G(int L, const ContigArgs& a, cudaStream_t s); \
+  bool launch_zr2c_##P##_##G(int M, const ContigArgs& a, cudaStream_t s); \
+  bool launch_zc2r_##P##_##G(int M, const ContigArgs& a, cudaStream_t s); \
+  bool launch_zsym_##P##_##G(int M, const ContigArgs& a, cudaStream_t s);
+AFG_DECL_LAUNCHERS(f32, g0)
+AFG_DECL_LAUNCHERS(f32, g1)
+AFG_DECL_LAUNCHERS(f64, g0)
+AFG_DECL_LAUNCHERS(f64, g1)
+
+bool launch_strided(bool dbl, int L, int mode, const StridedArgs& a, cudaStream_t s);
+bool launch_zc2c(bool dbl, int L, const ContigArgs& a, cudaStream_t s);
+bool launch_zr2c(bool dbl, int M, const ContigArgs& a, cudaStream_t s);
+bool launch_zc2r(bool dbl, int M, const ContigArgs& a, cudaStream_t s);
+bool launch_zsym(bool dbl, int M, const ContigArgs& a, cudaStream_t s);
+
+// number of kernel launches issued by this process through the launchers
+unsigned long long launch_count();
+void count_launch();
+
+}  // namespace afg

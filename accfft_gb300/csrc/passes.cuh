@@ -1,0 +1,331 @@
+// Pass kernels: each kernel moves one batch of lines HBM -> registers ->
+// (shared-memory Stockham exchanges) -> HBM exactly once.
+//
+//   k_strided   lines along a strided axis (y or x of a row-major 3-D array).
+//               A CTA owns TC adjacent "columns" (the contiguous index) and
+//               the whole line of each, so loads/stores of one line position
+//               are TC*sizeof(complex) contiguous bytes.  Columns are numbered
+//               across slabs (g -> slab g/cps, column g%cps), so ragged column
+//               counts (e.g. N2/2+1) never leave idle tiles.  MODE 1 fuses
+//               forward FFT -> spectral symbol -> inverse FFT on the same line
+//               (operators, single-axis derivatives) with an optional
+//               accumulate input.
+//   k_zc2c      contiguous complex lines (the z axis of a c2c transform).
+//   k_zr2c      contiguous real lines of length 2M: one M-point complex FFT
+//               of the even/odd packed samples + split to M+1 outputs.
+//   k_zc2r      the inverse of k_zr2c (imaginary parts of the DC and Nyquist
+//               inputs are ignored, as a Hermitian-input real transform does).
+//   k_zsym      r2c -> per-frequency symbol -> c2r on contiguous real lines
+//               (z-direction derivatives) with an optional accumulate input.
+#pragma once
+#include "fft_core.cuh"
+#include "args.h"
+
+namespace afg {
+
+// wave number of index i on an axis of length n: i, i-n above n/2, and 0 at
+// i == n/2 (integer n/2, the Nyquist filter of the reference's kernels)
+__device__ __forceinline__ int fold_wave(int i, int n) {
+  int w = i;
+  if (i > n / 2) w -= n;
+  if (i == n / 2) w = 0;
+  return w;
+}
+__device__ __forceinline__ int fold_wave_nofilter(int i, int n) { return i > n / 2 ? i - n : i; }
+// 1-D line symbols zero the mirror of n/2 as well, so that the symbol stays
+// Hermitian-consistent for odd n (a real-to-real operator on complex-packed
+// real pairs); for even n the two indices coincide
+__device__ __forceinline__ int fold_wave_line(int i, int n) {
+  return (i == n - n / 2) ? 0 : fold_wave(i, n);
+}
+
+// per-column part of a 3-D symbol evaluated in the x pass (column g = y*h2 + kz)
+struct SymCol {
+  int wy, wz;       // folded wave numbers
+  int wy_nf, wz_nf; // unfiltered (for SYM_INVBIHARM)
+};
+__device__ __forceinline__ SymCol sym_column(const SymArgs& s, long long g) {
+  SymCol c{0, 0, 0, 0};
+  if (s.kind >= SYM_LAPLACE && s.kind <= SYM_GRADZ) {
+    int y = int(g / s.h2), kz = int(g - (long long)y * s.h2);
+    c.wy = fold_wave(y, s.n1); c.wz = fold_wave(kz, s.n2);
+    c.wy_nf = fold_wave_nofilter(y, s.n1); c.wz_nf = fold_wave_nofilter(kz, s.n2);
+  }
+  return c;
+}
+
+// multiply x (frequency p along the pass axis, column part c) by the symbol
+template <typename T, typename V>
+__device__ __forceinline__ V sym_apply(const SymArgs& s, const SymCol& c, int p, V x) {
+  const T sc = T(s.scale);
+  switch (s.kind) {
+    case SYM_LAPLACE: {
+      int wx = fold_wave(p, s.n0);
+      T w = T(-(wx * wx + c.wy * c.wy + c.wz * c.wz)) * sc;
+      return c_scale(x, w);
+    }
+    case SYM_BIHARM: {
+      int wx = fold_wave(p, s.n0);
+      T w = T(wx * wx + c.wy * c.wy + c.wz * c.wz);
+      return c_scale(x, w * w * sc);
+    }
+    case SYM_INVLAP: {
+      int wx = fold_wave(p, s.n0);
+      int w = -(wx * wx + c.wy * c.wy + c.wz * c.wz);
+      T m = (w == 0) ? T(0) : sc / T(w);
+      return c_scale(x, m);
+    }
+    case SYM_INVBIHARM: {
+      int wx = fold_wave_nofilter(p, s.n0);
+      T w = T(wx * wx + c.wy_nf * c.wy_nf + c.wz_nf * c.wz_nf);
+      w = w * w;
+      if (w == T(0)) w = T(1);
+      return c_scale(x, sc / w);
+    }
+    case SYM_GRADX: case SYM_GRADY: case SYM_GRADZ: {
+      int w = s.kind == SYM_GRADX ? fold_wave(p, s.n0) : (s.kind == SYM_GRADY ? c.wy : c.wz);
+      T m = T(w) * sc;
+      return c_make<V>(-m * x.y, m * x.x);
+    }
+    case SYM_DERIV1: {
+      T m = T(fold_wave_line(p, s.axis_len)) * sc;
+      return c_make<V>(-m * x.y, m * x.x);
+    }
+    case SYM_DERIV2: {
+      int w = fold_wave_line(p, s.axis_len);
+      return c_scale(x, -T(w * w) * sc);
+    }
+    default:
+      return x;
+  }
+}
+
+// ------------------------------------------------------------ tile shapes
+template <typename T, int L> struct StridedShape {
+  static constexpr int P = LineFFT<T, L>::P;
+  static constexpr int tmin = sizeof(T) == 4 ? 16 : 8;      // 128-byte row segments
+  static constexpr int want = (sizeof(T) == 4 ? 256 : 128) / P;
+  static constexpr int TC = want > tmin ? (want > 64 ? 64 : want) : tmin;
+  static constexpr int threads = P * TC;
+  static constexpr size_t smem = size_t(L) * TC * sizeof(typename CT<T>::V);
+};
+
+template <typename T, int L> struct ContigShape {
+  static constexpr int P = LineFFT<T, L>::P;
+  static constexpr int want = (sizeof(T) == 4 ? 256 : 128) / P;
+  static constexpr int TL = want > 1 ? want : 1;
+  static constexpr int threads = P * TL;
+  // line pitch: room for L+1 entries (r2c spectra), rounded to a 128-byte
+  // bank row, plus a shift of P slots when several lines share a warp so
+  // that their accesses land in different banks
+  static constexpr int slots = sizeof(T) == 4 ? 16 : 8;
+  static constexpr int LP = ((L + 1 + slots - 1) / slots) * slots + (P < slots ? P : 0);
+  static constexpr size_t smem = size_t(LP) * TL * sizeof(typename CT<T>::V);
+};
+
+// ------------------------------------------------------------------ kernels
+template <typename T, int L, int MODE>
+__global__ void __launch_bounds__(StridedShape<T, L>::threads)
+k_strided(const StridedArgs a) {
+  typedef LineFFT<T, L> LN;
+  typedef typename CT<T>::V V;
+  constexpr int TC = StridedShape<T, L>::TC;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  V* sm = reinterpret_cast<V*>(smraw);
+  const int c = threadIdx.x % TC;
+  const int t = threadIdx.x / TC;
+  const long long g = (long long)blockIdx.x * TC + c;
+  const bool valid = g < a.ncols;
+  const long long gs = valid ? g : 0;          // idle lanes read column 0, store nothing
+  const long long slab = gs / a.cps;
+  const long long cc = gs - slab * a.cps;
+  const V* in = static_cast<const V*>(a.in) + slab * a.in_slab + cc;
+  V* out = static_cast<V*>(a.out) + slab * a.out_slab + cc;
+  const V* tw = static_cast<const V*>(a.tw);
+  auto xw = [&](int p, V x) { sm[p * TC + c] = x; };
+  auto xr = [&](int p) { return sm[p * TC + c]; };
+  if constexpr (MODE == 0) {
+    const T sg = a.inverse ? T(-1) : T(1);
+    const long long il = a.in_line, ol = a.out_line;
+    auto ld = [&](int p) { V x = in[p * il]; x.y *= sg; return x; };
+    auto st = [&](int p, V x) { x.y *= sg; if (valid) out[p * ol] = x; };
+    LN::template run<false, false>(t, tw, ld, st, xw, xr);
+  } else {
+    const SymCol scol = sym_column(a.sym, gs);
+    const long long il = a.in_line, ol = a.out_line;
+    auto ld = [&](int p) { return in[p * il]; };
+    // forward result times the symbol, stored conjugated for the inverse run
+    auto sst = [&](int p, V x) { sm[p * TC + c] = c_conj(sym_apply<T>(a.sym, scol, p, x)); };
+    LN::template run<true, false>(t, tw, ld, sst, xw, xr);
+    __syncthreads();
+    const V* acc = a.acc ? static_cast<const V*>(a.acc) + slab * a.out_slab + cc : nullptr;
+    auto sld = [&](int p) { return sm[p * TC + c]; };
+    auto gst = [&](int p, V x) {
+      x.y = -x.y;
+      if (valid) {
+        if (acc) x = c_add(x, acc[p * ol]);
+        out[p * ol] = x;
+      }
+    };
+    LN::template run<false, true>(t, tw, sld, gst, xw, xr);
+  }
+}
+
+template <typename T, int L>
+__global__ void __launch_bounds__(ContigShape<T, L>::threads)
+k_zc2c(const ContigArgs a) {
+  typedef LineFFT<T, L> LN;
+  typedef typename CT<T>::V V;
+  constexpr int P = LN::P, LP = ContigShape<T, L>::LP, TL = ContigShape<T, L>::TL;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  V* sm = reinterpret_cast<V*>(smraw);
+  const int t = threadIdx.x % P, li = threadIdx.x / P;
+  const long long line = (long long)blockIdx.x * TL + li;
+  const bool valid = line < a.nlines;
+  const long long ls = valid ? line : 0;
+  const V* in = static_cast<const V*>(a.in) + ls * a.in_dist;
+  V* out = static_cast<V*>(a.out) + ls * a.out_dist;
+  V* sl = sm + li * LP;
+  const T sg = a.inverse ? T(-1) : T(1);
+  auto xw = [&](int p, V x) { sl[p] = x; };
+  auto xr = [&](int p) { return sl[p]; };
+  auto ld = [&](int p) { V x = in[p]; x.y *= sg; return x; };
+  auto st = [&](int p, V x) { x.y *= sg; if (valid) out[p] = x; };
+  LN::template run<false, false>(t, static_cast<const V*>(a.tw), ld, st, xw, xr);
+}
+
+// X[k] from the packed half-length spectrum: zk = Z[k mod M], zm = Z[(M-k) mod M], w = w_{2M}^k
+template <typename V>
+__device__ __forceinline__ V r2c_split(V zk, V zm, V w) {
+  typedef decltype(V().x) T;
+  V e = c_make<V>(T(0.5) * (zk.x + zm.x), T(0.5) * (zk.y - zm.y));
+  V o = c_make<V>(T(0.5) * (zk.y + zm.y), T(-0.5) * (zk.x - zm.x));
+  return c_add(e, c_mul(w, o));
+}
+// Z[k] of the packed inverse from X[k], X[M-k] and wc = conj(w_{2M}^k)
+template <typename V>
+__device__ __forceinline__ V c2r_merge(V xk, V xm, V wc) {
+  V s = c_make<V>(xk.x + xm.x, xk.y - xm.y);
+  V d = c_make<V>(xk.x - xm.x, xk.y + xm.y);
+  V wd = c_mul(wc, d);
+  return c_make<V>(s.x - wd.y, s.y + wd.x);
+}
+
+template <typename T, int M>
+__global__ void __launch_bounds__(ContigShape<T, M>::threads)
+k_zr2c(const ContigArgs a) {
+  typedef LineFFT<T, M> LN;
+  typedef typename CT<T>::V V;
+  constexpr int P = LN::P, LP = ContigShape<T, M>::LP, TL = ContigShape<T, M>::TL;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  V* sm = reinterpret_cast<V*>(smraw);
+  const int t = threadIdx.x % P, li = threadIdx.x / P;
+  const long long line = (long long)blockIdx.x * TL + li;
+  const bool valid = line < a.nlines;
+  const long long ls = valid ? line : 0;
+  const V* in = reinterpret_cast<const V*>(static_cast<const T*>(a.in) + ls * a.in_dist);
+  V* out = static_cast<V*>(a.out) + ls * a.out_dist;
+  V* sl = sm + li * LP;
+  auto xw = [&](int p, V x) { sl[p] = x; };
+  auto xr = [&](int p) { return sl[p]; };
+  auto ld = [&](int p) { return in[p]; };
+  auto st = [&](int p, V x) { sl[p] = x; };
+  LN::template run<true, false>(t, static_cast<const V*>(a.tw), ld, st, xw, xr);
+  __syncthreads();
+  const V* twp = static_cast<const V*>(a.tw_post);
+  for (int k = t; k <= M; k += P) {
+    V zk = sl[k == M ? 0 : k];
+    V zm = sl[k == 0 ? 0 : M - k];
+    V x = r2c_split(zk, zm, __ldg(twp + k));
+    if (valid) out[k] = x;
+  }
+}
+
+template <typename T, int M>
+__global__ void __launch_bounds__(ContigShape<T, M>::threads)
+k_zc2r(const ContigArgs a) {
+  typedef LineFFT<T, M> LN;
+  typedef typename CT<T>::V V;
+  constexpr int P = LN::P, LP = ContigShape<T, M>::LP, TL = ContigShape<T, M>::TL;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  V* sm = reinterpret_cast<V*>(smraw);
+  const int t = threadIdx.x % P, li = threadIdx.x / P;
+  const long long line = (long long)blockIdx.x * TL + li;
+  const bool valid = line < a.nlines;
+  const long long ls = valid ? line : 0;
+  const V* in = static_cast<const V*>(a.in) + ls * a.in_dist;
+  V* out = reinterpret_cast<V*>(static_cast<T*>(a.out) + ls * a.out_dist);
+  V* sl = sm + li * LP;
+  for (int k = t; k <= M; k += P) sl[k] = in[k];
+  __syncthreads();
+  const V* twp = static_cast<const V*>(a.tw_post);
+  auto xw = [&](int p, V x) { sl[p] = x; };
+  auto xr = [&](int p) { return sl[p]; };
+  auto ld = [&](int p) {
+    V xk = sl[p], xm = sl[M - p];
+    if (p == 0) { xk.y = T(0); xm.y = T(0); }
+    return c_conj(c2r_merge(xk, xm, c_conj(__ldg(twp + p))));
+  };
+  auto st = [&](int p, V x) { x.y = -x.y; if (valid) out[p] = x; };
+  LN::template run<false, true>(t, static_cast<const V*>(a.tw), ld, st, xw, xr);
+}
+
+// real line r2c -> symbol(k) -> c2r, one pass (z-direction derivative)
+template <typename T, int M>
+__global__ void __launch_bounds__(ContigShape<T, M>::threads)
+k_zsym(const ContigArgs a) {
+  typedef LineFFT<T, M> LN;
+  typedef typename CT<T>::V V;
+  constexpr int P = LN::P, LP = ContigShape<T, M>::LP, TL = ContigShape<T, M>::TL;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  V* sm = reinterpret_cast<V*>(smraw);
+  const int t = threadIdx.x % P, li = threadIdx.x / P;
+  const long long line = (long long)blockIdx.x * TL + li;
+  const bool valid = line < a.nlines;
+  const long long ls = valid ? line : 0;
+  const V* in = reinterpret_cast<const V*>(static_cast<const T*>(a.in) + ls * a.in_dist);
+  V* out = reinterpret_cast<V*>(static_cast<T*>(a.out) + ls * a.out_dist);
+  const V* acc = a.acc ? reinterpret_cast<const V*>(static_cast<const T*>(a.acc) + ls * a.out_dist) : nullptr;
+  V* sl = sm + li * LP;
+  const V* tw = static_cast<const V*>(a.tw);
+  auto xw = [&](int p, V x) { sl[p] = x; };
+  auto xr = [&](int p) { return sl[p]; };
+  auto ld = [&](int p) { return in[p]; };
+  auto st = [&](int p, V x) { sl[p] = x; };
+  LN::template run<true, false>(t, tw, ld, st, xw, xr);
+  __syncthreads();
+  const V* twp = static_cast<const V*>(a.tw_post);
+  const SymCol none{0, 0, 0, 0};
+  for (int k = t; 2 * k <= M; k += P) {
+    if (k == 0) {
+      V z0 = sl[0];
+      V x0 = sym_apply<T>(a.sym, none, 0, c_make<V>(z0.x + z0.y, T(0)));
+      V xn = sym_apply<T>(a.sym, none, M, c_make<V>(z0.x - z0.y, T(0)));
+      // imaginary parts of DC and Nyquist are dropped by the real inverse
+      sl[0] = c_make<V>(x0.x + xn.x, -(x0.x - xn.x));   // conj(Z'[0])
+    } else {
+      V zk = sl[k], zm = sl[M - k];
+      V wk = __ldg(twp + k), wm = __ldg(twp + (M - k));
+      V xk = sym_apply<T>(a.sym, none, k, r2c_split(zk, zm, wk));
+      if (2 * k == M) {
+        sl[k] = c_conj(c2r_merge(xk, xk, c_conj(wk)));
+      } else {
+        V xm = sym_apply<T>(a.sym, none, M - k, r2c_split(zm, zk, wm));
+        sl[k] = c_conj(c2r_merge(xk, xm, c_conj(wk)));
+        sl[M - k] = c_conj(c2r_merge(xm, xk, c_conj(wm)));
+      }
+    }
+  }
+  __syncthreads();
+  auto sld = [&](int p) { return sl[p]; };
+  auto gst = [&](int p, V x) {
+    x.y = -x.y;
+    if (valid) {
+      if (acc) x = c_add(x, acc[p]);
+      out[p] = x;
+    }
+  };
+  LN::template run<false, true>(t, tw, sld, gst, xw, xr);
+}
+
+}  // namespace afg

@@ -1,0 +1,664 @@
+// Plan layer of the C ABI (include/accfft_gb300.h): size bookkeeping with the
+// reference's semantics, twiddle tables, scratch ownership and the pass
+// sequences of every transform and operator.  All device work is issued by
+// the pass kernels through the launchers in launch.h; there is no host
+// fallback: a size without kernels is rejected at plan time.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdarg>
+#include <cstdint>
+#include <initializer_list>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/accfft_gb300.h"
+#include "args.h"
+#include "launch.h"
+#include "line_plan.h"
+
+using namespace afg;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+  return fail(ACCFFT_C_ECUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+// exp(-2*pi*i*m/d) with exact integer octant reduction and long-double
+// evaluation on [0, pi/4]
+void twiddle(long long m, long long d, long double* c, long double* s) {
+  m %= d;
+  if (m < 0) m += d;
+  const long double q = 0.785398163397448309615660845819875721L;  // pi/4
+  long long o = (8 * m) / d;
+  long long r = 8 * m - o * d;
+  long double phi = q * (long double)r / (long double)d;
+  long double psi = q * (long double)(d - r) / (long double)d;
+  long double cc = 0, ss = 0;
+  switch (o) {
+    case 0: cc = cosl(phi); ss = sinl(phi); break;
+    case 1: cc = sinl(psi); ss = cosl(psi); break;
+    case 2: cc = -sinl(phi); ss = cosl(phi); break;
+    case 3: cc = -cosl(psi); ss = sinl(psi); break;
+    case 4: cc = -cosl(phi); ss = -sinl(phi); break;
+    case 5: cc = -sinl(psi); ss = -cosl(psi); break;
+    case 6: cc = sinl(phi); ss = -cosl(phi); break;
+    default: cc = cosl(psi); ss = -sinl(psi); break;
+  }
+  *c = cc;
+  *s = -ss;   // forward sign
+}
+
+// stage twiddles of a line length (layout fixed by plan_tw_offset)
+std::vector<long double> stage_table(int L, bool dbl) {
+  LinePlan pl = plan_for(L, dbl);
+  int n = plan_tw_size(pl);
+  std::vector<long double> t(2 * (size_t)(n > 0 ? n : 1), 0.0L);
+  for (int s = 1; s < pl.ns; ++s) {
+    int Ns = plan_ns_before(pl, s), R = pl.radix[s], off = plan_tw_offset(pl, s);
+    for (int r = 1; r < R; ++r)
+      for (int k = 0; k < Ns; ++k) {
+        long double c, si;
+        twiddle((long long)k * r, (long long)Ns * R, &c, &si);
+        size_t i = (size_t)off + (size_t)(r - 1) * Ns + k;
+        t[2 * i] = c;
+        t[2 * i + 1] = si;
+      }
+  }
+  return t;
+}
+
+// r2c split twiddles w_{2M}^k, k = 0..M
+std::vector<long double> post_table(int M) {
+  std::vector<long double> t(2 * (size_t)(M + 1));
+  for (int k = 0; k <= M; ++k) twiddle(k, 2LL * M, &t[2 * k], &t[2 * k + 1]);
+  return t;
+}
+
+constexpr unsigned XB = 1, YB = 2, ZB = 4;
+
+}  // namespace
+
+struct accfft_c_plan {
+  int kind = 0;         // 1 = r2c, 2 = c2c
+  bool dbl = false;
+  int n[3] = {0, 0, 0};
+  bool inplace = false;
+  void* data = nullptr;
+  void* data_out = nullptr;
+  long long alloc_max = 0;
+  int device = 0;
+  // device tables: x, y and z stage twiddles (z: length N2/2 for r2c, N2 for
+  // c2c) and the r2c split twiddles
+  void* tw_block = nullptr;
+  const void* tw_x = nullptr;
+  const void* tw_y = nullptr;
+  const void* tw_z = nullptr;
+  const void* tw_post = nullptr;
+  // spectrum-sized scratch (r2c plans): out-of-place c2r and operators
+  void* scratch = nullptr;
+  cudaStream_t stream = 0;
+  bool blocking = true;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+
+  long long esz() const { return dbl ? 8 : 4; }
+  int M() const { return n[2] / 2; }
+  long long H2() const { return n[2] / 2 + 1; }
+  // row length (reals) of the plan's real arrays
+  long long rrow() const { return inplace ? 2 * H2() : n[2]; }
+};
+
+namespace {
+
+// ----------------------------------------------------------- local sizes
+// P = 1 restatement of dfft_get_local_size_t: isize = {N0, N1, tuple}
+long long local_size(int N0, int N1, int tuple, int* isize, int* istart, int real_bytes) {
+  isize[0] = N0;
+  isize[1] = N1;
+  isize[2] = tuple;
+  istart[0] = istart[1] = istart[2] = 0;
+  return (long long)N0 * N1 * tuple * real_bytes;
+}
+
+long long local_size_r2c(const int* n, int* isize, int* istart, int* osize, int* ostart, int rb) {
+  int s0[3], s1[3], st[3];
+  long long amax = 0;
+  long long nt = (long long)(n[2] / 2 + 1) * 2;
+  amax = std::max(amax, local_size(n[0], n[1], (int)nt, s0, st, rb));
+  amax = std::max(amax, 2 * local_size(n[0], (int)(nt / 2), n[1], s1, st, rb));
+  amax = std::max(amax, 2 * local_size(n[1], (int)(nt / 2), n[0], s1, st, rb));
+  // single-axis y and x transforms
+  amax = std::max(amax, local_size(n[0], n[2], n[1], s1, st, rb));
+  amax = std::max(amax, 2 * local_size(n[0], n[2], n[1] / 2 + 1, s1, st, rb));
+  amax = std::max(amax, (long long)n[1] * n[2] * n[0] * rb);
+  amax = std::max(amax, 2LL * n[1] * n[2] * (n[0] / 2 + 1) * rb);
+  local_size(n[0], n[1], n[2], isize, istart, rb);
+  osize[0] = n[0];
+  osize[1] = n[1];
+  osize[2] = n[2] / 2 + 1;
+  ostart[0] = ostart[1] = ostart[2] = 0;
+  return amax;
+}
+
+long long local_size_c2c(const int* n, int* isize, int* istart, int* osize, int* ostart, int rb) {
+  local_size(n[0], n[1], n[2], isize, istart, rb);
+  for (int i = 0; i < 3; ++i) {
+    osize[i] = n[i];
+    ostart[i] = 0;
+  }
+  return 2LL * n[0] * n[1] * n[2] * rb;
+}
+
+// -------------------------------------------------------------- plan make
+accfft_c_plan* make_plan(int kind, bool dbl, const int* n, void* data, void* data_out) {
+  g_err.clear();
+  if (!n) {
+    fail(ACCFFT_C_EINVAL, "plan: NULL size array");
+    return nullptr;
+  }
+  for (int i = 0; i < 3; ++i)
+    if (n[i] < 1) {
+      fail(ACCFFT_C_EINVAL, "plan: size n[%d]=%d must be positive", i, n[i]);
+      return nullptr;
+    }
+  if (kind == 1 && n[2] % 2) {
+    fail(ACCFFT_C_EUNSUPPORTED, "plan: r2c needs an even N2 (got %d)", n[2]);
+    return nullptr;
+  }
+  int zlen = kind == 1 ? n[2] / 2 : n[2];
+  int lens[3] = {n[0], n[1], zlen};
+  for (int i = 0; i < 3; ++i)
+    if (!length_supported(lens[i])) {
+      fail(ACCFFT_C_EUNSUPPORTED, "plan: no kernels for %s length %d (sizes %dx%dx%d)",
+           i == 0 ? "x" : i == 1 ? "y" : "z", lens[i], n[0], n[1], n[2]);
+      return nullptr;
+    }
+  auto* p = new accfft_c_plan;
+  p->kind = kind;
+  p->dbl = dbl;
+  for (int i = 0; i < 3; ++i) p->n[i] = n[i];
+  // in place when the plan-time pointers are equal (the reference's rule);
+  // two NULL pointers make an out-of-place plan
+  p->inplace = (data == data_out) && data != nullptr;
+  p->data = data;
+  p->data_out = data_out;
+  int is[3], ist[3], os[3], ost[3];
+  p->alloc_max = kind == 1 ? local_size_r2c(n, is, ist, os, ost, dbl ? 8 : 4)
+                           : local_size_c2c(n, is, ist, os, ost, dbl ? 8 : 4);
+  cudaGetDevice(&p->device);
+
+  // twiddle tables, rounded from long double to the plan's precision
+  std::vector<std::vector<long double>> tabs;
+  tabs.push_back(stage_table(n[0], dbl));
+  tabs.push_back(stage_table(n[1], dbl));
+  tabs.push_back(stage_table(zlen, dbl));
+  if (kind == 1) tabs.push_back(post_table(n[2] / 2));
+  const size_t cbytes = dbl ? 16 : 8;
+  std::vector<size_t> off;
+  size_t total = 0;
+  for (auto& t : tabs) {
+    off.push_back(total);
+    total += ((t.size() / 2) * cbytes + 255) / 256 * 256;
+  }
+  std::vector<unsigned char> host(total, 0);
+  for (size_t i = 0; i < tabs.size(); ++i) {
+    auto& t = tabs[i];
+    for (size_t j = 0; j < t.size(); ++j) {
+      if (dbl) {
+        double v = (double)t[j];
+        memcpy(&host[off[i] + j * 8], &v, 8);
+      } else {
+        float v = (float)t[j];
+        memcpy(&host[off[i] + j * 4], &v, 4);
+      }
+    }
+  }
+  cudaError_t e = cudaMalloc(&p->tw_block, total);
+  if (e == cudaSuccess) e = cudaMemcpy(p->tw_block, host.data(), total, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && kind == 1) e = cudaMalloc(&p->scratch, (size_t)p->alloc_max);
+  if (e == cudaSuccess) e = cudaEventCreate(&p->ev0);
+  if (e == cudaSuccess) e = cudaEventCreate(&p->ev1);
+  if (e != cudaSuccess) {
+    cuda_fail(e, "plan: device allocation");
+    accfft_c_destroy_plan(p);
+    return nullptr;
+  }
+  auto* base = static_cast<unsigned char*>(p->tw_block);
+  p->tw_x = base + off[0];
+  p->tw_y = base + off[1];
+  p->tw_z = base + off[2];
+  if (kind == 1) p->tw_post = base + off[3];
+  return p;
+}
+
+// ------------------------------------------------------------ execution
+struct Exec {
+  accfft_c_plan* p;
+  double* timer;
+  int rc = ACCFFT_C_OK;
+
+  Exec(accfft_c_plan* plan, double* t) : p(plan), timer(t) {
+    if (p->blocking || timer) cudaEventRecord(p->ev0, p->stream);
+  }
+  bool ok() const { return rc == ACCFFT_C_OK; }
+  void unsupported(const char* what, int L) {
+    if (ok()) rc = fail(ACCFFT_C_EUNSUPPORTED, "%s: no kernel for length %d", what, L);
+  }
+  void strided(const void* in, void* out, const void* tw, int L, long long ncols, long long cps, long long slab,
+               long long line, int inverse) {
+    if (!ok()) return;
+    StridedArgs a{};
+    a.in = in;
+    a.out = out;
+    a.tw = tw;
+    a.ncols = ncols;
+    a.cps = cps;
+    a.in_slab = a.out_slab = slab;
+    a.in_line = a.out_line = line;
+    a.inverse = inverse;
+    if (!launch_strided(p->dbl, L, 0, a, p->stream)) unsupported("strided pass", L);
+  }
+  void strided_sym(const void* in, void* out, const void* acc, const void* tw, int L, long long ncols, long long cps,
+                   long long slab, long long line, const SymArgs& sym) {
+    if (!ok()) return;
+    StridedArgs a{};
+    a.in = in;
+    a.out = out;
+    a.acc = acc;
+    a.tw = tw;
+    a.ncols = ncols;
+    a.cps = cps;
+    a.in_slab = a.out_slab = slab;
+    a.in_line = a.out_line = line;
+    a.sym = sym;
+    if (!launch_strided(p->dbl, L, 1, a, p->stream)) unsupported("symbol pass", L);
+  }
+  // y pass over an [N0][N1][h] complex array, x pass over [N0][N1*h]
+  void ypass(const void* in, void* out, long long h, int inverse) {
+    strided(in, out, p->tw_y, p->n[1], (long long)p->n[0] * h, h, (long long)p->n[1] * h, h, inverse);
+  }
+  void xpass(const void* in, void* out, long long h, int inverse) {
+    long long c = (long long)p->n[1] * h;
+    strided(in, out, p->tw_x, p->n[0], c, c, 0, c, inverse);
+  }
+  void zr2c(const void* in, void* out, long long in_row) {
+    if (!ok()) return;
+    ContigArgs a{};
+    a.in = in;
+    a.out = out;
+    a.tw = p->tw_z;
+    a.tw_post = p->tw_post;
+    a.nlines = (long long)p->n[0] * p->n[1];
+    a.in_dist = in_row;
+    a.out_dist = p->H2();
+    if (!launch_zr2c(p->dbl, p->M(), a, p->stream)) unsupported("z r2c pass", p->M());
+  }
+  void zc2r(const void* in, void* out, long long out_row) {
+    if (!ok()) return;
+    ContigArgs a{};
+    a.in = in;
+    a.out = out;
+    a.tw = p->tw_z;
+    a.tw_post = p->tw_post;
+    a.nlines = (long long)p->n[0] * p->n[1];
+    a.in_dist = p->H2();
+    a.out_dist = out_row;
+    if (!launch_zc2r(p->dbl, p->M(), a, p->stream)) unsupported("z c2r pass", p->M());
+  }
+  void zc2c(const void* in, void* out, int inverse) {
+    if (!ok()) return;
+    ContigArgs a{};
+    a.in = in;
+    a.out = out;
+    a.tw = p->tw_z;
+    a.nlines = (long long)p->n[0] * p->n[1];
+    a.in_dist = a.out_dist = p->n[2];
+    a.inverse = inverse;
+    if (!launch_zc2c(p->dbl, p->n[2], a, p->stream)) unsupported("z c2c pass", p->n[2]);
+  }
+  void zsym(const void* in, void* out, const void* acc, long long row, const SymArgs& sym) {
+    if (!ok()) return;
+    ContigArgs a{};
+    a.in = in;
+    a.out = out;
+    a.acc = acc;
+    a.tw = p->tw_z;
+    a.tw_post = p->tw_post;
+    a.nlines = (long long)p->n[0] * p->n[1];
+    a.in_dist = a.out_dist = row;
+    a.sym = sym;
+    if (!launch_zsym(p->dbl, p->M(), a, p->stream)) unsupported("z symbol pass", p->M());
+  }
+  int finish() {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess && ok()) rc = cuda_fail(e, "kernel launch");
+    if (p->blocking || timer) {
+      cudaEventRecord(p->ev1, p->stream);
+      e = cudaEventSynchronize(p->ev1);
+      if (e != cudaSuccess && ok()) rc = cuda_fail(e, "kernel execution");
+      if (ok() && timer) {
+        float ms = 0;
+        cudaEventElapsedTime(&ms, p->ev0, p->ev1);
+        timer[4] += ms / 1000.0;
+      }
+    }
+    return rc;
+  }
+};
+
+// every array is accessed as whole complex elements (8 or 16 bytes)
+int check_align(const accfft_c_plan* p, const char* fn, std::initializer_list<const void*> ptrs) {
+  const uintptr_t a = p->dbl ? 16 : 8;
+  for (const void* q : ptrs)
+    if (q && (reinterpret_cast<uintptr_t>(q) % a))
+      return fail(ACCFFT_C_EINVAL, "%s: array %p is not %d-byte aligned", fn, q, (int)a);
+  return ACCFFT_C_OK;
+}
+
+int check_plan(accfft_c_plan* p, int kind, int dbl, const char* fn) {
+  g_err.clear();
+  if (!p) return fail(ACCFFT_C_EINVAL, "%s: NULL plan", fn);
+  if (kind && p->kind != kind)
+    return fail(ACCFFT_C_ENOTBAKED, "%s: the plan was made for a %s transform", fn, p->kind == 1 ? "r2c" : "c2c");
+  if (dbl >= 0 && (int)p->dbl != dbl)
+    return fail(ACCFFT_C_EINVAL, "%s: precision mismatch (plan is %s)", fn, p->dbl ? "double" : "float");
+  return ACCFFT_C_OK;
+}
+
+// accfft_execute_gpu (src/accfft_gpu.cpp:444-623) at P = 1
+int exec_r2c_plan(accfft_c_plan* p, int direction, void* in, void* out, double* timer, unsigned xyz) {
+  if (!in) in = p->data;
+  if (!out) out = p->data_out;
+  if (!in || !out) return fail(ACCFFT_C_EINVAL, "execute: NULL data pointer and none given at plan time");
+  if (int rc = check_align(p, "execute", {in, out})) return rc;
+  const long long h = p->H2();
+  Exec ex(p, timer);
+  if (direction == -1) {
+    void* work = in;   // with z skipped the reference transforms the input in place
+    if (xyz & ZB) {
+      ex.zr2c(in, out, p->rrow());
+      work = out;
+    }
+    if (xyz & YB) ex.ypass(work, work, h, 0);
+    if (xyz & XB) ex.xpass(work, work, h, 0);
+  } else if (direction == 1) {
+    // x and y inverse passes read the input spectrum; out of place they write
+    // the plan scratch so the input survives (the reference overwrites it)
+    void* src = in;
+    void* buf = (!(xyz & ZB) || p->inplace) ? in : p->scratch;
+    if (xyz & XB) {
+      ex.xpass(src, buf, h, 1);
+      src = buf;
+    }
+    if (xyz & YB) {
+      ex.ypass(src, buf, h, 1);
+      src = buf;
+    }
+    if (xyz & ZB) ex.zc2r(src, out, p->rrow());
+  } else {
+    return fail(ACCFFT_C_EINVAL, "execute: direction must be -1 or +1 (got %d)", direction);
+  }
+  return ex.finish();
+}
+
+// accfft_execute_c2c_gpu (src/accfft_gpu.cpp:943-1136) at P = 1
+int exec_c2c_plan(accfft_c_plan* p, int direction, void* in, void* out, double* timer, unsigned xyz) {
+  if (!in) in = p->data;
+  if (!out) out = p->data_out;
+  if (!in || !out) return fail(ACCFFT_C_EINVAL, "execute: NULL data pointer and none given at plan time");
+  if (direction != -1 && direction != 1)
+    return fail(ACCFFT_C_EINVAL, "execute: direction must be -1 or +1 (got %d)", direction);
+  if (int rc = check_align(p, "execute_c2c", {in, out})) return rc;
+  const int inv = direction == 1;
+  const long long h = p->n[2];
+  Exec ex(p, timer);
+  // the axes are independent, so the backward transform also starts with z
+  // (in -> out) and never writes its input
+  void* work = in;
+  if (xyz & ZB) {
+    ex.zc2c(in, out, inv);
+    work = out;
+  }
+  if (xyz & YB) ex.ypass(work, work, h, inv);
+  if (xyz & XB) ex.xpass(work, work, h, inv);
+  return ex.finish();
+}
+
+SymArgs make_sym(const accfft_c_plan* p, int kind, double scale, int axis_len = 0) {
+  SymArgs s{};
+  s.kind = kind;
+  s.n0 = p->n[0];
+  s.n1 = p->n[1];
+  s.n2 = p->n[2];
+  s.h2 = (int)p->H2();
+  s.axis_len = axis_len;
+  s.scale = scale;
+  return s;
+}
+
+// full 3-D operator: r2c (z, y) -> fused x pass (forward, symbol, inverse) ->
+// inverse y -> c2r, through the plan scratch spectrum
+int op3d(accfft_c_plan* p, int sym_kind, void* outr, const void* inr, double* timer) {
+  if (!outr || !inr) return fail(ACCFFT_C_EINVAL, "operator: NULL array");
+  if (int rc = check_align(p, "operator", {outr, inr})) return rc;
+  const long long h = p->H2();
+  const double N = (double)p->n[0] * p->n[1] * p->n[2];
+  Exec ex(p, timer);
+  void* s = p->scratch;
+  ex.zr2c(inr, s, p->rrow());
+  ex.ypass(s, s, h, 0);
+  long long c = (long long)p->n[1] * h;
+  ex.strided_sym(s, s, nullptr, p->tw_x, p->n[0], c, c, 0, c, make_sym(p, sym_kind, 1.0 / N));
+  ex.ypass(s, s, h, 1);
+  ex.zc2r(s, outr, p->rrow());
+  return ex.finish();
+}
+
+// one-pass single-axis derivative d/dx_axis of a real field (optionally added
+// to acc).  y and x lines view pairs of adjacent reals as one complex value:
+// the symbol i*w/N is Hermitian-consistent, so it maps real to real and acts
+// on both members of the pair independently.
+void deriv_axis(Exec& ex, accfft_c_plan* p, int axis, void* out, const void* in, const void* acc) {
+  const long long rr = p->rrow();
+  const int N0 = p->n[0], N1 = p->n[1], N2 = p->n[2];
+  if (axis == 2) {
+    ex.zsym(in, out, acc, rr, make_sym(p, SYM_DERIV1, 1.0 / N2, N2));
+    return;
+  }
+  const long long cr = rr / 2;            // complex pairs per stored row
+  const long long cols = N2 / 2;          // pairs holding data
+  if (axis == 1) {
+    ex.strided_sym(in, out, acc, p->tw_y, N1, (long long)N0 * cols, cols, (long long)N1 * cr, cr,
+                   make_sym(p, SYM_DERIV1, 1.0 / N1, N1));
+  } else {
+    ex.strided_sym(in, out, acc, p->tw_x, N0, (long long)N1 * cols, cols, cr, (long long)N1 * cr,
+                   make_sym(p, SYM_DERIV1, 1.0 / N0, N0));
+  }
+}
+
+}  // namespace
+
+// ================================================================== C ABI
+extern "C" {
+
+const char* accfft_c_last_error(void) { return g_err.c_str(); }
+int accfft_c_version(void) { return 1; }
+int accfft_c_length_supported(int len) { return length_supported(len) ? 1 : 0; }
+unsigned long long accfft_c_kernel_launches(void) { return launch_count(); }
+
+long long accfft_c_dfft_get_local_size(int N0, int N1, int tuple, int isize[3], int istart[3], int real_bytes) {
+  return local_size(N0, N1, tuple, isize, istart, real_bytes);
+}
+long long accfft_c_local_size_dft_r2c(const int n[3], int isize[3], int istart[3], int osize[3], int ostart[3],
+                                      int real_bytes) {
+  return local_size_r2c(n, isize, istart, osize, ostart, real_bytes);
+}
+long long accfft_c_local_size_dft_c2c(const int n[3], int isize[3], int istart[3], int osize[3], int ostart[3],
+                                      int real_bytes) {
+  return local_size_c2c(n, isize, istart, osize, ostart, real_bytes);
+}
+
+accfft_c_plan* accfft_c_plan_dft_3d_r2c_gpu(const int n[3], double* data, double* data_out, unsigned) {
+  return make_plan(1, true, n, data, data_out);
+}
+accfft_c_plan* accfft_c_plan_dft_3d_r2c_gpuf(const int n[3], float* data, float* data_out, unsigned) {
+  return make_plan(1, false, n, data, data_out);
+}
+accfft_c_plan* accfft_c_plan_dft_3d_c2c_gpu(const int n[3], double* data, double* data_out, unsigned) {
+  return make_plan(2, true, n, data, data_out);
+}
+accfft_c_plan* accfft_c_plan_dft_3d_c2c_gpuf(const int n[3], float* data, float* data_out, unsigned) {
+  return make_plan(2, false, n, data, data_out);
+}
+
+void accfft_c_destroy_plan(accfft_c_plan* p) {
+  if (!p) return;
+  if (p->tw_block) cudaFree(p->tw_block);
+  if (p->scratch) cudaFree(p->scratch);
+  if (p->ev0) cudaEventDestroy(p->ev0);
+  if (p->ev1) cudaEventDestroy(p->ev1);
+  delete p;
+}
+
+int accfft_c_plan_info(const accfft_c_plan* p, int n[3], int* kind, int* is_double, int* inplace,
+                       long long* alloc_max) {
+  if (!p) return fail(ACCFFT_C_EINVAL, "plan_info: NULL plan");
+  if (n)
+    for (int i = 0; i < 3; ++i) n[i] = p->n[i];
+  if (kind) *kind = p->kind;
+  if (is_double) *is_double = p->dbl;
+  if (inplace) *inplace = p->inplace;
+  if (alloc_max) *alloc_max = p->alloc_max;
+  return ACCFFT_C_OK;
+}
+
+int accfft_c_set_stream(accfft_c_plan* p, void* stream, int blocking) {
+  if (!p) return fail(ACCFFT_C_EINVAL, "set_stream: NULL plan");
+  p->stream = static_cast<cudaStream_t>(stream);
+  p->blocking = blocking != 0;
+  return ACCFFT_C_OK;
+}
+
+#define AFG_EXEC_R2C(SFX, T, DBL)                                                                        \
+  int accfft_c_execute_r2c_gpu##SFX(accfft_c_plan* p, T* in, T* out, double* timer, unsigned xyz) {     \
+    int rc = check_plan(p, 1, DBL, "execute_r2c");                                                       \
+    return rc ? rc : exec_r2c_plan(p, -1, in, out, timer, xyz);                                          \
+  }                                                                                                      \
+  int accfft_c_execute_c2r_gpu##SFX(accfft_c_plan* p, T* in, T* out, double* timer, unsigned xyz) {     \
+    int rc = check_plan(p, 1, DBL, "execute_c2r");                                                       \
+    return rc ? rc : exec_r2c_plan(p, 1, in, out, timer, xyz);                                           \
+  }                                                                                                      \
+  int accfft_c_execute_gpu##SFX(accfft_c_plan* p, int dir, T* in, T* out, double* timer, unsigned xyz) { \
+    int rc = check_plan(p, 1, DBL, "execute");                                                           \
+    return rc ? rc : exec_r2c_plan(p, dir, in, out, timer, xyz);                                         \
+  }                                                                                                      \
+  int accfft_c_execute_c2c_gpu##SFX(accfft_c_plan* p, int dir, T* in, T* out, double* timer,            \
+                                    unsigned xyz) {                                                      \
+    int rc = check_plan(p, 2, DBL, "execute_c2c");                                                       \
+    return rc ? rc : exec_c2c_plan(p, dir, in, out, timer, xyz);                                         \
+  }
+AFG_EXEC_R2C(, double, 1)
+AFG_EXEC_R2C(f, float, 0)
+#undef AFG_EXEC_R2C
+
+int accfft_c_execute_r2c_axis(accfft_c_plan* p, int axis, const void* in, void* out, double* timer) {
+  int rc = check_plan(p, 1, -1, "execute_r2c_axis");
+  if (rc) return rc;
+  if (!in || !out) return fail(ACCFFT_C_EINVAL, "execute_r2c_axis: NULL array");
+  if (int a = check_align(p, "execute_r2c_axis", {in, out})) return a;
+  if (axis != 2) return fail(ACCFFT_C_EUNSUPPORTED, "execute_r2c_axis: axis %d not available yet", axis);
+  Exec ex(p, timer);
+  ex.zr2c(in, out, p->rrow());
+  return ex.finish();
+}
+int accfft_c_execute_c2r_axis(accfft_c_plan* p, int axis, const void* in, void* out, double* timer) {
+  int rc = check_plan(p, 1, -1, "execute_c2r_axis");
+  if (rc) return rc;
+  if (!in || !out) return fail(ACCFFT_C_EINVAL, "execute_c2r_axis: NULL array");
+  if (int a = check_align(p, "execute_c2r_axis", {in, out})) return a;
+  if (axis != 2) return fail(ACCFFT_C_EUNSUPPORTED, "execute_c2r_axis: axis %d not available yet", axis);
+  Exec ex(p, timer);
+  ex.zc2r(in, out, p->rrow());
+  return ex.finish();
+}
+
+int accfft_c_laplace(accfft_c_plan* p, void* LA, const void* A, double* timer) {
+  int rc = check_plan(p, 1, -1, "laplace");
+  return rc ? rc : op3d(p, SYM_LAPLACE, LA, A, timer);
+}
+int accfft_c_biharmonic(accfft_c_plan* p, void* BA, const void* A, double* timer) {
+  int rc = check_plan(p, 1, -1, "biharmonic");
+  return rc ? rc : op3d(p, SYM_BIHARM, BA, A, timer);
+}
+int accfft_c_inv_laplace(accfft_c_plan* p, void* invLA, const void* A, double* timer) {
+  int rc = check_plan(p, 1, -1, "inv_laplace");
+  return rc ? rc : op3d(p, SYM_INVLAP, invLA, A, timer);
+}
+int accfft_c_inv_biharmonic(accfft_c_plan* p, void* invBA, const void* A, double* timer) {
+  int rc = check_plan(p, 1, -1, "inv_biharmonic");
+  return rc ? rc : op3d(p, SYM_INVBIHARM, invBA, A, timer);
+}
+
+int accfft_c_grad(accfft_c_plan* p, void* A_x, void* A_y, void* A_z, const void* A, unsigned xyz, double* timer) {
+  int rc = check_plan(p, 1, -1, "grad");
+  if (rc) return rc;
+  if (!A || ((xyz & XB) && !A_x) || ((xyz & YB) && !A_y) || ((xyz & ZB) && !A_z))
+    return fail(ACCFFT_C_EINVAL, "grad: NULL array for a selected component");
+  if (int a = check_align(p, "grad", {A_x, A_y, A_z, A})) return a;
+  Exec ex(p, timer);
+  if (xyz & XB) deriv_axis(ex, p, 0, A_x, A, nullptr);
+  if (xyz & YB) deriv_axis(ex, p, 1, A_y, A, nullptr);
+  if (xyz & ZB) deriv_axis(ex, p, 2, A_z, A, nullptr);
+  return ex.finish();
+}
+
+int accfft_c_grad_slow(accfft_c_plan* p, void* A_x, void* A_y, void* A_z, const void* A, unsigned xyz,
+                       double* timer) {
+  int rc = check_plan(p, 1, -1, "grad_slow");
+  if (rc) return rc;
+  if (!A || ((xyz & XB) && !A_x) || ((xyz & YB) && !A_y) || ((xyz & ZB) && !A_z))
+    return fail(ACCFFT_C_EINVAL, "grad_slow: NULL array for a selected component");
+  const int kinds[3] = {SYM_GRADX, SYM_GRADY, SYM_GRADZ};
+  void* outs[3] = {A_x, A_y, A_z};
+  for (int j = 0; j < 3; ++j)
+    if (xyz & (1u << j)) {
+      rc = op3d(p, kinds[j], outs[j], A, timer);
+      if (rc) return rc;
+    }
+  return ACCFFT_C_OK;
+}
+
+int accfft_c_divergence(accfft_c_plan* p, void* divA, const void* A_x, const void* A_y, const void* A_z,
+                        double* timer) {
+  int rc = check_plan(p, 1, -1, "divergence");
+  if (rc) return rc;
+  if (!divA || !A_x || !A_y || !A_z) return fail(ACCFFT_C_EINVAL, "divergence: NULL array");
+  if (int a = check_align(p, "divergence", {divA, A_x, A_y, A_z})) return a;
+  Exec ex(p, timer);
+  deriv_axis(ex, p, 0, divA, A_x, nullptr);
+  deriv_axis(ex, p, 1, divA, A_y, divA);
+  deriv_axis(ex, p, 2, divA, A_z, divA);
+  return ex.finish();
+}
+
+int accfft_c_divergence_slow(accfft_c_plan* p, void* divA, const void* A_x, const void* A_y, const void* A_z,
+                             double* timer) {
+  return accfft_c_divergence(p, divA, A_x, A_y, A_z, timer);
+}
+
+}  // extern "C"

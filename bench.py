@@ -1,0 +1,339 @@
+"""Benchmark: 512^3 FP32 r2c + c2r round trips (pairs/s) on one GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--n 512]
+
+A step is one r2c + c2r pair of the 512^3 float32 field through the C ABI:
+forward z, y, x passes then inverse x, y, z passes, each pass issued by the
+public execute call with its xyz bit (AccFFT's std::bitset<3> argument), so
+every kernel is bracketed by CUDA events on the plan's stream.  Inputs
+(537 MB) exceed the 129 MB L2, so no flush is needed between steps.
+
+value   pairs/s with the field resident in HBM (max time over ranks)
+e2e     pairs/s through accfft_c_execute_r2c_gpuf / _c2r_gpuf with the field
+        copied host->device (pinned) before and the result device->host after
+        every step
+roofline  the dominant kernel's algorithmic bytes per launch / its mean
+        CUDA-event duration, against MEASURED_PEAKS.json's hbm_gbs
+cpu_baseline  the oracle (CPU restatement of the reference's FFTW path,
+        double) on the host cores over a proportional sample
+
+--impl reference times that CPU path alone (the reference cannot run here:
+its GPU and CPU paths need MPI and FFTW, absent on this image).
+
+Under torchrun (N > 1) every rank runs an independent replica: the path has
+no exchange step at P = 1, so there is no collective.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=512)
+    ap.add_argument("--dtype", default="float32", choices=["float32", "float64"])
+    ap.add_argument("--no-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def algorithmic_bytes(n, esz):
+    """Per-launch bytes of each pass (each pass reads and writes its array once)."""
+    N = n[0] * n[1] * n[2]
+    H = n[0] * n[1] * (n[2] // 2 + 1)
+    c = 2 * esz
+    return {
+        "z_r2c": N * esz + H * c,
+        "y_fwd": 2 * H * c,
+        "x_fwd": 2 * H * c,
+        "x_inv": 2 * H * c,
+        "y_inv": 2 * H * c,
+        "z_c2r": H * c + N * esz,
+    }
+
+
+KERNEL_OF = {"z_r2c": "k_zr2c", "y_fwd": "k_strided (y)", "x_fwd": "k_strided (x)",
+             "x_inv": "k_strided (x)", "y_inv": "k_strided (y)", "z_c2r": "k_zc2r"}
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, index):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(index), f"--query-gpu={q}",
+                                       "--format=csv,noheader,nounits", "-lms", "100"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return None
+        self.p.terminate()
+        self.p.wait()
+        self.f.seek(0)
+        rows = [r.split(",") for r in self.f.read().strip().splitlines() if r.strip()]
+        os.unlink(self.f.name)
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[0]))
+                mx = float(r[1])
+                for nm, v in zip(names, r[4:8]):
+                    if v.strip() == "Active":
+                        reasons.add(nm)
+            except (ValueError, IndexError):
+                continue
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        return float(json.load(open(p))["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def cpu_pairs_per_s(n, budget_s=20.0, nthreads=0):
+    """Oracle r2c + c2r (double, all host threads) on a proportional sample:
+    complete z rows, y lines and x lines of a fraction f of the grid.
+    Returns (pairs/s, sample description, threads)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import accfft_oracle as orc
+
+    orc.build()
+    th = nthreads or (os.cpu_count() or 1)
+    rng = np.random.default_rng(7)
+    N0, N1, N2 = n
+    H2 = N2 // 2 + 1
+
+    def run(f):
+        k0 = max(1, int(round(N0 * f)))
+        k1 = max(1, int(round(N1 * f)))
+        u = rng.standard_normal((k0, N1, N2))
+        s = rng.standard_normal((k0, N1, H2)) + 1j * rng.standard_normal((k0, N1, H2))
+        sx = rng.standard_normal((N0, k1, H2)) + 1j * rng.standard_normal((N0, k1, H2))
+        t = time.perf_counter()
+        orc.r2c_z(u, nthreads=th)                          # z forward on k0*N1 rows
+        orc.c2c_axis(s, 1, -1, nthreads=th)                # y forward on k0*H2 lines
+        orc.c2c_axis(sx, 0, -1, nthreads=th)               # x forward on k1*H2 lines
+        orc.c2c_axis(sx, 0, +1, nthreads=th)
+        orc.c2c_axis(s, 1, +1, nthreads=th)
+        orc.c2r_z(s, N2, nthreads=th)
+        dt = time.perf_counter() - t
+        frac = (k0 / N0 + k0 / N0 + k1 / N1 + k1 / N1 + k0 / N0 + k0 / N0) / 6
+        return dt, frac
+
+    dt, frac = run(1.0 / 64)
+    est = dt / frac
+    f = min(1.0, max(1.0 / 64, budget_s / max(est, 1e-9)))
+    dt, frac = run(f)
+    pairs = frac / dt
+    return pairs, f"{frac:.4f} of one {N0}x{N1}x{N2} pair (complete lines of each pass), double, {th} threads", th
+
+
+def reference_arm(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    n = (args.n,) * 3
+    per_step = max(2.0, 150.0 / max(1, args.steps + args.warmup))
+    vals = []
+    for i in range(args.warmup + args.steps):
+        v, sample, th = cpu_pairs_per_s(n, budget_s=per_step)
+        if i >= args.warmup:
+            vals.append(v)
+    value = statistics.median(vals)
+    line = {
+        "impl": "reference", "metric": f"{args.n}^3 r2c+c2r pairs/s", "value": value, "unit": "pairs/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / value,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic N(0,1), seeded",
+        "config": {"workload": f"{args.n}^3 r2c+c2r round trip", "grid": list(n), "flush": "inputs_larger_than_l2"},
+        "cpu_baseline": {"value": value, "unit": "pairs/s", "cores": th, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": "pairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "oracle port of the reference's FFTW CPU path (FFTW and MPI are absent on this image)",
+    }
+    print(json.dumps(line), flush=True)
+
+
+def ours(args):
+    import torch
+
+    import accfft_gb300 as ag
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    n = (args.n,) * 3
+    dt = args.dtype
+    esz = 4 if dt == "float32" else 8
+    tdt = getattr(torch, dt)
+    N0, N1, N2 = n
+    H2 = N2 // 2 + 1
+    plan = ag.PlanR2C(n, dt)
+    stream = torch.cuda.Stream()
+    plan.set_stream(stream, blocking=False)
+    g = torch.Generator(device="cuda").manual_seed(1234 + rank)
+    u = torch.randn(n, dtype=tdt, device="cuda", generator=g)
+    spec = torch.empty((N0, N1, H2, 2), dtype=tdt, device="cuda")
+    back = torch.empty(n, dtype=tdt, device="cuda")
+    passes = ["z_r2c", "y_fwd", "x_fwd", "x_inv", "y_inv", "z_c2r"]
+
+    def step(evs=None):
+        calls = [
+            lambda: plan.r2c(u, spec, xyz=4),
+            lambda: plan.r2c(spec, spec, xyz=2),
+            lambda: plan.r2c(spec, spec, xyz=1),
+            lambda: plan.c2r(spec, spec, xyz=1),
+            lambda: plan.c2r(spec, spec, xyz=2),
+            lambda: plan.c2r(spec, back, xyz=4),
+        ]
+        for i, c in enumerate(calls):
+            if evs is not None:
+                evs[i][0].record(stream)
+            c()
+            if evs is not None:
+                evs[i][1].record(stream)
+
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            step()
+    stream.synchronize()
+    # correctness gate on the benchmarked buffers: round trip returns N*u
+    err = (back / (N0 * N1 * N2) - u).norm().item() / u.norm().item()
+    assert err < (1e-5 if dt == "float32" else 1e-12), err
+
+    evs = [[[torch.cuda.Event(enable_timing=True) for _ in range(2)] for _ in passes] for _ in range(args.steps)]
+    launches0 = ag.kernel_launches()
+    clk = Clocks(torch.cuda.current_device()) if rank == 0 else None
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    t0.record(stream)
+    for k in range(args.steps):
+        step(evs[k])
+    t1.record(stream)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    clocks = clk.stop() if clk else None
+    launches = ag.kernel_launches() - launches0
+    total_ms = t0.elapsed_time(t1)
+    if world > 1:
+        tt = torch.tensor([total_ms], device="cuda")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        total_ms = tt.item()
+    ms_step = total_ms / args.steps
+    value = world * args.steps / (total_ms / 1000.0)
+
+    per = {p: statistics.mean(evs[k][i][0].elapsed_time(evs[k][i][1]) for k in range(args.steps))
+           for i, p in enumerate(passes)}
+    nbytes = algorithmic_bytes(n, esz)
+    dom = max(per, key=per.get)
+    peak, peak_kind = measured_peak()
+    achieved = nbytes[dom] / (per[dom] / 1000.0) / 1e9
+    step_bytes = sum(nbytes.values())
+
+    # end to end through the public calls with host buffers
+    hu = torch.empty(n, dtype=tdt).pin_memory()
+    hu.copy_(u.cpu())
+    hb = torch.empty(n, dtype=tdt).pin_memory()
+    plan2 = ag.PlanR2C(n, dt)
+    plan2.set_stream(stream, blocking=False)
+    du = torch.empty(n, dtype=tdt, device="cuda")
+
+    def e2e_step():
+        du.copy_(hu, non_blocking=True)
+        plan2.r2c(du, spec)
+        plan2.c2r(spec, back)
+        hb.copy_(back, non_blocking=True)
+
+    with torch.cuda.stream(stream):
+        for _ in range(max(1, args.warmup)):
+            e2e_step()
+        stream.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        ksteps = max(3, args.steps // 2)
+        e0.record(stream)
+        for _ in range(ksteps):
+            e2e_step()
+        e1.record(stream)
+    stream.synchronize()
+    e2e_ms = e0.elapsed_time(e1) / ksteps
+    e2e_val = world * 1000.0 / e2e_ms
+    assert torch.allclose(hb, back.cpu())
+
+    if rank != 0:
+        return
+    line = {
+        "metric": f"{args.n}^3 r2c+c2r pairs/s", "value": value, "unit": "pairs/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32" if dt == "float32" else "f64",
+        "data": "synthetic N(0,1), seeded",
+        "config": {"workload": f"{args.n}^3 {dt} r2c+c2r round trip", "grid": list(n),
+                   "flush": "inputs_larger_than_l2", "parallelism": f"replicas{world}"},
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "hbm", "kernel": KERNEL_OF[dom], "pass": dom, "achieved": achieved, "peak": peak,
+                     "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": None, "bytes_per_launch": nbytes[dom], "ms_per_launch": per[dom]},
+        "passes_ms": per,
+        "step_algorithmic_GBps": step_bytes / (ms_step / 1000.0) / 1e9,
+        "gflops_5nlogn": 5 * N0 * N1 * N2 * np.log2(N0 * N1 * N2) / (ms_step / 1000.0) / 1e9,
+        "e2e": {"value": e2e_val, "unit": "pairs/s", "h2d_bytes_per_step": int(hu.numel() * esz),
+                "d2h_bytes_per_step": int(hb.numel() * esz)},
+        "clocks": clocks,
+        "roundtrip_rel_l2": err,
+    }
+    if not args.no_baseline and world == 1:
+        v, sample, th = cpu_pairs_per_s(n)
+        line["cpu_baseline"] = {"value": v, "unit": "pairs/s", "cores": th, "kind": "port", "sample": sample}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        reference_arm(args)
+    else:
+        ours(args)
+
+
+if __name__ == "__main__":
+    main()

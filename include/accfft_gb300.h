@@ -1,0 +1,135 @@
+/*
+ * accfft_gb300.h - C ABI of the GB300-native AccFFT single-GPU path.
+ *
+ * Every entry point takes plain pointers and sizes (no C++ or framework types)
+ * so it can be bound from C, ctypes, cgo or JNI.  The C++ API that mirrors
+ * AccFFT's own headers (accfft_gpu.h, accfft_gpuf.h, accfft_operators_gpu.h)
+ * is a thin layer over these functions.
+ *
+ * Conventions shared by all entry points
+ *   - Grids are row-major [N0][N1][N2] (x slowest, z fastest); one process,
+ *     one GPU, an MPI communicator of size one.
+ *   - r2c spectra are [N0][N1][N2/2+1] complex (interleaved re, im), c2c data
+ *     is [N0][N1][N2] complex.  An r2c plan is in place when data == data_out
+ *     (non-NULL) at plan time; its real arrays then use rows padded to
+ *     2*(N2/2+1).  Two NULL plan-time pointers make an out-of-place plan.
+ *   - Transforms are unnormalised: c2r(r2c(u)) = N0*N1*N2 * u.
+ *   - xyz is AccFFT's std::bitset<3> as an integer: bit 0 = x, bit 1 = y,
+ *     bit 2 = z; 7 selects all axes.
+ *   - timer (may be NULL) points to AccFFT's 5-slot timer; slot 4 accumulates
+ *     the device time of the transform in seconds, the others are untouched.
+ *   - Functions returning int return ACCFFT_C_OK (0) or an ACCFFT_C_E* code;
+ *     accfft_c_last_error() describes the last failure of the calling thread.
+ *   - By default every call blocks until the GPU work is done (AccFFT's
+ *     contract).  accfft_c_set_stream() makes a plan enqueue asynchronously.
+ *   - Plans are not thread-safe (one plan, one host thread at a time).
+ */
+#ifndef ACCFFT_GB300_H
+#define ACCFFT_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ACCFFT_C_OK 0
+#define ACCFFT_C_EINVAL 1        /* invalid argument (NULL plan/pointer, bad size, wrong precision) */
+#define ACCFFT_C_EUNSUPPORTED 2  /* an axis length without compiled kernels */
+#define ACCFFT_C_ECUDA 3         /* CUDA runtime error (allocation, launch, execution) */
+#define ACCFFT_C_ENOTBAKED 4     /* plan was not made for this transform kind */
+#define ACCFFT_C_EOVERFLOW 5     /* a size does not fit the reference's int interface */
+
+typedef struct accfft_c_plan accfft_c_plan; /* opaque */
+
+/* --- library --------------------------------------------------------- */
+const char* accfft_c_last_error(void);
+int accfft_c_version(void);
+/* 1 if an axis of this length has compiled kernels (complex length for
+ * c2c axes; for the real z axis of an r2c plan the check is on N2/2) */
+int accfft_c_length_supported(int len);
+/* kernels launched by this process through the library (for audits) */
+unsigned long long accfft_c_kernel_launches(void);
+
+/* --- local sizes ------------------------------------------------------
+ * Replaces dfft_get_local_size_t (src/accfft_common.cpp:49-91),
+ * accfft_local_size_dft_r2c_t (src/accfft_common.cpp:98-192) and
+ * accfft_local_size_dft_c2c_t (src/accfft_common.cpp:203-256) at P = 1.
+ * real_bytes is sizeof(double) or sizeof(float).  The return value is the
+ * byte count the reference would return (alloc_max), as 64-bit. */
+long long accfft_c_dfft_get_local_size(int N0, int N1, int tuple, int isize[3], int istart[3],
+                                       int real_bytes);
+long long accfft_c_local_size_dft_r2c(const int n[3], int isize[3], int istart[3], int osize[3],
+                                      int ostart[3], int real_bytes);
+long long accfft_c_local_size_dft_c2c(const int n[3], int isize[3], int istart[3], int osize[3],
+                                      int ostart[3], int real_bytes);
+
+/* --- plans ------------------------------------------------------------
+ * Replace accfft_plan_dft_3d_r2c_gpu (src/accfft_gpu.cpp:77-442),
+ * accfft_plan_dft_3d_c2c_gpu (src/accfft_gpu.cpp:704-931) and their float
+ * twins (src/accfft_gpuf.cpp:74, :697).  Return NULL on failure. */
+accfft_c_plan* accfft_c_plan_dft_3d_r2c_gpu(const int n[3], double* data, double* data_out, unsigned flags);
+accfft_c_plan* accfft_c_plan_dft_3d_r2c_gpuf(const int n[3], float* data, float* data_out, unsigned flags);
+accfft_c_plan* accfft_c_plan_dft_3d_c2c_gpu(const int n[3], double* data, double* data_out, unsigned flags);
+accfft_c_plan* accfft_c_plan_dft_3d_c2c_gpuf(const int n[3], float* data, float* data_out, unsigned flags);
+/* Replaces accfft_destroy_plan_gpu (src/accfft_gpu.cpp:1142-1192); frees the plan itself too. */
+void accfft_c_destroy_plan(accfft_c_plan* plan);
+/* kind: 1 = r2c, 2 = c2c; is_double: 1 for the double plans */
+int accfft_c_plan_info(const accfft_c_plan* plan, int n[3], int* kind, int* is_double, int* inplace,
+                       long long* alloc_max);
+/* extension: enqueue on `stream` (a cudaStream_t); blocking = 0 returns
+ * without waiting (timer slots are then not updated) */
+int accfft_c_set_stream(accfft_c_plan* plan, void* stream, int blocking);
+
+/* --- transforms -------------------------------------------------------
+ * Replace accfft_execute_r2c_gpu (src/accfft_gpu.cpp:635-649),
+ * accfft_execute_c2r_gpu (:661-675), accfft_execute_gpu (:444-623),
+ * accfft_execute_c2c_gpu (:943-1136) and the float twins
+ * (src/accfft_gpuf.cpp:443, :632, :656, :935).  NULL data pointers select
+ * the pointers given at plan time.  Unlike the reference, an out-of-place
+ * c2r or backward c2c leaves its input unchanged. */
+int accfft_c_execute_r2c_gpu(accfft_c_plan* plan, double* data, double* data_out, double* timer, unsigned xyz);
+int accfft_c_execute_c2r_gpu(accfft_c_plan* plan, double* data, double* data_out, double* timer, unsigned xyz);
+int accfft_c_execute_gpu(accfft_c_plan* plan, int direction, double* data, double* data_out, double* timer,
+                         unsigned xyz);
+int accfft_c_execute_c2c_gpu(accfft_c_plan* plan, int direction, double* data, double* data_out, double* timer,
+                             unsigned xyz);
+int accfft_c_execute_r2c_gpuf(accfft_c_plan* plan, float* data, float* data_out, double* timer, unsigned xyz);
+int accfft_c_execute_c2r_gpuf(accfft_c_plan* plan, float* data, float* data_out, double* timer, unsigned xyz);
+int accfft_c_execute_gpuf(accfft_c_plan* plan, int direction, float* data, float* data_out, double* timer,
+                          unsigned xyz);
+int accfft_c_execute_c2c_gpuf(accfft_c_plan* plan, int direction, float* data, float* data_out, double* timer,
+                              unsigned xyz);
+
+/* Single-axis real transforms, replacing accfft_execute_{r2c,c2r}_{z,y,x}_gpu_t
+ * (src/accfft_gpu.cpp:1212-1604; float src/accfft_gpuf.cpp:1197-1572).
+ * Spectrum layouts: z -> [N0][N1][N2/2+1], y -> [N0][N1/2+1][N2],
+ * x -> [N0/2+1][N1][N2].  axis: 0 = x, 1 = y, 2 = z.  Double plans take
+ * double arrays, float plans float arrays (passed as void*). */
+int accfft_c_execute_r2c_axis(accfft_c_plan* plan, int axis, const void* data, void* data_out, double* timer);
+int accfft_c_execute_c2r_axis(accfft_c_plan* plan, int axis, const void* data, void* data_out, double* timer);
+
+/* --- spectral operators (r2c plans) -----------------------------------
+ * Replace accfft_{grad,laplace,divergence,biharmonic}_gpu[f]
+ * (src/operators_gpu.cpp:85-135, src/operators_gpu.txx:72-609,
+ * src/operators_gpuf.cpp:93-143).  inv_laplace and inv_biharmonic have no
+ * GPU version in the reference; they follow the CPU kernels
+ * mult_wave_number_inv_laplace (src/operators.txx:276-333) and
+ * mult_wave_number_inv_biharmonic (src/operators.txx:336-388).
+ * Arrays have the plan's precision and real layout.  grad's xyz selects the
+ * components (NULL outputs are allowed for unselected ones). */
+int accfft_c_grad(accfft_c_plan* plan, void* A_x, void* A_y, void* A_z, const void* A, unsigned xyz, double* timer);
+int accfft_c_grad_slow(accfft_c_plan* plan, void* A_x, void* A_y, void* A_z, const void* A, unsigned xyz,
+                       double* timer);
+int accfft_c_laplace(accfft_c_plan* plan, void* LA, const void* A, double* timer);
+int accfft_c_divergence(accfft_c_plan* plan, void* divA, const void* A_x, const void* A_y, const void* A_z,
+                        double* timer);
+int accfft_c_divergence_slow(accfft_c_plan* plan, void* divA, const void* A_x, const void* A_y, const void* A_z,
+                             double* timer);
+int accfft_c_biharmonic(accfft_c_plan* plan, void* BA, const void* A, double* timer);
+int accfft_c_inv_laplace(accfft_c_plan* plan, void* invLA, const void* A, double* timer);
+int accfft_c_inv_biharmonic(accfft_c_plan* plan, void* invBA, const void* A, double* timer);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ACCFFT_GB300_H */

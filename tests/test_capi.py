@@ -1,0 +1,80 @@
+"""C ABI checks that need no GPU: the library loads, exports every symbol the
+header declares, answers the local-size queries like the reference, and turns
+bad plans into errors instead of crashes."""
+import ctypes
+import subprocess
+
+import pytest
+
+
+def test_exports_every_declared_symbol(native):
+    L = native.lib()
+    names = native.header_symbols()
+    assert len(names) >= 30
+    missing = [n for n in names if not hasattr(L, n)]
+    assert not missing, missing
+
+
+def test_library_is_sm103a_and_exports_cabi(native):
+    out = subprocess.run(["nm", "-D", "--defined-only", native.LIB_PATH], capture_output=True, text=True).stdout
+    for n in native.header_symbols():
+        assert f" T {n}" in out, n
+
+
+def ref_local_size_r2c(n, rb):
+    """accfft_local_size_dft_r2c_t (src/accfft_common.cpp:98-192) at P = 1."""
+    nt = (n[2] // 2 + 1) * 2
+    amax = max(n[0] * n[1] * nt * rb,
+               2 * n[0] * (nt // 2) * n[1] * rb,
+               2 * n[1] * (nt // 2) * n[0] * rb,
+               n[0] * n[2] * n[1] * rb,
+               2 * n[0] * n[2] * (n[1] // 2 + 1) * rb,
+               n[0] * n[1] * n[2] * rb,
+               2 * (n[0] // 2 + 1) * n[1] * n[2] * rb)
+    return amax, (n[0], n[1], n[2]), (n[0], n[1], n[2] // 2 + 1)
+
+
+@pytest.mark.parametrize("n", [(128, 128, 128), (512, 512, 512), (160, 180, 200), (1024, 1024, 1024), (5, 9, 4)])
+@pytest.mark.parametrize("rb", [4, 8])
+def test_local_size_r2c(native, n, rb):
+    amax, isz, ist, osz, ost = native.local_size_r2c(n, rb)
+    ramax, risz, rosz = ref_local_size_r2c(n, rb)
+    assert (amax, isz, osz) == (ramax, risz, rosz)
+    assert ist == (0, 0, 0) and ost == (0, 0, 0)
+
+
+def test_local_size_known_values(native):
+    # figures quoted for the reference's configurations
+    assert native.local_size_r2c((128, 128, 128), 8)[0] == 17_039_360
+    assert native.local_size_r2c((512, 512, 512), 8)[0] == 1_077_936_128
+    assert native.local_size_r2c((1024, 1024, 1024), 4)[0] == 4_303_355_904   # beyond int: 64-bit here
+    assert native.local_size_c2c((512, 512, 512), 8)[0] == 2_147_483_648
+    assert native.local_size_c2c((256, 256, 256), 8)[0] == 268_435_456
+
+
+def test_supported_lengths(native):
+    L = native.lib()
+    for n in (1, 2, 4, 8, 16, 32, 64, 128, 256, 512, 1024, 48, 90, 96, 100, 160, 180, 192, 200):
+        assert L.accfft_c_length_supported(n) == 1, n
+    for n in (7, 11, 13, 17, 1000003):
+        assert L.accfft_c_length_supported(n) == 0, n
+
+
+def test_plan_rejects_bad_sizes(native):
+    L = native.lib()
+    n = (ctypes.c_int * 3)(8, 8, 7)
+    assert not L.accfft_c_plan_dft_3d_r2c_gpuf(n, None, None, 2)
+    assert "even N2" in native.last_error()
+    n = (ctypes.c_int * 3)(8, 13, 8)
+    assert not L.accfft_c_plan_dft_3d_c2c_gpu(n, None, None, 2)
+    assert "length 13" in native.last_error()
+    n = (ctypes.c_int * 3)(0, 8, 8)
+    assert not L.accfft_c_plan_dft_3d_r2c_gpu(n, None, None, 2)
+
+
+def test_null_plan_is_an_error(native):
+    L = native.lib()
+    rc = L.accfft_c_execute_r2c_gpu(None, None, None, None, 7)
+    assert rc == native.EINVAL
+    assert "NULL plan" in native.last_error()
+    assert L.accfft_c_laplace(None, None, None, None) == native.EINVAL

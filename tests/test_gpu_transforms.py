@@ -1,0 +1,145 @@
+"""Parity of the CUDA transforms with the oracle, through the C ABI.
+
+Tolerances (relative L2 against the oracle computed in double from the same
+inputs): 1e-12 for double plans, 1e-5 for float plans (the float result is
+also stated against the double oracle)."""
+import numpy as np
+import pytest
+
+from conftest import rng
+
+pytestmark = pytest.mark.gpu
+
+TOL = {"float64": 1e-12, "float32": 1e-5}
+
+R2C_SHAPES = [(4, 6, 8), (8, 8, 8), (16, 12, 10), (5, 9, 4), (32, 64, 16), (48, 96, 64), (64, 32, 128),
+              (128, 128, 128), (90, 100, 180), (160, 180, 200), (256, 256, 256), (200, 192, 96)]
+C2C_SHAPES = [(4, 6, 8), (8, 8, 8), (9, 5, 6), (16, 12, 10), (48, 96, 64), (128, 128, 128), (160, 180, 200),
+              (256, 128, 64)]
+
+
+def to_dev(torch, a, dtype):
+    if np.iscomplexobj(a):
+        a = np.ascontiguousarray(np.stack([a.real, a.imag], axis=-1))
+    return torch.from_numpy(np.ascontiguousarray(a).astype(dtype)).cuda()
+
+
+def from_dev(t, cplx=False):
+    a = t.cpu().numpy().astype(np.float64)
+    if cplx:
+        a = a[..., 0] + 1j * a[..., 1]
+    return a
+
+
+def empty(torch, shape, dtype):
+    return torch.empty(shape, dtype=getattr(torch, dtype), device="cuda")
+
+
+@pytest.mark.parametrize("dtype", ["float64", "float32"])
+@pytest.mark.parametrize("n", R2C_SHAPES)
+def test_r2c_c2r(cuda, native, oracle, n, dtype):
+    torch = cuda
+    u = rng(10).standard_normal(n)
+    plan = native.PlanR2C(n, dtype)
+    du = to_dev(torch, u, dtype)
+    dh = empty(torch, (n[0], n[1], n[2] // 2 + 1, 2), dtype)
+    plan.r2c(du, dh)
+    ref = oracle.r2c(u.astype(dtype).astype(np.float64))
+    assert oracle.rel_l2(from_dev(dh, True), ref) < TOL[dtype]
+    # c2r of an arbitrary (non-Hermitian-consistent) half spectrum
+    h = rng(11).standard_normal(ref.shape) + 1j * rng(12).standard_normal(ref.shape)
+    dh2 = to_dev(torch, h, dtype)
+    keep = dh2.clone()
+    db = empty(torch, n, dtype)
+    plan.c2r(dh2, db)
+    refb = oracle.c2r(from_dev(keep, True), n[2])
+    assert oracle.rel_l2(from_dev(db), refb) < TOL[dtype]
+    assert torch.equal(dh2, keep), "out-of-place c2r must leave its input unchanged"
+    plan.destroy()
+
+
+@pytest.mark.parametrize("dtype", ["float64", "float32"])
+@pytest.mark.parametrize("n", C2C_SHAPES)
+def test_c2c(cuda, native, oracle, n, dtype):
+    torch = cuda
+    r = rng(20)
+    d = r.standard_normal(n) + 1j * r.standard_normal(n)
+    plan = native.PlanC2C(n, dtype)
+    dd = to_dev(torch, d, dtype)
+    keep = dd.clone()
+    do = empty(torch, n + (2,), dtype)
+    dq = from_dev(keep, True)
+    for direction in (-1, 1):
+        plan.c2c(direction, dd, do)
+        assert oracle.rel_l2(from_dev(do, True), oracle.c2c(dq, direction)) < TOL[dtype]
+        assert torch.equal(dd, keep)
+    plan.destroy()
+
+
+@pytest.mark.parametrize("dtype", ["float64", "float32"])
+def test_r2c_inplace_padded(cuda, native, oracle, dtype):
+    """In-place plan (data == data_out): rows padded to 2*(N2/2+1) as in
+    steps/step2/step2_gpu.cpp:40-72; round trip returns N*u."""
+    torch = cuda
+    n = (32, 24, 40)
+    u = rng(30).standard_normal(n)
+    pad = oracle.pad_rows(u)
+    d = to_dev(torch, pad, dtype)
+    plan = native.PlanR2C(n, dtype, data=d, data_out=d)
+    assert plan.inplace
+    plan.r2c(d, d)
+    s = from_dev(d.view(n[0], n[1], n[2] // 2 + 1, 2), True)
+    assert oracle.rel_l2(s, oracle.r2c(u.astype(dtype).astype(np.float64))) < TOL[dtype]
+    plan.c2r(d, d)
+    back = from_dev(d)[:, :, :n[2]] / np.prod(n)
+    assert oracle.rel_l2(back, u) < TOL[dtype]
+
+
+@pytest.mark.parametrize("dtype", ["float64", "float32"])
+@pytest.mark.parametrize("xyz", [1, 2, 3, 4, 5, 6])
+def test_partial_axes(cuda, native, oracle, dtype, xyz):
+    """xyz bitsets: the selected passes only (with z skipped the remaining
+    passes transform the input array in place, as the reference does)."""
+    torch = cuda
+    n = (16, 12, 20)
+    h = (n[0], n[1], n[2] // 2 + 1)
+    plan = native.PlanR2C(n, dtype)
+    if xyz & 4:
+        u = rng(40).standard_normal(n)
+        du = to_dev(torch, u, dtype)
+        dh = empty(torch, h + (2,), dtype)
+        plan.r2c(du, dh, xyz=xyz)
+        got = from_dev(dh, True)
+        ref = oracle.r2c(u.astype(dtype).astype(np.float64), xyz)
+    else:
+        c = rng(41).standard_normal(h) + 1j * rng(42).standard_normal(h)
+        dc = to_dev(torch, c, dtype)
+        q = from_dev(dc, True)
+        plan.r2c(dc, empty(torch, h + (2,), dtype), xyz=xyz)
+        got = from_dev(dc, True)
+        ref = oracle.r2c(q, xyz)
+    assert oracle.rel_l2(got, ref) < TOL[dtype]
+
+
+@pytest.mark.parametrize("dtype", ["float64", "float32"])
+def test_timer_slot4_accumulates(cuda, native, dtype):
+    torch = cuda
+    n = (64, 64, 64)
+    plan = native.PlanR2C(n, dtype)
+    du = torch.randn(n, dtype=getattr(torch, dtype), device="cuda")
+    dh = empty(torch, (64, 64, 33, 2), dtype)
+    timer = [0.0] * 5
+    plan.r2c(du, dh, timer=timer)
+    plan.r2c(du, dh, timer=timer)
+    assert timer[4] > 0 and timer[:4] == [0.0] * 4
+
+
+def test_kernel_launch_counter(cuda, native):
+    torch = cuda
+    n = (32, 32, 32)
+    plan = native.PlanR2C(n, "float32")
+    du = torch.randn(n, device="cuda")
+    dh = torch.empty((32, 32, 17, 2), device="cuda")
+    before = native.kernel_launches()
+    plan.r2c(du, dh)
+    assert native.kernel_launches() - before == 3      # z, y and x passes
