@@ -41,10 +41,10 @@ typedef double Real;
 
 namespace afg {
 
+// opt-in to more than 48 KB of dynamic shared memory; `done` lives in the
+// caller's per-kernel instantiation
 template <typename K>
-static void prepare(K kernel, size_t smem) {
-  // per-instantiation one-time opt-in to large dynamic shared memory
-  static bool done = false;
+static void prepare(K kernel, size_t smem, bool& done) {
   if (!done) {
     if (smem > 48 * 1024) cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
     done = true;
@@ -56,7 +56,8 @@ template <int L, int MODE>
 static void run_strided(const StridedArgs& a, cudaStream_t s) {
   typedef StridedShape<Real, L> SH;
   auto k = k_strided<Real, L, MODE>;
-  prepare(k, SH::smem);
+  static bool done = false;
+  prepare(k, SH::smem, done);
   unsigned grid = unsigned((a.ncols + SH::TC - 1) / SH::TC);
   k<<<grid, SH::threads, SH::smem, s>>>(a);
   count_launch();
@@ -86,7 +87,8 @@ static void run_contig(const ContigArgs& a, cudaStream_t s) {
 #else
   auto k = k_zsym<Real, L>;
 #endif
-  prepare(k, SH::smem);
+  static bool done = false;
+  prepare(k, SH::smem, done);
   unsigned grid = unsigned((a.nlines + SH::TL - 1) / SH::TL);
   k<<<grid, SH::threads, SH::smem, s>>>(a);
   count_launch();
