@@ -92,6 +92,7 @@ def lib() -> ctypes.CDLL:
         "accfft_c_biharmonic": ([vp, vp, vp, dp], i),
         "accfft_c_inv_laplace": ([vp, vp, vp, dp], i),
         "accfft_c_inv_biharmonic": ([vp, vp, vp, dp], i),
+        "accfft_c_laplace_gpuf_noalloc": ([ip, vp, vp, vp], i),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)

@@ -93,6 +93,11 @@ def build(verbose: bool = False, jobs: int | None = None) -> str:
         obj = os.path.join(OBJ, name.replace(".cpp", ".o"))
         cmd = ["g++", *CXX_FLAGS, "-I", cuda_inc, "-c", src, "-o", obj]
         work.append((src, obj, cmd, _digest([src] + hdrs, cmd[1:])))
+    for name in ("noalloc.cu",):
+        src = os.path.join(CSRC, name)
+        obj = os.path.join(OBJ, name.replace(".cu", ".o"))
+        cmd = [nvcc, *NVCC_FLAGS, "-c", src, "-o", obj]
+        work.append((src, obj, cmd, _digest([src] + hdrs, cmd[1:])))
     # heaviest translation units first
     work.sort(key=lambda w: ("_k0_" not in w[1], "_g1" not in w[1]))
     n = jobs or max(1, os.cpu_count() or 1)

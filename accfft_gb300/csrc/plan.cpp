@@ -493,6 +493,11 @@ void deriv_axis(Exec& ex, accfft_c_plan* p, int axis, void* out, const void* in,
 
 }  // namespace
 
+namespace afg {
+// lets other translation units of the library report through accfft_c_last_error
+void set_last_error(int code, const char* msg) { fail(code, "%s", msg); }
+}  // namespace afg
+
 // ================================================================== C ABI
 extern "C" {
 

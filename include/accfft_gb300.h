@@ -128,6 +128,22 @@ int accfft_c_biharmonic(accfft_c_plan* plan, void* BA, const void* A, double* ti
 int accfft_c_inv_laplace(accfft_c_plan* plan, void* invLA, const void* A, double* timer);
 int accfft_c_inv_biharmonic(accfft_c_plan* plan, void* invBA, const void* A, double* timer);
 
+/* --- Laplacian without device allocation ------------------------------
+ * No counterpart in the reference.  For callers that may not call cudaMalloc
+ * (a plugin in an application whose memory manager has reserved the whole
+ * device, a latency-bound loop where an allocation could stall the GPU) and
+ * therefore cannot create a plan.  Computes the same result as
+ * accfft_c_laplace with a float r2c plan on out-of-place [N0][N1][N2] arrays
+ * (N2 even), using a library-owned array of 64 MiB per device instead of
+ * allocating: grids whose half spectrum plus twiddle tables exceed 64 MiB
+ * (e.g. beyond 256x256x240) are rejected with ACCFFT_C_EINVAL.  Nothing is
+ * allocated on the device and nothing is freed.
+ * The first call on a device performs a one-time set-up; make it before any
+ * stream capture.  Every call reuses the same array, so calls that overlap on
+ * the GPU race.  `stream` is a cudaStream_t (NULL: the default stream); the
+ * call returns when the result is complete. */
+int accfft_c_laplace_gpuf_noalloc(const int n[3], float* LA, const float* A, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
