@@ -245,10 +245,11 @@ template <int R, int S> struct Dft {
   }
 };
 
-template <typename T, int L>
+// EF != 0 forces the first radix (tuning sweeps); 0 selects plan_for()
+template <typename T, int L, int EF = 0>
 struct LineFFT {
   typedef typename CT<T>::V V;
-  static constexpr LinePlan pl = plan_for(L, std::is_same<T, double>::value);
+  static constexpr LinePlan pl = plan_select(L, std::is_same<T, double>::value, EF);
   static constexpr int E = pl.E;
   static constexpr int P = pl.P;
   static constexpr int NS = pl.ns;

@@ -59,6 +59,25 @@ AFG_HD constexpr LinePlan plan_for(int L, bool dbl) {
   return pl;   // E == 0 marks "no plan" (a prime factor above 32)
 }
 
+// plan with a fixed first radix E (E must divide L); E == 0 marks failure
+AFG_HD constexpr LinePlan plan_with_e(int L, int E) {
+  LinePlan pl{};
+  pl.L = L; pl.E = 0; pl.P = 0; pl.ns = 0;
+  for (int i = 0; i < 16; ++i) pl.radix[i] = 1;
+  if (L == 1) { pl.E = 1; pl.P = 1; return pl; }
+  if (E < 2 || L % E) return pl;
+  int rad[16] = {};
+  int ns = plan_greedy(L, E, rad);
+  if (ns == 0) return pl;
+  pl.E = E; pl.P = L / E; pl.ns = ns;
+  for (int i = 0; i < 16; ++i) pl.radix[i] = i < ns ? rad[i] : 1;
+  return pl;
+}
+
+AFG_HD constexpr LinePlan plan_select(int L, bool dbl, int E) {
+  return E ? plan_with_e(L, E) : plan_for(L, dbl);
+}
+
 // product of the radices of stages [0, s)
 AFG_HD constexpr int plan_ns_before(const LinePlan& pl, int s) {
   int n = 1;

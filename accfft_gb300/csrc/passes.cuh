@@ -101,35 +101,43 @@ __device__ __forceinline__ V sym_apply(const SymArgs& s, const SymCol& c, int p,
 }
 
 // ------------------------------------------------------------ tile shapes
-template <typename T, int L> struct StridedShape {
-  static constexpr int P = LineFFT<T, L>::P;
+// EF forces the first radix, TCF / TLF the columns / lines per CTA (tuning
+// sweeps); 0 selects the defaults
+template <typename T, int L, int EF = 0, int TCF = 0> struct StridedShape {
+  static constexpr int P = LineFFT<T, L, EF>::P;
   static constexpr int tmin = sizeof(T) == 4 ? 16 : 8;      // 128-byte row segments
   static constexpr int want = (sizeof(T) == 4 ? 256 : 128) / P;
-  static constexpr int TC = want > tmin ? (want > 64 ? 64 : want) : tmin;
+  static constexpr int TC = TCF ? TCF : (want > tmin ? (want > 64 ? 64 : want) : tmin);
   static constexpr int threads = P * TC;
   static constexpr size_t smem = size_t(L) * TC * sizeof(typename CT<T>::V);
 };
 
-template <typename T, int L> struct ContigShape {
-  static constexpr int P = LineFFT<T, L>::P;
+template <typename T, int L, int EF = 0, int TLF = 0> struct ContigShape {
+  static constexpr int E = LineFFT<T, L, EF>::E;
+  static constexpr int P = LineFFT<T, L, EF>::P;
   static constexpr int want = (sizeof(T) == 4 ? 256 : 128) / P;
-  static constexpr int TL = want > 1 ? want : 1;
+  static constexpr int TL = TLF ? TLF : (want > 1 ? want : 1);
   static constexpr int threads = P * TL;
-  // line pitch: room for L+1 entries (r2c spectra), rounded to a 128-byte
-  // bank row, plus a shift of P slots when several lines share a warp so
-  // that their accesses land in different banks
-  static constexpr int slots = sizeof(T) == 4 ? 16 : 8;
-  static constexpr int LP = ((L + 1 + slots - 1) / slots) * slots + (P < slots ? P : 0);
+  // Line-major shared memory.  Stage 0 writes position j*E + r (stride E
+  // across threads), so one pad slot after every PW = max(E, bank row)
+  // entries spreads those writes over all banks; consecutive positions stay
+  // consecutive.
+  static constexpr int slots = sizeof(T) == 4 ? 16 : 8;    // complex slots per 128-byte bank row
+  static constexpr int PW = E > slots ? E : slots;
+  __host__ __device__ static constexpr int pad(int p) { return p + p / PW; }
+  // line pitch: room for L+1 entries (r2c spectra) after padding, rounded to a
+  // bank row, plus a shift of P slots when several lines share a warp
+  static constexpr int LP = ((pad(L) + 1 + slots - 1) / slots) * slots + (P < slots ? P : 0);
   static constexpr size_t smem = size_t(LP) * TL * sizeof(typename CT<T>::V);
 };
 
 // ------------------------------------------------------------------ kernels
-template <typename T, int L, int MODE>
-__global__ void __launch_bounds__(StridedShape<T, L>::threads)
+template <typename T, int L, int MODE, int EF = 0, int TCF = 0>
+__global__ void __launch_bounds__(StridedShape<T, L, EF, TCF>::threads)
 k_strided(const StridedArgs a) {
-  typedef LineFFT<T, L> LN;
+  typedef LineFFT<T, L, EF> LN;
   typedef typename CT<T>::V V;
-  constexpr int TC = StridedShape<T, L>::TC;
+  constexpr int TC = StridedShape<T, L, EF, TCF>::TC;
   extern __shared__ __align__(16) unsigned char smraw[];
   V* sm = reinterpret_cast<V*>(smraw);
   const int c = threadIdx.x % TC;
@@ -171,24 +179,30 @@ k_strided(const StridedArgs a) {
   }
 }
 
-template <typename T, int L>
-__global__ void __launch_bounds__(ContigShape<T, L>::threads)
+// Contiguous-line kernels share this prologue: thread t of line li of the
+// CTA, the line's padded shared-memory row and the validity of the line.
+#define AFG_CONTIG_PROLOGUE(L_)                                                \
+  typedef LineFFT<T, L_, EF> LN;                                               \
+  typedef ContigShape<T, L_, EF, TLF> SH;                                      \
+  typedef typename CT<T>::V V;                                                 \
+  constexpr int P = LN::P, TL = SH::TL;                                        \
+  extern __shared__ __align__(16) unsigned char smraw[];                       \
+  V* sm = reinterpret_cast<V*>(smraw);                                         \
+  const int t = threadIdx.x % P, li = threadIdx.x / P;                         \
+  const long long line = (long long)blockIdx.x * TL + li;                      \
+  const bool valid = line < a.nlines;                                          \
+  const long long ls = valid ? line : 0;                                       \
+  V* sl = sm + li * SH::LP;                                                    \
+  auto xw = [&](int p, V x) { sl[SH::pad(p)] = x; };                          \
+  auto xr = [&](int p) { return sl[SH::pad(p)]; };
+
+template <typename T, int L, int EF = 0, int TLF = 0>
+__global__ void __launch_bounds__(ContigShape<T, L, EF, TLF>::threads)
 k_zc2c(const ContigArgs a) {
-  typedef LineFFT<T, L> LN;
-  typedef typename CT<T>::V V;
-  constexpr int P = LN::P, LP = ContigShape<T, L>::LP, TL = ContigShape<T, L>::TL;
-  extern __shared__ __align__(16) unsigned char smraw[];
-  V* sm = reinterpret_cast<V*>(smraw);
-  const int t = threadIdx.x % P, li = threadIdx.x / P;
-  const long long line = (long long)blockIdx.x * TL + li;
-  const bool valid = line < a.nlines;
-  const long long ls = valid ? line : 0;
+  AFG_CONTIG_PROLOGUE(L)
   const V* in = static_cast<const V*>(a.in) + ls * a.in_dist;
   V* out = static_cast<V*>(a.out) + ls * a.out_dist;
-  V* sl = sm + li * LP;
   const T sg = a.inverse ? T(-1) : T(1);
-  auto xw = [&](int p, V x) { sl[p] = x; };
-  auto xr = [&](int p) { return sl[p]; };
   auto ld = [&](int p) { V x = in[p]; x.y *= sg; return x; };
   auto st = [&](int p, V x) { x.y *= sg; if (valid) out[p] = x; };
   LN::template run<false, false>(t, static_cast<const V*>(a.tw), ld, st, xw, xr);
@@ -211,58 +225,50 @@ __device__ __forceinline__ V c2r_merge(V xk, V xm, V wc) {
   return c_make<V>(s.x - wd.y, s.y + wd.x);
 }
 
-template <typename T, int M>
-__global__ void __launch_bounds__(ContigShape<T, M>::threads)
+template <typename T, int M, int EF = 0, int TLF = 0>
+__global__ void __launch_bounds__(ContigShape<T, M, EF, TLF>::threads)
 k_zr2c(const ContigArgs a) {
-  typedef LineFFT<T, M> LN;
-  typedef typename CT<T>::V V;
-  constexpr int P = LN::P, LP = ContigShape<T, M>::LP, TL = ContigShape<T, M>::TL;
-  extern __shared__ __align__(16) unsigned char smraw[];
-  V* sm = reinterpret_cast<V*>(smraw);
-  const int t = threadIdx.x % P, li = threadIdx.x / P;
-  const long long line = (long long)blockIdx.x * TL + li;
-  const bool valid = line < a.nlines;
-  const long long ls = valid ? line : 0;
+  AFG_CONTIG_PROLOGUE(M)
   const V* in = reinterpret_cast<const V*>(static_cast<const T*>(a.in) + ls * a.in_dist);
   V* out = static_cast<V*>(a.out) + ls * a.out_dist;
-  V* sl = sm + li * LP;
-  auto xw = [&](int p, V x) { sl[p] = x; };
-  auto xr = [&](int p) { return sl[p]; };
   auto ld = [&](int p) { return in[p]; };
-  auto st = [&](int p, V x) { sl[p] = x; };
-  LN::template run<true, false>(t, static_cast<const V*>(a.tw), ld, st, xw, xr);
+  LN::template run<true, false>(t, static_cast<const V*>(a.tw), ld, xw, xw, xr);
   __syncthreads();
   const V* twp = static_cast<const V*>(a.tw_post);
-  for (int k = t; k <= M; k += P) {
-    V zk = sl[k == M ? 0 : k];
-    V zm = sl[k == 0 ? 0 : M - k];
-    V x = r2c_split(zk, zm, __ldg(twp + k));
+  // outputs k = t + r*P (r < E) cover 0..M-1; thread 0 also writes k = M
+#pragma unroll
+  for (int r = 0; r < LN::E; ++r) {
+    const int k = t + r * P;
+    V x = r2c_split(xr(k), xr(k == 0 ? 0 : M - k), __ldg(twp + k));
     if (valid) out[k] = x;
+  }
+  if (t == 0) {
+    V z0 = xr(0);
+    if (valid) out[M] = c_make<V>(z0.x - z0.y, T(0));
   }
 }
 
-template <typename T, int M>
-__global__ void __launch_bounds__(ContigShape<T, M>::threads)
+template <typename T, int M, int EF = 0, int TLF = 0>
+__global__ void __launch_bounds__(ContigShape<T, M, EF, TLF>::threads)
 k_zc2r(const ContigArgs a) {
-  typedef LineFFT<T, M> LN;
-  typedef typename CT<T>::V V;
-  constexpr int P = LN::P, LP = ContigShape<T, M>::LP, TL = ContigShape<T, M>::TL;
-  extern __shared__ __align__(16) unsigned char smraw[];
-  V* sm = reinterpret_cast<V*>(smraw);
-  const int t = threadIdx.x % P, li = threadIdx.x / P;
-  const long long line = (long long)blockIdx.x * TL + li;
-  const bool valid = line < a.nlines;
-  const long long ls = valid ? line : 0;
+  AFG_CONTIG_PROLOGUE(M)
   const V* in = static_cast<const V*>(a.in) + ls * a.in_dist;
   V* out = reinterpret_cast<V*>(static_cast<T*>(a.out) + ls * a.out_dist);
-  V* sl = sm + li * LP;
-  for (int k = t; k <= M; k += P) sl[k] = in[k];
+  {
+    // stage the M+1 input entries: E independent loads per thread, then the
+    // Nyquist entry by thread 0
+    V v[LN::E];
+#pragma unroll
+    for (int r = 0; r < LN::E; ++r) v[r] = in[t + r * P];
+    V nyq = in[t == 0 ? M : 0];
+#pragma unroll
+    for (int r = 0; r < LN::E; ++r) xw(t + r * P, v[r]);
+    if (t == 0) xw(M, nyq);
+  }
   __syncthreads();
   const V* twp = static_cast<const V*>(a.tw_post);
-  auto xw = [&](int p, V x) { sl[p] = x; };
-  auto xr = [&](int p) { return sl[p]; };
   auto ld = [&](int p) {
-    V xk = sl[p], xm = sl[M - p];
+    V xk = xr(p), xm = xr(M - p);
     if (p == 0) { xk.y = T(0); xm.y = T(0); }
     return c_conj(c2r_merge(xk, xm, c_conj(__ldg(twp + p))));
   };
@@ -271,53 +277,40 @@ k_zc2r(const ContigArgs a) {
 }
 
 // real line r2c -> symbol(k) -> c2r, one pass (z-direction derivative)
-template <typename T, int M>
-__global__ void __launch_bounds__(ContigShape<T, M>::threads)
+template <typename T, int M, int EF = 0, int TLF = 0>
+__global__ void __launch_bounds__(ContigShape<T, M, EF, TLF>::threads)
 k_zsym(const ContigArgs a) {
-  typedef LineFFT<T, M> LN;
-  typedef typename CT<T>::V V;
-  constexpr int P = LN::P, LP = ContigShape<T, M>::LP, TL = ContigShape<T, M>::TL;
-  extern __shared__ __align__(16) unsigned char smraw[];
-  V* sm = reinterpret_cast<V*>(smraw);
-  const int t = threadIdx.x % P, li = threadIdx.x / P;
-  const long long line = (long long)blockIdx.x * TL + li;
-  const bool valid = line < a.nlines;
-  const long long ls = valid ? line : 0;
+  AFG_CONTIG_PROLOGUE(M)
   const V* in = reinterpret_cast<const V*>(static_cast<const T*>(a.in) + ls * a.in_dist);
   V* out = reinterpret_cast<V*>(static_cast<T*>(a.out) + ls * a.out_dist);
   const V* acc = a.acc ? reinterpret_cast<const V*>(static_cast<const T*>(a.acc) + ls * a.out_dist) : nullptr;
-  V* sl = sm + li * LP;
   const V* tw = static_cast<const V*>(a.tw);
-  auto xw = [&](int p, V x) { sl[p] = x; };
-  auto xr = [&](int p) { return sl[p]; };
   auto ld = [&](int p) { return in[p]; };
-  auto st = [&](int p, V x) { sl[p] = x; };
-  LN::template run<true, false>(t, tw, ld, st, xw, xr);
+  LN::template run<true, false>(t, tw, ld, xw, xw, xr);
   __syncthreads();
   const V* twp = static_cast<const V*>(a.tw_post);
   const SymCol none{0, 0, 0, 0};
   for (int k = t; 2 * k <= M; k += P) {
     if (k == 0) {
-      V z0 = sl[0];
+      V z0 = xr(0);
       V x0 = sym_apply<T>(a.sym, none, 0, c_make<V>(z0.x + z0.y, T(0)));
       V xn = sym_apply<T>(a.sym, none, M, c_make<V>(z0.x - z0.y, T(0)));
       // imaginary parts of DC and Nyquist are dropped by the real inverse
-      sl[0] = c_make<V>(x0.x + xn.x, -(x0.x - xn.x));   // conj(Z'[0])
+      xw(0, c_make<V>(x0.x + xn.x, -(x0.x - xn.x)));   // conj(Z'[0])
     } else {
-      V zk = sl[k], zm = sl[M - k];
+      V zk = xr(k), zm = xr(M - k);
       V wk = __ldg(twp + k), wm = __ldg(twp + (M - k));
       V xk = sym_apply<T>(a.sym, none, k, r2c_split(zk, zm, wk));
       if (2 * k == M) {
-        sl[k] = c_conj(c2r_merge(xk, xk, c_conj(wk)));
+        xw(k, c_conj(c2r_merge(xk, xk, c_conj(wk))));
       } else {
         V xm = sym_apply<T>(a.sym, none, M - k, r2c_split(zm, zk, wm));
-        sl[k] = c_conj(c2r_merge(xk, xm, c_conj(wk)));
-        sl[M - k] = c_conj(c2r_merge(xm, xk, c_conj(wm)));
+        xw(k, c_conj(c2r_merge(xk, xm, c_conj(wk))));
+        xw(M - k, c_conj(c2r_merge(xm, xk, c_conj(wm))));
       }
     }
   }
   __syncthreads();
-  auto sld = [&](int p) { return sl[p]; };
   auto gst = [&](int p, V x) {
     x.y = -x.y;
     if (valid) {
@@ -325,7 +318,9 @@ k_zsym(const ContigArgs a) {
       out[p] = x;
     }
   };
-  LN::template run<false, true>(t, tw, sld, gst, xw, xr);
+  LN::template run<false, true>(t, tw, xr, gst, xw, xr);
 }
+
+#undef AFG_CONTIG_PROLOGUE
 
 }  // namespace afg

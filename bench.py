@@ -47,6 +47,9 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=512)
+    ap.add_argument("--grid", type=int, nargs=3, default=None,
+                    help="non-cubic grid N0 N1 N2 (smaller cases of the same kernels for profiling)")
+    ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--dtype", default="float32", choices=["float32", "float64"])
     ap.add_argument("--no-baseline", action="store_true")
     return ap.parse_args()
@@ -187,6 +190,46 @@ def reference_arm(args):
     print(json.dumps(line), flush=True)
 
 
+def e2e_pairs_per_s(args, ag, torch, n, dt, u, stream, world):
+    """pairs/s through the public r2c / c2r calls with the field in pinned host
+    memory: host->device copy, r2c, c2r, device->host copy every step."""
+    tdt = getattr(torch, dt)
+    H2 = n[2] // 2 + 1
+    hu = torch.empty(n, dtype=tdt).pin_memory()
+    hu.copy_(u.cpu())
+    hb = torch.empty(n, dtype=tdt).pin_memory()
+    plan = ag.PlanR2C(n, dt)
+    plan.set_stream(stream, blocking=False)
+    du = torch.empty(n, dtype=tdt, device="cuda")
+    spec = torch.empty((n[0], n[1], H2, 2), dtype=tdt, device="cuda")
+    back = torch.empty(n, dtype=tdt, device="cuda")
+
+    def e2e_step():
+        du.copy_(hu, non_blocking=True)
+        plan.r2c(du, spec)
+        plan.c2r(spec, back)
+        hb.copy_(back, non_blocking=True)
+
+    with torch.cuda.stream(stream):
+        for _ in range(max(1, args.warmup)):
+            e2e_step()
+        stream.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        ksteps = max(3, args.steps // 2)
+        e0.record(stream)
+        for _ in range(ksteps):
+            e2e_step()
+        e1.record(stream)
+    stream.synchronize()
+    assert torch.allclose(hb, back.cpu())
+    e2e_ms = e0.elapsed_time(e1) / ksteps
+    esz = hu.element_size()
+    plan.destroy()
+    return {"value": world * 1000.0 / e2e_ms, "unit": "pairs/s", "h2d_bytes_per_step": int(hu.numel() * esz),
+            "d2h_bytes_per_step": int(hb.numel() * esz)}
+
+
 def ours(args):
     import torch
 
@@ -198,7 +241,8 @@ def ours(args):
         import torch.distributed as dist
 
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
-    n = (args.n,) * 3
+    n = tuple(args.grid) if args.grid else (args.n,) * 3
+    label = "x".join(map(str, n)) if args.grid else f"{args.n}^3"
     dt = args.dtype
     esz = 4 if dt == "float32" else 8
     tdt = getattr(torch, dt)
@@ -233,7 +277,7 @@ def ours(args):
         for _ in range(args.warmup):
             step()
     stream.synchronize()
-    # correctness gate on the benchmarked buffers: round trip returns N*u
+    # correctness gate on the benchmarked buffers: the round trip returns N*u
     err = (back / (N0 * N1 * N2) - u).norm().item() / u.norm().item()
     assert err < (1e-5 if dt == "float32" else 1e-12), err
 
@@ -269,55 +313,26 @@ def ours(args):
     peak, peak_kind = measured_peak()
     achieved = nbytes[dom] / (per[dom] / 1000.0) / 1e9
     step_bytes = sum(nbytes.values())
-
-    # end to end through the public calls with host buffers
-    hu = torch.empty(n, dtype=tdt).pin_memory()
-    hu.copy_(u.cpu())
-    hb = torch.empty(n, dtype=tdt).pin_memory()
-    plan2 = ag.PlanR2C(n, dt)
-    plan2.set_stream(stream, blocking=False)
-    du = torch.empty(n, dtype=tdt, device="cuda")
-
-    def e2e_step():
-        du.copy_(hu, non_blocking=True)
-        plan2.r2c(du, spec)
-        plan2.c2r(spec, back)
-        hb.copy_(back, non_blocking=True)
-
-    with torch.cuda.stream(stream):
-        for _ in range(max(1, args.warmup)):
-            e2e_step()
-        stream.synchronize()
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        ksteps = max(3, args.steps // 2)
-        e0.record(stream)
-        for _ in range(ksteps):
-            e2e_step()
-        e1.record(stream)
-    stream.synchronize()
-    e2e_ms = e0.elapsed_time(e1) / ksteps
-    e2e_val = world * 1000.0 / e2e_ms
-    assert torch.allclose(hb, back.cpu())
+    e2e = None if args.no_e2e else e2e_pairs_per_s(args, ag, torch, n, dt, u, stream, world)
 
     if rank != 0:
         return
     line = {
-        "metric": f"{args.n}^3 r2c+c2r pairs/s", "value": value, "unit": "pairs/s", "n_gpus": world,
+        "metric": f"{label} r2c+c2r pairs/s", "value": value, "unit": "pairs/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32" if dt == "float32" else "f64",
         "data": "synthetic N(0,1), seeded",
-        "config": {"workload": f"{args.n}^3 {dt} r2c+c2r round trip", "grid": list(n),
+        "config": {"workload": f"{label} {dt} r2c+c2r round trip", "grid": list(n),
                    "flush": "inputs_larger_than_l2", "parallelism": f"replicas{world}"},
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "kernel": KERNEL_OF[dom], "pass": dom, "achieved": achieved, "peak": peak,
                      "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": None, "bytes_per_launch": nbytes[dom], "ms_per_launch": per[dom]},
         "passes_ms": per,
+        "passes_frac_of_peak": {p: nbytes[p] / (per[p] / 1000.0) / 1e9 / peak for p in passes},
         "step_algorithmic_GBps": step_bytes / (ms_step / 1000.0) / 1e9,
         "gflops_5nlogn": 5 * N0 * N1 * N2 * np.log2(N0 * N1 * N2) / (ms_step / 1000.0) / 1e9,
-        "e2e": {"value": e2e_val, "unit": "pairs/s", "h2d_bytes_per_step": int(hu.numel() * esz),
-                "d2h_bytes_per_step": int(hb.numel() * esz)},
+        "e2e": e2e,
         "clocks": clocks,
         "roundtrip_rel_l2": err,
     }
