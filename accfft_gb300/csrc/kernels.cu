@@ -64,10 +64,14 @@ static void run_strided(const StridedArgs& a, cudaStream_t s) {
 }
 bool AFG_NAME(int L, int mode, const StridedArgs& a, cudaStream_t s) {
   switch (L) {
-#define AFG_CASE(n) \
-  case n:                          \
-    if (mode) run_strided<n, 1>(a, s); \
-    else run_strided<n, 0>(a, s);  \
+#define AFG_CASE(n)                        \
+  case n:                                  \
+    switch (mode) {                        \
+      case 0: run_strided<n, 0>(a, s); break; \
+      case 1: run_strided<n, 1>(a, s); break; \
+      case 2: run_strided<n, 2>(a, s); break; \
+      default: run_strided<n, 3>(a, s); break; \
+    }                                      \
     return true;
     AFG_LIST(AFG_CASE)
 #undef AFG_CASE

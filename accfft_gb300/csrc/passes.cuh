@@ -158,6 +158,48 @@ k_strided(const StridedArgs a) {
     auto ld = [&](int p) { V x = in[p * il]; x.y *= sg; return x; };
     auto st = [&](int p, V x) { x.y *= sg; if (valid) out[p * ol] = x; };
     LN::template run<false, false>(t, tw, ld, st, xw, xr);
+  } else if constexpr (MODE == 2) {
+    // real transform along the line of column pairs (2cc, 2cc+1) packed as
+    // u = a + i*b: A[k] = (U[k] + conj U[L-k])/2, B[k] = (U[k] - conj U[L-k])/(2i),
+    // written to the half spectrum at complex columns 2cc and 2cc+1
+    const long long il = a.in_line, ol = a.out_line;
+    V* o2 = static_cast<V*>(a.out) + slab * a.out_slab + 2 * cc;
+    auto ld = [&](int p) { return in[p * il]; };
+    LN::template run<true, false>(t, tw, ld, xw, xw, xr);
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < LN::E; ++r) {
+      const int k = t + r * LN::P;
+      if (2 * k <= L) {
+        V uk = xr(k), um = xr(k == 0 ? 0 : L - k);
+        V A = c_make<V>(T(0.5) * (uk.x + um.x), T(0.5) * (uk.y - um.y));
+        V B = c_make<V>(T(0.5) * (uk.y + um.y), T(-0.5) * (uk.x - um.x));
+        if (valid) {
+          o2[k * ol] = A;
+          o2[k * ol + 1] = B;
+        }
+      }
+    }
+  } else if constexpr (MODE == 3) {
+    // inverse of MODE 2: U[k] = A[k] + i B[k], U[L-k] = conj A[k] + i conj B[k]
+    // (imaginary parts of A, B at k = 0 and k = L/2 dropped), inverse complex
+    // FFT, the real pair (a, b) stored at columns (2cc, 2cc+1)
+    const long long il = a.in_line, ol = a.out_line;
+    const V* i2 = static_cast<const V*>(a.in) + slab * a.in_slab + 2 * cc;
+#pragma unroll
+    for (int r = 0; r < LN::E; ++r) {
+      const int k = t + r * LN::P;
+      if (2 * k <= L) {
+        V A = i2[k * il], B = i2[k * il + 1];
+        if (k == 0 || 2 * k == L) { A.y = T(0); B.y = T(0); }
+        // conjugated for the forward-engine inverse
+        xw(k, c_make<V>(A.x - B.y, -(A.y + B.x)));
+        if (k != 0 && 2 * k != L) xw(L - k, c_make<V>(A.x + B.y, A.y - B.x));
+      }
+    }
+    __syncthreads();
+    auto st = [&](int p, V x) { x.y = -x.y; if (valid) out[p * ol] = x; };
+    LN::template run<false, true>(t, tw, xr, st, xw, xr);
   } else {
     const SymCol scol = sym_column(a.sym, gs);
     const long long il = a.in_line, ol = a.out_line;

@@ -344,6 +344,44 @@ struct Exec {
     a.sym = sym;
     if (!launch_zsym(p->dbl, p->M(), a, p->stream)) unsupported("z symbol pass", p->M());
   }
+  // single-axis real transform along x (axis 0) or y (axis 1) of an
+  // unpadded [N0][N1][N2] real array (the reference's x-only / y-only
+  // layouts, src/accfft_gpu.cpp:1319-1604): adjacent z columns are packed as
+  // one complex column; mode 2 = r2c, 3 = c2r
+  void pair_axis(int axis, int mode, const void* in, void* out) {
+    if (!ok()) return;
+    const long long N0 = p->n[0], N1 = p->n[1], N2 = p->n[2];
+    const long long pr = N2 / 2;   // complex pairs per real row
+    StridedArgs a{};
+    a.in = in;
+    a.out = out;
+    int L;
+    long long real_slab, real_line, spec_slab, spec_line;
+    if (axis == 1) {
+      L = (int)N1;
+      a.tw = p->tw_y;
+      a.ncols = N0 * pr;
+      a.cps = pr;
+      real_slab = N1 * pr;
+      real_line = pr;
+      spec_slab = (N1 / 2 + 1) * N2;
+      spec_line = N2;
+    } else {
+      L = (int)N0;
+      a.tw = p->tw_x;
+      a.ncols = a.cps = N1 * pr;
+      real_slab = 0;
+      real_line = N1 * pr;
+      spec_slab = 0;
+      spec_line = N1 * N2;
+    }
+    if (mode == 2) {
+      a.in_slab = real_slab; a.in_line = real_line; a.out_slab = spec_slab; a.out_line = spec_line;
+    } else {
+      a.in_slab = spec_slab; a.in_line = spec_line; a.out_slab = real_slab; a.out_line = real_line;
+    }
+    if (!launch_strided(p->dbl, L, mode, a, p->stream)) unsupported("single-axis pass", L);
+  }
   int finish() {
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess && ok()) rc = cuda_fail(e, "kernel launch");
@@ -586,9 +624,10 @@ int accfft_c_execute_r2c_axis(accfft_c_plan* p, int axis, const void* in, void* 
   if (rc) return rc;
   if (!in || !out) return fail(ACCFFT_C_EINVAL, "execute_r2c_axis: NULL array");
   if (int a = check_align(p, "execute_r2c_axis", {in, out})) return a;
-  if (axis != 2) return fail(ACCFFT_C_EUNSUPPORTED, "execute_r2c_axis: axis %d not available yet", axis);
+  if (axis < 0 || axis > 2) return fail(ACCFFT_C_EINVAL, "execute_r2c_axis: axis must be 0, 1 or 2");
   Exec ex(p, timer);
-  ex.zr2c(in, out, p->rrow());
+  if (axis == 2) ex.zr2c(in, out, p->rrow());
+  else ex.pair_axis(axis, 2, in, out);
   return ex.finish();
 }
 int accfft_c_execute_c2r_axis(accfft_c_plan* p, int axis, const void* in, void* out, double* timer) {
@@ -596,9 +635,10 @@ int accfft_c_execute_c2r_axis(accfft_c_plan* p, int axis, const void* in, void* 
   if (rc) return rc;
   if (!in || !out) return fail(ACCFFT_C_EINVAL, "execute_c2r_axis: NULL array");
   if (int a = check_align(p, "execute_c2r_axis", {in, out})) return a;
-  if (axis != 2) return fail(ACCFFT_C_EUNSUPPORTED, "execute_c2r_axis: axis %d not available yet", axis);
+  if (axis < 0 || axis > 2) return fail(ACCFFT_C_EINVAL, "execute_c2r_axis: axis must be 0, 1 or 2");
   Exec ex(p, timer);
-  ex.zc2r(in, out, p->rrow());
+  if (axis == 2) ex.zc2r(in, out, p->rrow());
+  else ex.pair_axis(axis, 3, in, out);
   return ex.finish();
 }
 

@@ -103,7 +103,9 @@ int accfft_c_execute_c2c_gpuf(accfft_c_plan* plan, int direction, float* data, f
  * (src/accfft_gpu.cpp:1212-1604; float src/accfft_gpuf.cpp:1197-1572).
  * Spectrum layouts: z -> [N0][N1][N2/2+1], y -> [N0][N1/2+1][N2],
  * x -> [N0/2+1][N1][N2].  axis: 0 = x, 1 = y, 2 = z.  Double plans take
- * double arrays, float plans float arrays (passed as void*). */
+ * double arrays, float plans float arrays (passed as void*).  The x and y
+ * transforms use unpadded [N0][N1][N2] real arrays (as the reference's), the
+ * z transform the plan's real layout; c2r leaves its input unchanged. */
 int accfft_c_execute_r2c_axis(accfft_c_plan* plan, int axis, const void* data, void* data_out, double* timer);
 int accfft_c_execute_c2r_axis(accfft_c_plan* plan, int axis, const void* data, void* data_out, double* timer);
 

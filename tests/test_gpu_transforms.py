@@ -143,3 +143,33 @@ def test_kernel_launch_counter(cuda, native):
     before = native.kernel_launches()
     plan.r2c(du, dh)
     assert native.kernel_launches() - before == 3      # z, y and x passes
+
+
+AXIS_SHAPES = [(8, 6, 4), (16, 12, 10), (5, 9, 4), (48, 96, 64), (128, 128, 128), (160, 180, 200), (9, 5, 6)]
+
+
+@pytest.mark.parametrize("dtype", ["float64", "float32"])
+@pytest.mark.parametrize("n", AXIS_SHAPES)
+@pytest.mark.parametrize("axis", [0, 1, 2])
+def test_single_axis_r2c_c2r(cuda, native, oracle, n, dtype, axis):
+    """accfft_execute_{r2c,c2r}_{x,y,z}_gpu_t layouts: x -> [N0/2+1][N1][N2],
+    y -> [N0][N1/2+1][N2], z -> [N0][N1][N2/2+1] (src/accfft_gpu.cpp:1212-1604)."""
+    torch = cuda
+    u = rng(60 + axis).standard_normal(n)
+    plan = native.PlanR2C(n, dtype)
+    du = to_dev(torch, u, dtype)
+    hshape = list(n)
+    hshape[axis] = n[axis] // 2 + 1
+    dh = empty(torch, tuple(hshape) + (2,), dtype)
+    plan.r2c_axis(axis, du, dh)
+    ref = oracle.r2c_axis(u.astype(dtype).astype(np.float64), axis)
+    assert oracle.rel_l2(from_dev(dh, True), ref) < TOL[dtype]
+    # c2r of an arbitrary half spectrum (imaginary DC / Nyquist parts ignored)
+    h = rng(70).standard_normal(ref.shape) + 1j * rng(71).standard_normal(ref.shape)
+    dh2 = to_dev(torch, h, dtype)
+    keep = dh2.clone()
+    db = empty(torch, n, dtype)
+    plan.c2r_axis(axis, dh2, db)
+    refb = oracle.c2r_axis(from_dev(keep, True), axis, n)
+    assert oracle.rel_l2(from_dev(db), refb) < TOL[dtype]
+    assert torch.equal(dh2, keep)
