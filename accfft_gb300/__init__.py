@@ -120,14 +120,14 @@ def _ints(vals):
 
 
 def _ptr(x) -> int | None:
-    """Device address of a CUDA tensor, an int pointer, or None."""
+    """Address of a CUDA tensor or a pinned host tensor, an int pointer, or None."""
     if x is None:
         return None
     if isinstance(x, int):
         return x
     if hasattr(x, "data_ptr"):
-        if not x.is_cuda:
-            raise ValueError("expected a CUDA tensor")
+        if not x.is_cuda and not x.is_pinned():
+            raise ValueError("expected a CUDA tensor or a pinned host tensor")
         if not x.is_contiguous():
             raise ValueError("expected a contiguous tensor")
         return x.data_ptr()

@@ -50,4 +50,14 @@ struct ContigArgs {
   SymArgs sym;
 };
 
+struct SlabArgs {
+  const void* in;           // forward: real [N0][N1][row]; inverse: spectrum [N0][N1][N2/2+1]
+  void* out;                // forward: spectrum; inverse: real
+  const void* tw_y;         // stage twiddles of N1
+  const void* tw_z;         // stage twiddles of N2/2
+  const void* tw_post;      // r2c split twiddles
+  long long n0;             // slabs
+  long long real_row;       // reals per row of the real array
+};
+
 }  // namespace afg

@@ -255,68 +255,91 @@ struct LineFFT {
   static constexpr int NS = pl.ns;
   static_assert(E > 0, "no radix plan for this length");
 
-  // kSmemStore : the storer writes shared memory (add a barrier after the
-  //              last stage's shared-memory reads).
-  // kSyncAfterLoad : the loader reads shared memory (add a barrier before the
-  //              first exchange overwrites it).
+  // compute(): every stage of the line transform, outputs left in v[] with
+  // the last stage's position mapping (emit() hands them to a storer).
+  //   load(p)      stage-0 input at line position p (global or shared memory)
+  //   xw/xr        shared-memory exchange accessors of this line
+  //   after_load() runs once the stage-0 loads are issued and before the first
+  //                exchange overwrites shared memory (a barrier when the loads
+  //                read shared memory; a cluster barrier when they read another
+  //                CTA's shared memory)
+  template <class Load, class XW, class XR, class AfterLoad>
+  __device__ __forceinline__ static void compute(int t, const V* __restrict__ tw, Load&& load, XW&& xw, XR&& xr,
+                                                 AfterLoad&& after_load, V (&v)[E]) {
+#pragma unroll
+    for (int r = 0; r < E; ++r) v[r] = load(t + r * P);
+    after_load();
+    if constexpr (NS >= 1) Dft<E, 1>::run(v);
+    if constexpr (NS >= 2) {
+      static_for<1, NS>([&](auto s_) {
+        constexpr int s = decltype(s_)::value;
+        constexpr int Rp = pl.radix[s - 1];
+        constexpr int R = pl.radix[s];
+        constexpr int Nsp = plan_ns_before(pl, s - 1);
+        constexpr int Ns = plan_ns_before(pl, s);
+        constexpr int two = plan_tw_offset(pl, s);
+#pragma unroll
+        for (int b = 0; b < E / Rp; ++b) {
+          const int j = t + b * P;
+          const int base = (j / Nsp) * Nsp * Rp + (j % Nsp);
+#pragma unroll
+          for (int r = 0; r < Rp; ++r) xw(base + r * Nsp, v[b * Rp + r]);
+        }
+        __syncthreads();
+#pragma unroll
+        for (int b = 0; b < E / R; ++b) {
+          const int j = t + b * P;
+#pragma unroll
+          for (int r = 0; r < R; ++r) v[b * R + r] = xr(j + r * (L / R));
+        }
+        if constexpr (s < NS - 1) __syncthreads();
+#pragma unroll
+        for (int b = 0; b < E / R; ++b) {
+          const int j = t + b * P;
+          const int k = j % Ns;
+#pragma unroll
+          for (int r = 1; r < R; ++r) v[b * R + r] = c_mul(v[b * R + r], __ldg(tw + two + (r - 1) * Ns + k));
+          Dft<R, 1>::run(v + b * R);
+        }
+      });
+    }
+  }
+
+  // hand the outputs of compute() to store(p, value), p = frequency index
+  template <class Store>
+  __device__ __forceinline__ static void emit(int t, V (&v)[E], Store&& store) {
+    if constexpr (NS == 0) {
+      store(t, v[0]);
+    } else if constexpr (NS == 1) {
+#pragma unroll
+      for (int r = 0; r < E; ++r) store(r, v[r]);
+    } else {
+      constexpr int R = pl.radix[NS - 1];
+      constexpr int Ns = plan_ns_before(pl, NS - 1);
+#pragma unroll
+      for (int b = 0; b < E / R; ++b) {
+        const int j = t + b * P;
+#pragma unroll
+        for (int r = 0; r < R; ++r) store(j + r * Ns, v[b * R + r]);
+      }
+    }
+  }
+
+  // kSmemStore : the storer writes shared memory (barrier after the last
+  //              stage's shared-memory reads).
+  // kSyncAfterLoad : the loader reads shared memory (barrier before the first
+  //              exchange overwrites it).
   template <bool kSmemStore, bool kSyncAfterLoad, class Load, class Store, class XW, class XR>
   __device__ __forceinline__ static void run(int t, const V* __restrict__ tw, Load&& load, Store&& store,
                                              XW&& xw, XR&& xr) {
     V v[E];
-#pragma unroll
-    for (int r = 0; r < E; ++r) v[r] = load(t + r * P);
-    if constexpr (NS == 0) {
-#pragma unroll
-      for (int r = 0; r < E; ++r) store(t + r, v[r]);
-      return;
-    } else {
-      Dft<E, 1>::run(v);
-      if constexpr (NS == 1) {
-#pragma unroll
-        for (int r = 0; r < E; ++r) store(r, v[r]);
-      } else {
-        if constexpr (kSyncAfterLoad) __syncthreads();
-        static_for<1, NS>([&](auto s_) {
-          constexpr int s = decltype(s_)::value;
-          constexpr int Rp = pl.radix[s - 1];
-          constexpr int R = pl.radix[s];
-          constexpr int Nsp = plan_ns_before(pl, s - 1);
-          constexpr int Ns = plan_ns_before(pl, s);
-          constexpr int two = plan_tw_offset(pl, s);
-#pragma unroll
-          for (int b = 0; b < E / Rp; ++b) {
-            const int j = t + b * P;
-            const int base = (j / Nsp) * Nsp * Rp + (j % Nsp);
-#pragma unroll
-            for (int r = 0; r < Rp; ++r) xw(base + r * Nsp, v[b * Rp + r]);
-          }
-          __syncthreads();
-#pragma unroll
-          for (int b = 0; b < E / R; ++b) {
-            const int j = t + b * P;
-#pragma unroll
-            for (int r = 0; r < R; ++r) v[b * R + r] = xr(j + r * (L / R));
-          }
-          if constexpr (s < NS - 1 || kSmemStore) __syncthreads();
-#pragma unroll
-          for (int b = 0; b < E / R; ++b) {
-            const int j = t + b * P;
-            const int k = j % Ns;
-#pragma unroll
-            for (int r = 1; r < R; ++r) v[b * R + r] = c_mul(v[b * R + r], __ldg(tw + two + (r - 1) * Ns + k));
-            Dft<R, 1>::run(v + b * R);
-          }
-          if constexpr (s == NS - 1) {
-#pragma unroll
-            for (int b = 0; b < E / R; ++b) {
-              const int j = t + b * P;
-#pragma unroll
-              for (int r = 0; r < R; ++r) store(j + r * Ns, v[b * R + r]);
-            }
-          }
-        });
-      }
-    }
+    compute(t, tw, load, xw, xr,
+            [] {
+              if constexpr (kSyncAfterLoad && NS >= 2) __syncthreads();
+            },
+            v);
+    if constexpr (kSmemStore && NS >= 2) __syncthreads();
+    emit(t, v, store);
   }
 };
 

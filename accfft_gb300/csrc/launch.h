@@ -36,6 +36,11 @@ bool launch_zr2c(bool dbl, int M, const ContigArgs& a, cudaStream_t s);
 bool launch_zc2r(bool dbl, int M, const ContigArgs& a, cudaStream_t s);
 bool launch_zsym(bool dbl, int M, const ContigArgs& a, cudaStream_t s);
 
+// fused z+y slab passes (thread-block clusters); false when the grid has no
+// slab kernel or its cluster cannot be scheduled on this device
+bool slab_available(bool dbl, int N1, int N2);
+bool launch_slab(bool dbl, int N1, int N2, bool forward, const SlabArgs& a, cudaStream_t s);
+
 // number of kernel launches issued by this process through the launchers
 unsigned long long launch_count();
 void count_launch();

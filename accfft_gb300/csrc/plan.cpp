@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <cstdlib>
 #include <cstdarg>
 #include <cstdint>
 #include <initializer_list>
@@ -112,6 +113,15 @@ struct accfft_c_plan {
   const void* tw_post = nullptr;
   // spectrum-sized scratch (r2c plans): out-of-place c2r and operators
   void* scratch = nullptr;
+  // how the z and y passes of r2c/c2r run: 0 = one kernel each over the whole
+  // grid, 1 = one cluster slab kernel, 2 = slab batches alternating z and y
+  // (z(b+1) on a second stream overlaps y(b); a batch's intermediate spectrum
+  // is still in L2 when the next pass reads it)
+  int zy_mode = 0;
+  int zy_batches = 1;
+  cudaStream_t stream2 = nullptr;
+  static constexpr int kMaxBatches = 64;
+  cudaEvent_t evb[kMaxBatches + 2] = {};
   cudaStream_t stream = 0;
   bool blocking = true;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -238,6 +248,30 @@ accfft_c_plan* make_plan(int kind, bool dbl, const int* n, void* data, void* dat
     accfft_c_destroy_plan(p);
     return nullptr;
   }
+  if (kind == 1) {
+    // second stream and events for the slab-batch pipelines (host-resident
+    // real arrays, see Exec::zy)
+    e = cudaStreamCreateWithFlags(&p->stream2, cudaStreamNonBlocking);
+    for (int b = 0; e == cudaSuccess && b < accfft_c_plan::kMaxBatches + 2; ++b)
+      e = cudaEventCreateWithFlags(&p->evb[b], cudaEventDisableTiming);
+    if (e != cudaSuccess) {
+      cuda_fail(e, "plan: stream creation");
+      accfft_c_destroy_plan(p);
+      return nullptr;
+    }
+    // ACCFFT_GB300_ZY = fused | batch<n> selects an alternative z+y schedule
+    // for device-resident data (both measured slower on GB300 than the
+    // default whole-grid passes; kept for comparison)
+    const char* env = getenv("ACCFFT_GB300_ZY");
+    std::string zy = env ? env : "";
+    if (zy == "fused" && slab_available(dbl, n[1], n[2])) {
+      p->zy_mode = 1;
+    } else if (zy.rfind("batch", 0) == 0) {
+      int nb = atoi(zy.c_str() + 5);
+      p->zy_mode = 2;
+      p->zy_batches = nb < 1 ? 1 : nb > accfft_c_plan::kMaxBatches ? accfft_c_plan::kMaxBatches : nb;
+    }
+  }
   auto* base = static_cast<unsigned char*>(p->tw_block);
   p->tw_x = base + off[0];
   p->tw_y = base + off[1];
@@ -320,6 +354,85 @@ struct Exec {
     a.out_dist = out_row;
     if (!launch_zc2r(p->dbl, p->M(), a, p->stream)) unsupported("z c2r pass", p->M());
   }
+  // z passes and y pass restricted to slabs [s0, s0 + ns) on stream st
+  void zr2c_slabs(const void* in, void* out, long long in_row, long long s0, long long ns, cudaStream_t st) {
+    if (!ok()) return;
+    const long long N1 = p->n[1];
+    ContigArgs a{};
+    a.in = static_cast<const char*>(in) + s0 * N1 * in_row * p->esz();
+    a.out = static_cast<char*>(out) + s0 * N1 * p->H2() * 2 * p->esz();
+    a.tw = p->tw_z;
+    a.tw_post = p->tw_post;
+    a.nlines = ns * N1;
+    a.in_dist = in_row;
+    a.out_dist = p->H2();
+    if (!launch_zr2c(p->dbl, p->M(), a, st)) unsupported("z r2c pass", p->M());
+  }
+  void zc2r_slabs(const void* in, void* out, long long out_row, long long s0, long long ns, cudaStream_t st) {
+    if (!ok()) return;
+    const long long N1 = p->n[1];
+    ContigArgs a{};
+    a.in = static_cast<const char*>(in) + s0 * N1 * p->H2() * 2 * p->esz();
+    a.out = static_cast<char*>(out) + s0 * N1 * out_row * p->esz();
+    a.tw = p->tw_z;
+    a.tw_post = p->tw_post;
+    a.nlines = ns * N1;
+    a.in_dist = p->H2();
+    a.out_dist = out_row;
+    if (!launch_zc2r(p->dbl, p->M(), a, st)) unsupported("z c2r pass", p->M());
+  }
+  void ypass_slabs(const void* in, void* out, int inverse, long long s0, long long ns, cudaStream_t st) {
+    if (!ok()) return;
+    const long long N1 = p->n[1], h = p->H2();
+    const long long off = s0 * N1 * h * 2 * p->esz();
+    StridedArgs a{};
+    a.in = static_cast<const char*>(in) + off;
+    a.out = static_cast<char*>(out) + off;
+    a.tw = p->tw_y;
+    a.ncols = ns * h;
+    a.cps = h;
+    a.in_slab = a.out_slab = N1 * h;
+    a.in_line = a.out_line = h;
+    a.inverse = inverse;
+    if (!launch_strided(p->dbl, p->n[1], 0, a, st)) unsupported("strided pass", p->n[1]);
+  }
+  // z r2c then y forward (forward = true), or y backward then z c2r, over
+  // the whole grid.  When the real array is in (pinned) host memory the z
+  // kernels read or write it directly over the host link, slab batch by slab
+  // batch on the plan's stream, while the y pass of the previous batch runs
+  // on a second stream.
+  void zy(bool forward, const void* in, void* mid, void* out, long long row, bool host_real) {
+    if (!ok()) return;
+    if (p->zy_mode == 1 && !host_real) {
+      slab(forward, in, out);
+      return;
+    }
+    const long long N0 = p->n[0];
+    int nb = host_real ? 8 : (p->zy_mode == 2 ? p->zy_batches : 1);
+    if (nb > N0) nb = (int)N0;
+    cudaStream_t A = p->stream, B = nb > 1 ? p->stream2 : p->stream;
+    if (B != A) {
+      cudaEventRecord(p->evb[0], A);
+      cudaStreamWaitEvent(B, p->evb[0], 0);
+    }
+    for (int b = 0; b < nb; ++b) {
+      const long long s0 = N0 * b / nb, s1 = N0 * (b + 1) / nb;
+      // forward: z (reads the real array) on A, y on B; inverse: y on A,
+      // z (writes the real array) on B
+      if (forward) zr2c_slabs(in, out, row, s0, s1 - s0, A);
+      else ypass_slabs(in, mid, 1, s0, s1 - s0, A);
+      if (B != A) {
+        cudaEventRecord(p->evb[1 + b], A);
+        cudaStreamWaitEvent(B, p->evb[1 + b], 0);
+      }
+      if (forward) ypass_slabs(out, out, 0, s0, s1 - s0, B);
+      else zc2r_slabs(mid, out, row, s0, s1 - s0, B);
+    }
+    if (B != A) {
+      cudaEventRecord(p->evb[nb + 1], B);
+      cudaStreamWaitEvent(A, p->evb[nb + 1], 0);
+    }
+  }
   void zc2c(const void* in, void* out, int inverse) {
     if (!ok()) return;
     ContigArgs a{};
@@ -343,6 +456,18 @@ struct Exec {
     a.in_dist = a.out_dist = row;
     a.sym = sym;
     if (!launch_zsym(p->dbl, p->M(), a, p->stream)) unsupported("z symbol pass", p->M());
+  }
+  void slab(bool forward, const void* in, void* out) {
+    if (!ok()) return;
+    SlabArgs a{};
+    a.in = in;
+    a.out = out;
+    a.tw_y = p->tw_y;
+    a.tw_z = p->tw_z;
+    a.tw_post = p->tw_post;
+    a.n0 = p->n[0];
+    a.real_row = p->rrow();
+    if (!launch_slab(p->dbl, p->n[1], p->n[2], forward, a, p->stream)) rc = fail(ACCFFT_C_ECUDA, "slab pass launch failed");
   }
   // single-axis real transform along x (axis 0) or y (axis 1) of an
   // unpadded [N0][N1][N2] real array (the reference's x-only / y-only
@@ -408,6 +533,27 @@ int check_align(const accfft_c_plan* p, const char* fn, std::initializer_list<co
   return ACCFFT_C_OK;
 }
 
+// 0: device (or managed) memory, 1: pinned host memory (kernels reach it
+// over the host link), -1: memory the GPU cannot address
+int classify(const void* q) {
+  if (!q) return 0;
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, q) != cudaSuccess) {
+    cudaGetLastError();
+    return -1;
+  }
+  if (at.type == cudaMemoryTypeHost) return 1;
+  if (at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged) return 0;
+  return -1;
+}
+
+int check_addressable(const char* fn, std::initializer_list<const void*> ptrs) {
+  for (const void* q : ptrs)
+    if (classify(q) < 0)
+      return fail(ACCFFT_C_EINVAL, "%s: array %p is neither device memory nor pinned host memory", fn, q);
+  return ACCFFT_C_OK;
+}
+
 int check_plan(accfft_c_plan* p, int kind, int dbl, const char* fn) {
   g_err.clear();
   if (!p) return fail(ACCFFT_C_EINVAL, "%s: NULL plan", fn);
@@ -424,15 +570,22 @@ int exec_r2c_plan(accfft_c_plan* p, int direction, void* in, void* out, double* 
   if (!out) out = p->data_out;
   if (!in || !out) return fail(ACCFFT_C_EINVAL, "execute: NULL data pointer and none given at plan time");
   if (int rc = check_align(p, "execute", {in, out})) return rc;
+  if (int rc = check_addressable("execute", {in, out})) return rc;
+  const bool host_in = classify(in) == 1, host_out = classify(out) == 1;
   const long long h = p->H2();
   Exec ex(p, timer);
   if (direction == -1) {
     void* work = in;   // with z skipped the reference transforms the input in place
-    if (xyz & ZB) {
-      ex.zr2c(in, out, p->rrow());
+    if ((xyz & ZB) && (xyz & YB)) {
+      ex.zy(true, in, nullptr, out, p->rrow(), host_in);
       work = out;
+    } else {
+      if (xyz & ZB) {
+        ex.zr2c(in, out, p->rrow());
+        work = out;
+      }
+      if (xyz & YB) ex.ypass(work, work, h, 0);
     }
-    if (xyz & YB) ex.ypass(work, work, h, 0);
     if (xyz & XB) ex.xpass(work, work, h, 0);
   } else if (direction == 1) {
     // x and y inverse passes read the input spectrum; out of place they write
@@ -443,11 +596,15 @@ int exec_r2c_plan(accfft_c_plan* p, int direction, void* in, void* out, double* 
       ex.xpass(src, buf, h, 1);
       src = buf;
     }
-    if (xyz & YB) {
-      ex.ypass(src, buf, h, 1);
-      src = buf;
+    if ((xyz & YB) && (xyz & ZB)) {
+      ex.zy(false, src, buf, out, p->rrow(), host_out);
+    } else {
+      if (xyz & YB) {
+        ex.ypass(src, buf, h, 1);
+        src = buf;
+      }
+      if (xyz & ZB) ex.zc2r(src, out, p->rrow());
     }
-    if (xyz & ZB) ex.zc2r(src, out, p->rrow());
   } else {
     return fail(ACCFFT_C_EINVAL, "execute: direction must be -1 or +1 (got %d)", direction);
   }
@@ -462,6 +619,7 @@ int exec_c2c_plan(accfft_c_plan* p, int direction, void* in, void* out, double* 
   if (direction != -1 && direction != 1)
     return fail(ACCFFT_C_EINVAL, "execute: direction must be -1 or +1 (got %d)", direction);
   if (int rc = check_align(p, "execute_c2c", {in, out})) return rc;
+  if (int rc = check_addressable("execute_c2c", {in, out})) return rc;
   const int inv = direction == 1;
   const long long h = p->n[2];
   Exec ex(p, timer);
@@ -494,6 +652,7 @@ SymArgs make_sym(const accfft_c_plan* p, int kind, double scale, int axis_len = 
 int op3d(accfft_c_plan* p, int sym_kind, void* outr, const void* inr, double* timer) {
   if (!outr || !inr) return fail(ACCFFT_C_EINVAL, "operator: NULL array");
   if (int rc = check_align(p, "operator", {outr, inr})) return rc;
+  if (int rc = check_addressable("operator", {outr, inr})) return rc;
   const long long h = p->H2();
   const double N = (double)p->n[0] * p->n[1] * p->n[2];
   Exec ex(p, timer);
@@ -575,6 +734,9 @@ void accfft_c_destroy_plan(accfft_c_plan* p) {
   if (p->scratch) cudaFree(p->scratch);
   if (p->ev0) cudaEventDestroy(p->ev0);
   if (p->ev1) cudaEventDestroy(p->ev1);
+  for (cudaEvent_t e : p->evb)
+    if (e) cudaEventDestroy(e);
+  if (p->stream2) cudaStreamDestroy(p->stream2);
   delete p;
 }
 
@@ -624,6 +786,7 @@ int accfft_c_execute_r2c_axis(accfft_c_plan* p, int axis, const void* in, void* 
   if (rc) return rc;
   if (!in || !out) return fail(ACCFFT_C_EINVAL, "execute_r2c_axis: NULL array");
   if (int a = check_align(p, "execute_r2c_axis", {in, out})) return a;
+  if (int a = check_addressable("execute_r2c_axis", {in, out})) return a;
   if (axis < 0 || axis > 2) return fail(ACCFFT_C_EINVAL, "execute_r2c_axis: axis must be 0, 1 or 2");
   Exec ex(p, timer);
   if (axis == 2) ex.zr2c(in, out, p->rrow());
@@ -635,6 +798,7 @@ int accfft_c_execute_c2r_axis(accfft_c_plan* p, int axis, const void* in, void* 
   if (rc) return rc;
   if (!in || !out) return fail(ACCFFT_C_EINVAL, "execute_c2r_axis: NULL array");
   if (int a = check_align(p, "execute_c2r_axis", {in, out})) return a;
+  if (int a = check_addressable("execute_c2r_axis", {in, out})) return a;
   if (axis < 0 || axis > 2) return fail(ACCFFT_C_EINVAL, "execute_c2r_axis: axis must be 0, 1 or 2");
   Exec ex(p, timer);
   if (axis == 2) ex.zc2r(in, out, p->rrow());
@@ -665,6 +829,7 @@ int accfft_c_grad(accfft_c_plan* p, void* A_x, void* A_y, void* A_z, const void*
   if (!A || ((xyz & XB) && !A_x) || ((xyz & YB) && !A_y) || ((xyz & ZB) && !A_z))
     return fail(ACCFFT_C_EINVAL, "grad: NULL array for a selected component");
   if (int a = check_align(p, "grad", {A_x, A_y, A_z, A})) return a;
+  if (int a = check_addressable("grad", {A_x, A_y, A_z, A})) return a;
   Exec ex(p, timer);
   if (xyz & XB) deriv_axis(ex, p, 0, A_x, A, nullptr);
   if (xyz & YB) deriv_axis(ex, p, 1, A_y, A, nullptr);
@@ -694,6 +859,7 @@ int accfft_c_divergence(accfft_c_plan* p, void* divA, const void* A_x, const voi
   if (rc) return rc;
   if (!divA || !A_x || !A_y || !A_z) return fail(ACCFFT_C_EINVAL, "divergence: NULL array");
   if (int a = check_align(p, "divergence", {divA, A_x, A_y, A_z})) return a;
+  if (int a = check_addressable("divergence", {divA, A_x, A_y, A_z})) return a;
   Exec ex(p, timer);
   deriv_axis(ex, p, 0, divA, A_x, nullptr);
   deriv_axis(ex, p, 1, divA, A_y, divA);

@@ -43,7 +43,7 @@ sys.path.insert(0, ROOT)
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=512)
@@ -63,7 +63,9 @@ def dist_env():
 
 
 def algorithmic_bytes(n, esz):
-    """Per-launch bytes of each pass (each pass reads and writes its array once)."""
+    """Per-launch bytes of each pass: every pass reads its input and writes its
+    output once (the fused z+y slab passes read the real field and write the
+    spectrum, or the reverse)."""
     N = n[0] * n[1] * n[2]
     H = n[0] * n[1] * (n[2] // 2 + 1)
     c = 2 * esz
@@ -74,11 +76,14 @@ def algorithmic_bytes(n, esz):
         "x_inv": 2 * H * c,
         "y_inv": 2 * H * c,
         "z_c2r": H * c + N * esz,
+        "zy_fwd": N * esz + H * c,
+        "zy_inv": H * c + N * esz,
     }
 
 
 KERNEL_OF = {"z_r2c": "k_zr2c", "y_fwd": "k_strided (y)", "x_fwd": "k_strided (x)",
-             "x_inv": "k_strided (x)", "y_inv": "k_strided (y)", "z_c2r": "k_zc2r"}
+             "x_inv": "k_strided (x)", "y_inv": "k_strided (y)", "z_c2r": "k_zc2r",
+             "zy_fwd": "k_slab_fwd (z+y, cluster)", "zy_inv": "k_slab_inv (y+z, cluster)"}
 
 
 class Clocks:
@@ -191,8 +196,10 @@ def reference_arm(args):
 
 
 def e2e_pairs_per_s(args, ag, torch, n, dt, u, stream, world):
-    """pairs/s through the public r2c / c2r calls with the field in pinned host
-    memory: host->device copy, r2c, c2r, device->host copy every step."""
+    """pairs/s through the public r2c / c2r calls with the real field in pinned
+    host memory: every step the r2c reads the field from the host and the c2r
+    writes the result back to the host (the z passes move the data over the
+    host link themselves, overlapped with the y passes)."""
     tdt = getattr(torch, dt)
     H2 = n[2] // 2 + 1
     hu = torch.empty(n, dtype=tdt).pin_memory()
@@ -200,15 +207,11 @@ def e2e_pairs_per_s(args, ag, torch, n, dt, u, stream, world):
     hb = torch.empty(n, dtype=tdt).pin_memory()
     plan = ag.PlanR2C(n, dt)
     plan.set_stream(stream, blocking=False)
-    du = torch.empty(n, dtype=tdt, device="cuda")
     spec = torch.empty((n[0], n[1], H2, 2), dtype=tdt, device="cuda")
-    back = torch.empty(n, dtype=tdt, device="cuda")
 
     def e2e_step():
-        du.copy_(hu, non_blocking=True)
-        plan.r2c(du, spec)
-        plan.c2r(spec, back)
-        hb.copy_(back, non_blocking=True)
+        plan.r2c(hu, spec)
+        plan.c2r(spec, hb)
 
     with torch.cuda.stream(stream):
         for _ in range(max(1, args.warmup)):
@@ -216,18 +219,20 @@ def e2e_pairs_per_s(args, ag, torch, n, dt, u, stream, world):
         stream.synchronize()
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
-        ksteps = max(3, args.steps // 2)
+        ksteps = max(3, min(args.steps, 30))
         e0.record(stream)
         for _ in range(ksteps):
             e2e_step()
         e1.record(stream)
     stream.synchronize()
-    assert torch.allclose(hb, back.cpu())
+    err = ((hb / (n[0] * n[1] * n[2]) - hu).norm() / hu.norm()).item()
+    assert err < (1e-5 if dt == "float32" else 1e-12), err
     e2e_ms = e0.elapsed_time(e1) / ksteps
     esz = hu.element_size()
     plan.destroy()
     return {"value": world * 1000.0 / e2e_ms, "unit": "pairs/s", "h2d_bytes_per_step": int(hu.numel() * esz),
-            "d2h_bytes_per_step": int(hb.numel() * esz)}
+            "d2h_bytes_per_step": int(hb.numel() * esz), "ms_per_step": e2e_ms,
+            "path": "pinned host field read and written by the z passes over the host link"}
 
 
 def ours(args):
@@ -255,17 +260,23 @@ def ours(args):
     u = torch.randn(n, dtype=tdt, device="cuda", generator=g)
     spec = torch.empty((N0, N1, H2, 2), dtype=tdt, device="cuda")
     back = torch.empty(n, dtype=tdt, device="cuda")
-    passes = ["z_r2c", "y_fwd", "x_fwd", "x_inv", "y_inv", "z_c2r"]
+    # one public call per kernel: the z+y passes are a single cluster kernel
+    # when the grid has one (detected by counting launches of an xyz = z|y call)
+    l0 = ag.kernel_launches()
+    plan.r2c(u, spec, xyz=6)
+    stream.synchronize()
+    fused = ag.kernel_launches() - l0 == 1
+    if fused:
+        passes = ["zy_fwd", "x_fwd", "x_inv", "zy_inv"]
+        calls = [lambda: plan.r2c(u, spec, xyz=6), lambda: plan.r2c(spec, spec, xyz=1),
+                 lambda: plan.c2r(spec, spec, xyz=1), lambda: plan.c2r(spec, back, xyz=6)]
+    else:
+        passes = ["z_r2c", "y_fwd", "x_fwd", "x_inv", "y_inv", "z_c2r"]
+        calls = [lambda: plan.r2c(u, spec, xyz=4), lambda: plan.r2c(spec, spec, xyz=2),
+                 lambda: plan.r2c(spec, spec, xyz=1), lambda: plan.c2r(spec, spec, xyz=1),
+                 lambda: plan.c2r(spec, spec, xyz=2), lambda: plan.c2r(spec, back, xyz=4)]
 
     def step(evs=None):
-        calls = [
-            lambda: plan.r2c(u, spec, xyz=4),
-            lambda: plan.r2c(spec, spec, xyz=2),
-            lambda: plan.r2c(spec, spec, xyz=1),
-            lambda: plan.c2r(spec, spec, xyz=1),
-            lambda: plan.c2r(spec, spec, xyz=2),
-            lambda: plan.c2r(spec, back, xyz=4),
-        ]
         for i, c in enumerate(calls):
             if evs is not None:
                 evs[i][0].record(stream)
@@ -312,7 +323,7 @@ def ours(args):
     dom = max(per, key=per.get)
     peak, peak_kind = measured_peak()
     achieved = nbytes[dom] / (per[dom] / 1000.0) / 1e9
-    step_bytes = sum(nbytes.values())
+    step_bytes = sum(nbytes[p] for p in passes)
     e2e = None if args.no_e2e else e2e_pairs_per_s(args, ag, torch, n, dt, u, stream, world)
 
     if rank != 0:
@@ -329,6 +340,7 @@ def ours(args):
                      "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": None, "bytes_per_launch": nbytes[dom], "ms_per_launch": per[dom]},
         "passes_ms": per,
+        "fused_zy": fused,
         "passes_frac_of_peak": {p: nbytes[p] / (per[p] / 1000.0) / 1e9 / peak for p in passes},
         "step_algorithmic_GBps": step_bytes / (ms_step / 1000.0) / 1e9,
         "gflops_5nlogn": 5 * N0 * N1 * N2 * np.log2(N0 * N1 * N2) / (ms_step / 1000.0) / 1e9,

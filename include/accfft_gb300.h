@@ -22,6 +22,11 @@
  *     accfft_c_last_error() describes the last failure of the calling thread.
  *   - By default every call blocks until the GPU work is done (AccFFT's
  *     contract).  accfft_c_set_stream() makes a plan enqueue asynchronously.
+ *   - Arrays may be device memory or pinned host memory (cudaHostAlloc /
+ *     cudaHostRegister); other host memory is rejected with ACCFFT_C_EINVAL.
+ *     When an r2c input or a c2r output is pinned host memory, the z passes
+ *     read or write it directly over the host link in slab batches that
+ *     overlap with the y passes, so no device copy of the real array is made.
  *   - Plans are not thread-safe (one plan, one host thread at a time).
  */
 #ifndef ACCFFT_GB300_H

@@ -173,3 +173,72 @@ def test_single_axis_r2c_c2r(cuda, native, oracle, n, dtype, axis):
     refb = oracle.c2r_axis(from_dev(keep, True), axis, n)
     assert oracle.rel_l2(from_dev(db), refb) < TOL[dtype]
     assert torch.equal(dh2, keep)
+
+
+@pytest.mark.parametrize("n", [(512, 512, 512), (64, 256, 256), (32, 128, 128)])
+def test_fused_slab_pass_float(cuda, native, oracle, n, monkeypatch):
+    """Grids with a cluster slab kernel (z and y passes fused, selected with
+    ACCFFT_GB300_ZY=fused): the full transform against the oracle, and against
+    the same plan run pass by pass (xyz = z, then y, then x), which uses the
+    separate z and y kernels."""
+    torch = cuda
+    u = rng(80).standard_normal(n)
+    monkeypatch.setenv("ACCFFT_GB300_ZY", "fused")
+    plan = native.PlanR2C(n, "float32")
+    du = to_dev(torch, u, "float32")
+    h = (n[0], n[1], n[2] // 2 + 1, 2)
+    fused, split = empty(torch, h, "float32"), empty(torch, h, "float32")
+    before = native.kernel_launches()
+    plan.r2c(du, fused)
+    fused_launches = native.kernel_launches() - before
+    plan.r2c(du, split, xyz=4)
+    plan.r2c(split, split, xyz=2)
+    plan.r2c(split, split, xyz=1)
+    assert fused_launches == 2, "expected the z+y slab kernel and the x pass"
+    ref = oracle.r2c(u.astype(np.float32).astype(np.float64))
+    assert oracle.rel_l2(from_dev(fused, True), ref) < 1e-5
+    assert oracle.rel_l2(from_dev(fused, True), from_dev(split, True)) < 1e-6
+    back, back2 = empty(torch, n, "float32"), empty(torch, n, "float32")
+    keep = fused.clone()
+    plan.c2r(fused, back)
+    assert torch.equal(fused, keep)
+    plan.c2r(split, split, xyz=1)
+    plan.c2r(split, split, xyz=2)
+    plan.c2r(split, back2, xyz=4)
+    assert oracle.rel_l2(from_dev(back) / np.prod(n), u) < 1e-5
+    assert oracle.rel_l2(from_dev(back), from_dev(back2)) < 1e-6
+    plan.destroy()
+
+
+@pytest.mark.parametrize("dtype", ["float32", "float64"])
+@pytest.mark.parametrize("n", [(64, 48, 80), (128, 128, 128)])
+def test_pinned_host_real_arrays(cuda, native, oracle, n, dtype):
+    """r2c reading its real input from pinned host memory and c2r writing its
+    real output to pinned host memory (slab-batch pipeline over the host
+    link) give the device-path results."""
+    torch = cuda
+    u = rng(90).standard_normal(n)
+    plan = native.PlanR2C(n, dtype)
+    hu = torch.from_numpy(u.astype(dtype)).pin_memory()
+    du = hu.cuda()
+    s_host, s_dev = empty(torch, (n[0], n[1], n[2] // 2 + 1, 2), dtype), empty(torch, (n[0], n[1], n[2] // 2 + 1, 2), dtype)
+    plan.r2c(hu, s_host)
+    plan.r2c(du, s_dev)
+    assert torch.equal(s_host, s_dev)
+    hb = torch.empty(n, dtype=getattr(torch, dtype)).pin_memory()
+    db = empty(torch, n, dtype)
+    plan.c2r(s_dev, hb)
+    plan.c2r(s_dev, db)
+    assert torch.equal(hb, db.cpu())
+    assert oracle.rel_l2(hb.numpy().astype(np.float64) / np.prod(n), u) < TOL[dtype] * 10
+
+
+def test_unregistered_host_memory_is_refused(cuda, native):
+    torch = cuda
+    n = (16, 16, 16)
+    plan = native.PlanR2C(n, "float32")
+    host = np.zeros(n, np.float32)          # ordinary pageable memory
+    spec = empty(torch, (16, 16, 9, 2), "float32")
+    with pytest.raises(native.AccfftError) as e:
+        plan.r2c(host.ctypes.data, spec)
+    assert e.value.code == native.EINVAL and "pinned host memory" in str(e.value)
