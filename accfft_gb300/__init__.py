@@ -93,6 +93,10 @@ def lib() -> ctypes.CDLL:
         "accfft_c_inv_laplace": ([vp, vp, vp, dp], i),
         "accfft_c_inv_biharmonic": ([vp, vp, vp, dp], i),
         "accfft_c_laplace_gpuf_noalloc": ([ip, vp, vp, vp], i),
+        "accfft_c_r2c_adjoint": ([vp, vp, vp, dp], i),
+        "accfft_c_c2r_adjoint": ([vp, vp, vp, dp], i),
+        "accfft_c_grad_adjoint": ([vp, vp, vp, vp, vp, dp], i),
+        "accfft_c_divergence_adjoint": ([vp, vp, vp, vp, vp, dp], i),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -251,9 +255,26 @@ class PlanR2C(_Plan):
         _check(f(self._h, _ptr(div), _ptr(ax), _ptr(ay), _ptr(az), tp))
         self._timer_back(buf, timer)
 
-    def _op(self, name, out, a, timer):
+    # ---- adjoints (backward passes of accfft_gb300.autograd)
+    def r2c_adjoint(self, dX, du, timer=None):
+        self._op("r2c_adjoint", dX, du, timer)
+
+    def c2r_adjoint(self, dx, dY, timer=None):
+        self._op("c2r_adjoint", dx, dY, timer)
+
+    def grad_adjoint(self, out, gx, gy, gz, timer=None):
         buf, tp = self._timer(timer)
-        _check(getattr(lib(), "accfft_c_" + name)(self._h, _ptr(out), _ptr(a), tp))
+        _check(lib().accfft_c_grad_adjoint(self._h, _ptr(out), _ptr(gx), _ptr(gy), _ptr(gz), tp))
+        self._timer_back(buf, timer)
+
+    def divergence_adjoint(self, ax, ay, az, d, timer=None):
+        buf, tp = self._timer(timer)
+        _check(lib().accfft_c_divergence_adjoint(self._h, _ptr(ax), _ptr(ay), _ptr(az), _ptr(d), tp))
+        self._timer_back(buf, timer)
+
+    def _op(self, name, first, second, timer):
+        buf, tp = self._timer(timer)
+        _check(getattr(lib(), "accfft_c_" + name)(self._h, _ptr(first), _ptr(second), tp))
         self._timer_back(buf, timer)
 
     def laplace(self, out, a, timer=None):

@@ -47,6 +47,9 @@ struct ContigArgs {
   long long nlines;
   long long in_dist, out_dist;   // in elements of the array's own type
   int inverse;
+  // adjoint weighting of the half spectrum (interior planes 0 < kz < N2/2):
+  // 1 = k_zc2r reads them at weight 1/2, 2 = k_zr2c writes them at weight 2
+  int weight;
   SymArgs sym;
 };
 

@@ -277,11 +277,13 @@ k_zr2c(const ContigArgs a) {
   LN::template run<true, false>(t, static_cast<const V*>(a.tw), ld, xw, xw, xr);
   __syncthreads();
   const V* twp = static_cast<const V*>(a.tw_post);
+  const T wint = a.weight == 2 ? T(2) : T(1);
   // outputs k = t + r*P (r < E) cover 0..M-1; thread 0 also writes k = M
 #pragma unroll
   for (int r = 0; r < LN::E; ++r) {
     const int k = t + r * P;
     V x = r2c_split(xr(k), xr(k == 0 ? 0 : M - k), __ldg(twp + k));
+    if (k != 0) x = c_scale(x, wint);
     if (valid) out[k] = x;
   }
   if (t == 0) {
@@ -309,9 +311,16 @@ k_zc2r(const ContigArgs a) {
   }
   __syncthreads();
   const V* twp = static_cast<const V*>(a.tw_post);
+  const T wint = a.weight == 1 ? T(0.5) : T(1);
   auto ld = [&](int p) {
     V xk = xr(p), xm = xr(M - p);
-    if (p == 0) { xk.y = T(0); xm.y = T(0); }
+    if (p == 0) {
+      xk.y = T(0);
+      xm.y = T(0);
+    } else {
+      xk = c_scale(xk, wint);
+      xm = c_scale(xm, wint);
+    }
     return c_conj(c2r_merge(xk, xm, c_conj(__ldg(twp + p))));
   };
   auto st = [&](int p, V x) { x.y = -x.y; if (valid) out[p] = x; };

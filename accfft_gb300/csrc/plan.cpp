@@ -285,6 +285,7 @@ struct Exec {
   accfft_c_plan* p;
   double* timer;
   int rc = ACCFFT_C_OK;
+  int weight = 0;   // adjoint weighting of the z passes (ContigArgs::weight)
 
   Exec(accfft_c_plan* plan, double* t) : p(plan), timer(t) {
     if (p->blocking || timer) cudaEventRecord(p->ev0, p->stream);
@@ -333,6 +334,7 @@ struct Exec {
   void zr2c(const void* in, void* out, long long in_row) {
     if (!ok()) return;
     ContigArgs a{};
+    a.weight = weight;
     a.in = in;
     a.out = out;
     a.tw = p->tw_z;
@@ -345,6 +347,7 @@ struct Exec {
   void zc2r(const void* in, void* out, long long out_row) {
     if (!ok()) return;
     ContigArgs a{};
+    a.weight = weight;
     a.in = in;
     a.out = out;
     a.tw = p->tw_z;
@@ -359,6 +362,7 @@ struct Exec {
     if (!ok()) return;
     const long long N1 = p->n[1];
     ContigArgs a{};
+    a.weight = weight;
     a.in = static_cast<const char*>(in) + s0 * N1 * in_row * p->esz();
     a.out = static_cast<char*>(out) + s0 * N1 * p->H2() * 2 * p->esz();
     a.tw = p->tw_z;
@@ -372,6 +376,7 @@ struct Exec {
     if (!ok()) return;
     const long long N1 = p->n[1];
     ContigArgs a{};
+    a.weight = weight;
     a.in = static_cast<const char*>(in) + s0 * N1 * p->H2() * 2 * p->esz();
     a.out = static_cast<char*>(out) + s0 * N1 * out_row * p->esz();
     a.tw = p->tw_z;
@@ -403,7 +408,7 @@ struct Exec {
   // on a second stream.
   void zy(bool forward, const void* in, void* mid, void* out, long long row, bool host_real) {
     if (!ok()) return;
-    if (p->zy_mode == 1 && !host_real) {
+    if (p->zy_mode == 1 && !host_real && weight == 0) {
       slab(forward, in, out);
       return;
     }
@@ -565,7 +570,8 @@ int check_plan(accfft_c_plan* p, int kind, int dbl, const char* fn) {
 }
 
 // accfft_execute_gpu (src/accfft_gpu.cpp:444-623) at P = 1
-int exec_r2c_plan(accfft_c_plan* p, int direction, void* in, void* out, double* timer, unsigned xyz) {
+int exec_r2c_plan(accfft_c_plan* p, int direction, void* in, void* out, double* timer, unsigned xyz,
+                  int weight = 0) {
   if (!in) in = p->data;
   if (!out) out = p->data_out;
   if (!in || !out) return fail(ACCFFT_C_EINVAL, "execute: NULL data pointer and none given at plan time");
@@ -574,6 +580,7 @@ int exec_r2c_plan(accfft_c_plan* p, int direction, void* in, void* out, double* 
   const bool host_in = classify(in) == 1, host_out = classify(out) == 1;
   const long long h = p->H2();
   Exec ex(p, timer);
+  ex.weight = weight;
   if (direction == -1) {
     void* work = in;   // with z skipped the reference transforms the input in place
     if ((xyz & ZB) && (xyz & YB)) {
@@ -670,21 +677,22 @@ int op3d(accfft_c_plan* p, int sym_kind, void* outr, const void* inr, double* ti
 // to acc).  y and x lines view pairs of adjacent reals as one complex value:
 // the symbol i*w/N is Hermitian-consistent, so it maps real to real and acts
 // on both members of the pair independently.
-void deriv_axis(Exec& ex, accfft_c_plan* p, int axis, void* out, const void* in, const void* acc) {
+void deriv_axis(Exec& ex, accfft_c_plan* p, int axis, void* out, const void* in, const void* acc,
+                double alpha = 1.0) {
   const long long rr = p->rrow();
   const int N0 = p->n[0], N1 = p->n[1], N2 = p->n[2];
   if (axis == 2) {
-    ex.zsym(in, out, acc, rr, make_sym(p, SYM_DERIV1, 1.0 / N2, N2));
+    ex.zsym(in, out, acc, rr, make_sym(p, SYM_DERIV1, alpha / N2, N2));
     return;
   }
   const long long cr = rr / 2;            // complex pairs per stored row
   const long long cols = N2 / 2;          // pairs holding data
   if (axis == 1) {
     ex.strided_sym(in, out, acc, p->tw_y, N1, (long long)N0 * cols, cols, (long long)N1 * cr, cr,
-                   make_sym(p, SYM_DERIV1, 1.0 / N1, N1));
+                   make_sym(p, SYM_DERIV1, alpha / N1, N1));
   } else {
     ex.strided_sym(in, out, acc, p->tw_x, N0, (long long)N1 * cols, cols, cr, (long long)N1 * cr,
-                   make_sym(p, SYM_DERIV1, 1.0 / N0, N0));
+                   make_sym(p, SYM_DERIV1, alpha / N0, N0));
   }
 }
 
@@ -870,6 +878,41 @@ int accfft_c_divergence(accfft_c_plan* p, void* divA, const void* A_x, const voi
 int accfft_c_divergence_slow(accfft_c_plan* p, void* divA, const void* A_x, const void* A_y, const void* A_z,
                              double* timer) {
   return accfft_c_divergence(p, divA, A_x, A_y, A_z, timer);
+}
+
+// --- adjoints (no counterpart in the reference; used by the autograd layer)
+int accfft_c_r2c_adjoint(accfft_c_plan* p, const void* dX, void* du, double* timer) {
+  int rc = check_plan(p, 1, -1, "r2c_adjoint");
+  return rc ? rc : exec_r2c_plan(p, 1, const_cast<void*>(dX), du, timer, 7, 1);
+}
+int accfft_c_c2r_adjoint(accfft_c_plan* p, const void* dx, void* dY, double* timer) {
+  int rc = check_plan(p, 1, -1, "c2r_adjoint");
+  return rc ? rc : exec_r2c_plan(p, -1, const_cast<void*>(dx), dY, timer, 7, 2);
+}
+int accfft_c_grad_adjoint(accfft_c_plan* p, void* out, const void* g_x, const void* g_y, const void* g_z,
+                          double* timer) {
+  int rc = check_plan(p, 1, -1, "grad_adjoint");
+  if (rc) return rc;
+  if (!out || !g_x || !g_y || !g_z) return fail(ACCFFT_C_EINVAL, "grad_adjoint: NULL array");
+  if (int a = check_align(p, "grad_adjoint", {out, g_x, g_y, g_z})) return a;
+  if (int a = check_addressable("grad_adjoint", {out, g_x, g_y, g_z})) return a;
+  Exec ex(p, timer);
+  deriv_axis(ex, p, 0, out, g_x, nullptr, -1.0);
+  deriv_axis(ex, p, 1, out, g_y, out, -1.0);
+  deriv_axis(ex, p, 2, out, g_z, out, -1.0);
+  return ex.finish();
+}
+int accfft_c_divergence_adjoint(accfft_c_plan* p, void* a_x, void* a_y, void* a_z, const void* d, double* timer) {
+  int rc = check_plan(p, 1, -1, "divergence_adjoint");
+  if (rc) return rc;
+  if (!d || !a_x || !a_y || !a_z) return fail(ACCFFT_C_EINVAL, "divergence_adjoint: NULL array");
+  if (int a = check_align(p, "divergence_adjoint", {a_x, a_y, a_z, d})) return a;
+  if (int a = check_addressable("divergence_adjoint", {a_x, a_y, a_z, d})) return a;
+  Exec ex(p, timer);
+  deriv_axis(ex, p, 0, a_x, d, nullptr, -1.0);
+  deriv_axis(ex, p, 1, a_y, d, nullptr, -1.0);
+  deriv_axis(ex, p, 2, a_z, d, nullptr, -1.0);
+  return ex.finish();
 }
 
 }  // extern "C"

@@ -135,6 +135,22 @@ int accfft_c_biharmonic(accfft_c_plan* plan, void* BA, const void* A, double* ti
 int accfft_c_inv_laplace(accfft_c_plan* plan, void* invLA, const void* A, double* timer);
 int accfft_c_inv_biharmonic(accfft_c_plan* plan, void* invBA, const void* A, double* timer);
 
+/* --- adjoints ------------------------------------------------------------
+ * No counterpart in the reference; they are the backward passes of the
+ * autograd layer (accfft_gb300/autograd.py).  With R the unnormalised 3-D r2c
+ * of the plan and w the half-spectrum weights (1 on the kz = 0 and
+ * kz = N2/2 planes, 2 on the interior planes, so that c2r(Y) = Re sum w Y e^{+i theta}):
+ *   r2c_adjoint:  du = R^T dX = Re sum_k dX_k e^{+i theta}  = c2r(dX / w)
+ *   c2r_adjoint:  dY = w * R dx                            = w * r2c(dx)
+ *   grad_adjoint: out = -(d g_x/dx + d g_y/dy + d g_z/dz)  (the transpose of grad)
+ *   divergence_adjoint: (a_x, a_y, a_z) = -grad(d)          (the transpose of divergence)
+ * The weights are applied inside the z kernels; no extra pass runs. */
+int accfft_c_r2c_adjoint(accfft_c_plan* plan, const void* dX, void* du, double* timer);
+int accfft_c_c2r_adjoint(accfft_c_plan* plan, const void* dx, void* dY, double* timer);
+int accfft_c_grad_adjoint(accfft_c_plan* plan, void* out, const void* g_x, const void* g_y, const void* g_z,
+                          double* timer);
+int accfft_c_divergence_adjoint(accfft_c_plan* plan, void* a_x, void* a_y, void* a_z, const void* d, double* timer);
+
 /* --- Laplacian without device allocation ------------------------------
  * No counterpart in the reference.  For callers that may not call cudaMalloc
  * (a plugin in an application whose memory manager has reserved the whole
