@@ -74,6 +74,7 @@ def lib() -> ctypes.CDLL:
         "accfft_c_destroy_plan": ([vp], None),
         "accfft_c_plan_info": ([vp, ip, ip, ip, ip, ctypes.POINTER(ll)], i),
         "accfft_c_set_stream": ([vp, vp, i], i),
+        "accfft_c_set_zy_schedule": ([vp, i], i),
         "accfft_c_execute_r2c_gpu": ([vp, vp, vp, dp, u], i),
         "accfft_c_execute_c2r_gpu": ([vp, vp, vp, dp, u], i),
         "accfft_c_execute_gpu": ([vp, i, vp, vp, dp, u], i),
@@ -93,6 +94,8 @@ def lib() -> ctypes.CDLL:
         "accfft_c_inv_laplace": ([vp, vp, vp, dp], i),
         "accfft_c_inv_biharmonic": ([vp, vp, vp, dp], i),
         "accfft_c_laplace_gpuf_noalloc": ([ip, vp, vp, vp], i),
+        "accfft_c_heat": ([vp, vp, vp, ctypes.c_double, dp], i),
+        "accfft_c_helmholtz": ([vp, vp, vp, ctypes.c_double, dp], i),
         "accfft_c_r2c_adjoint": ([vp, vp, vp, dp], i),
         "accfft_c_c2r_adjoint": ([vp, vp, vp, dp], i),
         "accfft_c_grad_adjoint": ([vp, vp, vp, vp, vp, dp], i),
@@ -185,6 +188,10 @@ class _Plan:
         s = getattr(stream, "cuda_stream", stream)
         _check(lib().accfft_c_set_stream(self._h, s, 1 if blocking else 0))
 
+    def set_zy_schedule(self, mode):
+        """0: separate z and y passes (default); 1: cluster slab kernel (r2c plans)"""
+        _check(lib().accfft_c_set_zy_schedule(self._h, int(mode)))
+
     def destroy(self):
         if getattr(self, "_h", None):
             lib().accfft_c_destroy_plan(self._h)
@@ -253,6 +260,19 @@ class PlanR2C(_Plan):
         buf, tp = self._timer(timer)
         f = lib().accfft_c_divergence_slow if slow else lib().accfft_c_divergence
         _check(f(self._h, _ptr(div), _ptr(ax), _ptr(ay), _ptr(az), tp))
+        self._timer_back(buf, timer)
+
+    # ---- spectral solvers
+    def heat(self, out, a, t, timer=None):
+        """exact heat propagator exp(t * laplace) applied to a"""
+        buf, tp = self._timer(timer)
+        _check(lib().accfft_c_heat(self._h, _ptr(out), _ptr(a), float(t), tp))
+        self._timer_back(buf, timer)
+
+    def helmholtz(self, out, a, alpha, timer=None):
+        """solve (alpha - laplace) out = a (zero mean part dropped where alpha + |k|^2 = 0)"""
+        buf, tp = self._timer(timer)
+        _check(lib().accfft_c_helmholtz(self._h, _ptr(out), _ptr(a), float(alpha), tp))
         self._timer_back(buf, timer)
 
     # ---- adjoints (backward passes of accfft_gb300.autograd)

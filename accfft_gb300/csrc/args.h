@@ -14,7 +14,9 @@ enum SymKind {
   SYM_GRADY = 6,
   SYM_GRADZ = 7,
   SYM_DERIV1 = 8,       // i * w(p) * scale (1-D symbol along the pass axis)
-  SYM_DERIV2 = 9        // -w(p)^2 * scale
+  SYM_DERIV2 = 9,       // -w(p)^2 * scale
+  SYM_HEAT = 10,        // exp(-(wx^2+wy^2+wz^2) * param) * scale
+  SYM_HELMHOLTZ = 11    // scale / (param + wx^2+wy^2+wz^2), 0 where that is 0
 };
 
 struct SymArgs {
@@ -23,6 +25,7 @@ struct SymArgs {
   int h2;           // spectrum columns per y row (N2/2+1 for r2c spectra)
   int axis_len;     // line length for the 1-D symbols
   double scale;
+  double param;     // time (SYM_HEAT) or shift (SYM_HELMHOLTZ)
 };
 
 struct StridedArgs {

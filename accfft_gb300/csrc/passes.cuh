@@ -46,7 +46,7 @@ struct SymCol {
 };
 __device__ __forceinline__ SymCol sym_column(const SymArgs& s, long long g) {
   SymCol c{0, 0, 0, 0};
-  if (s.kind >= SYM_LAPLACE && s.kind <= SYM_GRADZ) {
+  if ((s.kind >= SYM_LAPLACE && s.kind <= SYM_GRADZ) || s.kind == SYM_HEAT || s.kind == SYM_HELMHOLTZ) {
     int y = int(g / s.h2), kz = int(g - (long long)y * s.h2);
     c.wy = fold_wave(y, s.n1); c.wz = fold_wave(kz, s.n2);
     c.wy_nf = fold_wave_nofilter(y, s.n1); c.wz_nf = fold_wave_nofilter(kz, s.n2);
@@ -94,6 +94,16 @@ __device__ __forceinline__ V sym_apply(const SymArgs& s, const SymCol& c, int p,
     case SYM_DERIV2: {
       int w = fold_wave_line(p, s.axis_len);
       return c_scale(x, -T(w * w) * sc);
+    }
+    case SYM_HEAT: {
+      int wx = fold_wave(p, s.n0);
+      T k2 = T(wx * wx + c.wy * c.wy + c.wz * c.wz);
+      return c_scale(x, exp(-k2 * T(s.param)) * sc);
+    }
+    case SYM_HELMHOLTZ: {
+      int wx = fold_wave(p, s.n0);
+      T d = T(s.param) + T(wx * wx + c.wy * c.wy + c.wz * c.wz);
+      return c_scale(x, d == T(0) ? T(0) : sc / d);
     }
     default:
       return x;

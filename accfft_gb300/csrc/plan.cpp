@@ -656,7 +656,7 @@ SymArgs make_sym(const accfft_c_plan* p, int kind, double scale, int axis_len = 
 
 // full 3-D operator: r2c (z, y) -> fused x pass (forward, symbol, inverse) ->
 // inverse y -> c2r, through the plan scratch spectrum
-int op3d(accfft_c_plan* p, int sym_kind, void* outr, const void* inr, double* timer) {
+int op3d(accfft_c_plan* p, int sym_kind, void* outr, const void* inr, double* timer, double param = 0.0) {
   if (!outr || !inr) return fail(ACCFFT_C_EINVAL, "operator: NULL array");
   if (int rc = check_align(p, "operator", {outr, inr})) return rc;
   if (int rc = check_addressable("operator", {outr, inr})) return rc;
@@ -667,7 +667,9 @@ int op3d(accfft_c_plan* p, int sym_kind, void* outr, const void* inr, double* ti
   ex.zr2c(inr, s, p->rrow());
   ex.ypass(s, s, h, 0);
   long long c = (long long)p->n[1] * h;
-  ex.strided_sym(s, s, nullptr, p->tw_x, p->n[0], c, c, 0, c, make_sym(p, sym_kind, 1.0 / N));
+  SymArgs sym = make_sym(p, sym_kind, 1.0 / N);
+  sym.param = param;
+  ex.strided_sym(s, s, nullptr, p->tw_x, p->n[0], c, c, 0, c, sym);
   ex.ypass(s, s, h, 1);
   ex.zc2r(s, outr, p->rrow());
   return ex.finish();
@@ -758,6 +760,22 @@ int accfft_c_plan_info(const accfft_c_plan* p, int n[3], int* kind, int* is_doub
   if (inplace) *inplace = p->inplace;
   if (alloc_max) *alloc_max = p->alloc_max;
   return ACCFFT_C_OK;
+}
+
+int accfft_c_set_zy_schedule(accfft_c_plan* p, int mode) {
+  if (!p) return fail(ACCFFT_C_EINVAL, "set_zy_schedule: NULL plan");
+  if (p->kind != 1) return fail(ACCFFT_C_ENOTBAKED, "set_zy_schedule: r2c plans only");
+  if (mode == 0) {
+    p->zy_mode = 0;
+    return ACCFFT_C_OK;
+  }
+  if (mode == 1) {
+    if (!slab_available(p->dbl, p->n[1], p->n[2]))
+      return fail(ACCFFT_C_EUNSUPPORTED, "set_zy_schedule: no slab kernel for %dx%d", p->n[1], p->n[2]);
+    p->zy_mode = 1;
+    return ACCFFT_C_OK;
+  }
+  return fail(ACCFFT_C_EINVAL, "set_zy_schedule: mode must be 0 (separate passes) or 1 (cluster slab kernel)");
 }
 
 int accfft_c_set_stream(accfft_c_plan* p, void* stream, int blocking) {
@@ -913,6 +931,20 @@ int accfft_c_divergence_adjoint(accfft_c_plan* p, void* a_x, void* a_y, void* a_
   deriv_axis(ex, p, 1, a_y, d, nullptr, -1.0);
   deriv_axis(ex, p, 2, a_z, d, nullptr, -1.0);
   return ex.finish();
+}
+
+// --- spectral solvers (no GPU counterpart in the reference; the analogues of
+// the Poisson filter of steps/step4/kernels.cu and the exact heat propagator
+// of steps/step6/step6.cpp, on the operators' folded wave numbers)
+int accfft_c_heat(accfft_c_plan* p, void* out, const void* in, double t, double* timer) {
+  int rc = check_plan(p, 1, -1, "heat");
+  if (rc) return rc;
+  if (!(t >= 0)) return fail(ACCFFT_C_EINVAL, "heat: time must be >= 0");
+  return op3d(p, SYM_HEAT, out, in, timer, t);
+}
+int accfft_c_helmholtz(accfft_c_plan* p, void* out, const void* in, double alpha, double* timer) {
+  int rc = check_plan(p, 1, -1, "helmholtz");
+  return rc ? rc : op3d(p, SYM_HELMHOLTZ, out, in, timer, alpha);
 }
 
 }  // extern "C"

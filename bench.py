@@ -46,6 +46,9 @@ def parse():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="pairs", choices=["pairs", "precision", "adjoint", "batch"],
+                    help="pairs: the 512^3 r2c+c2r headline; precision: 1024^3 float32 vs the FP64 "
+                         "drop-in against the oracle; adjoint: 256^3 differentiation; batch: 64 uneven grids")
     ap.add_argument("--n", type=int, default=512)
     ap.add_argument("--grid", type=int, nargs=3, default=None,
                     help="non-cubic grid N0 N1 N2 (smaller cases of the same kernels for profiling)")
@@ -354,10 +357,196 @@ def ours(args):
     print(json.dumps(line), flush=True)
 
 
+
+def _oracle():
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import accfft_oracle as orc
+
+    orc.build()
+    return orc
+
+
+def precision_workload(args):
+    """1024^3 real field from a turbulence-like random Fourier series
+    (amplitude N(0,1)|k|^-5/3 for 0 < |k| <= 256, uniform phases), rounded to
+    float32; r2c + c2r in float32 and with the FP64 drop-in, each result
+    against the oracle (double, host cores) applied to the same input."""
+    import torch
+
+    import accfft_gb300 as ag
+
+    orc = _oracle()
+    n = tuple(args.grid) if args.grid else (1024, 1024, 1024)
+    N0, N1, N2 = n
+    N = N0 * N1 * N2
+    g = torch.Generator(device="cuda").manual_seed(31)
+    kx = torch.fft.fftfreq(N0, 1.0 / N0, device="cuda", dtype=torch.float64)[:, None, None]
+    ky = torch.fft.fftfreq(N1, 1.0 / N1, device="cuda", dtype=torch.float64)[None, :, None]
+    kz = torch.arange(N2 // 2 + 1, device="cuda", dtype=torch.float64)[None, None, :]
+    kk = torch.sqrt(kx * kx + ky * ky + kz * kz)
+    amp = torch.randn(kk.shape, generator=g, device="cuda", dtype=torch.float64) * torch.where(
+        (kk > 0) & (kk <= 256), kk.clamp(min=1) ** (-5.0 / 3.0), torch.zeros_like(kk))
+    ph = 2 * np.pi * torch.rand(kk.shape, generator=g, device="cuda", dtype=torch.float64)
+    X = torch.polar(amp, ph)
+    del kk, amp, ph
+    p64 = ag.PlanR2C(n, "float64")
+    u64 = torch.empty(n, dtype=torch.float64, device="cuda")
+    p64.c2r(torch.view_as_real(X), u64)
+    del X
+    u64 /= u64.std()
+    u32 = u64.float()
+    uq = u32.double()
+    del u64
+    res = {}
+    host_u = uq.cpu().numpy()
+    t0 = time.perf_counter()
+    ref_spec = orc.r2c(host_u)
+    oracle_s = time.perf_counter() - t0
+    for name, dt in (("fp32_cuda_core", "float32"), ("fp64_drop_in", "float64")):
+        plan = ag.PlanR2C(n, dt)
+        x = u32 if dt == "float32" else uq
+        spec = torch.empty((N0, N1, N2 // 2 + 1, 2), dtype=x.dtype, device="cuda")
+        back = torch.empty(n, dtype=x.dtype, device="cuda")
+        plan.r2c(x, spec)
+        plan.c2r(spec, back)
+        torch.cuda.synchronize()
+        s = spec.double().cpu().numpy()
+        e_fwd = orc.rel_l2(s[..., 0] + 1j * s[..., 1], ref_spec)
+        e_rt = ((back.double() / N - uq).norm() / uq.norm()).item()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        reps = 5 if dt == "float32" else 2
+        a.record()
+        for _ in range(reps):
+            plan.r2c(x, spec)
+            plan.c2r(spec, back)
+        b.record()
+        torch.cuda.synchronize()
+        ms = a.elapsed_time(b) / reps
+        res[name] = {"r2c_rel_l2_vs_oracle": e_fwd, "roundtrip_rel_l2": e_rt, "ms_per_pair": ms,
+                     "pairs_per_s": 1000.0 / ms}
+        plan.destroy()
+        del spec, back
+    res["tensor_core_split_bf16_3xtf32"] = "not built: the float32 path is HBM-bound with CUDA-core radix stages"
+    line = {"metric": f"{N0}x{N1}x{N2} precision (rel-L2 vs FP64 oracle)", "workload": "precision",
+            "value": res["fp32_cuda_core"]["r2c_rel_l2_vs_oracle"], "unit": "rel-L2", "higher_is_better": False,
+            "variants": res, "oracle_seconds_r2c": oracle_s, "oracle_threads": os.cpu_count(),
+            "speedup_fp32_over_fp64": res["fp64_drop_in"]["ms_per_pair"] / res["fp32_cuda_core"]["ms_per_pair"],
+            "data": "synthetic turbulence-like spectrum, seeded"}
+    print(json.dumps(line), flush=True)
+
+
+def adjoint_workload(args):
+    """256^3 float32 differentiation: L(u) = 0.5|grad u|^2 + <f, inv_laplace u>,
+    forward + backward through the adjoint kernels; FP64 central differences
+    along 16 random directions."""
+    import torch
+
+    import accfft_gb300 as ag
+    import accfft_gb300.autograd as ad
+
+    n = (256, 256, 256)
+    r = np.random.default_rng(11)
+    U = np.fft.rfftn(r.standard_normal(n))
+    k = [np.fft.fftfreq(m) for m in n[:2]] + [np.fft.rfftfreq(n[2])]
+    kk = k[0][:, None, None] ** 2 + k[1][None, :, None] ** 2 + k[2][None, None, :] ** 2
+    u64 = torch.tensor(np.fft.irfftn(U * np.exp(-2 * np.pi ** 2 * 16.0 * kk), s=n, axes=(0, 1, 2)), device="cuda")
+    f64 = torch.tensor(np.random.default_rng(12).standard_normal(n), device="cuda")
+    p32, p64 = ag.PlanR2C(n, "float32"), ag.PlanR2C(n, "float64")
+
+    def loss(plan, u, f):
+        gx, gy, gz = ad.grad(u, plan)
+        return 0.5 * ((gx * gx).sum() + (gy * gy).sum() + (gz * gz).sum()) + (f * ad.inv_laplace(u, plan)).sum()
+
+    u32, f32 = u64.float(), f64.float()
+
+    def fwd_bwd():
+        x = u32.clone().requires_grad_(True)
+        (gg,) = torch.autograd.grad(loss(p32, x, f32), x)
+        return gg
+
+    for _ in range(3):
+        g32 = fwd_bwd()
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(10):
+        g32 = fwd_bwd()
+    b.record()
+    torch.cuda.synchronize()
+    ms = a.elapsed_time(b) / 10
+    xd = u64.clone().requires_grad_(True)
+    (g64,) = torch.autograd.grad(loss(p64, xd, f64), xd)
+    gen = torch.Generator(device="cuda").manual_seed(13)
+    w64 = w32 = 0.0
+    with torch.no_grad():
+        for _ in range(16):
+            v = torch.randn(n, dtype=torch.float64, device="cuda", generator=gen)
+            fd = (loss(p64, u64 + 1e-6 * v, f64).item() - loss(p64, u64 - 1e-6 * v, f64).item()) / 2e-6
+            w64 = max(w64, abs((g64 * v).sum().item() - fd) / abs(fd))
+            w32 = max(w32, abs((g32.double() * v).sum().item() - fd) / abs(fd))
+    line = {"metric": "256^3 float32 loss forward+backward ms (adjoint kernels)", "workload": "adjoint",
+            "value": ms, "unit": "ms", "higher_is_better": False,
+            "fd64_rel_err_worst_of_16": {"fp64_backward": w64, "fp32_backward": w32},
+            "note": "fp32 directional derivatives along random N(0,1) directions are bounded by ~eps32*sqrt(N)",
+            "data": "synthetic Gaussian-smoothed N(0,1) field, seeded"}
+    print(json.dumps(line), flush=True)
+
+
+def batch_workload(args):
+    """64 independent grids drawn with a seed from {32^3, 48^3, 64^3, 96^3,
+    128^3, 160x180x200, 192^3, 256^3}: half r2c+c2r, half laplace then
+    inv_laplace, inputs U[-1, 1]; one CUDA-graph launch per batch."""
+    import torch
+
+    from accfft_gb300.batch import BatchPlan
+
+    orc = _oracle()
+    sizes = [(32,) * 3, (48,) * 3, (64,) * 3, (96,) * 3, (128,) * 3, (160, 180, 200), (192,) * 3, (256,) * 3]
+    r = np.random.default_rng(41)
+    specs = [(sizes[r.integers(len(sizes))], "r2c_c2r" if i % 2 == 0 else "lap_invlap") for i in range(64)]
+    bp = BatchPlan(specs, "float32")
+    host = [r.uniform(-1, 1, s).astype(np.float32) for s, _ in specs]
+    bp.set_inputs([torch.from_numpy(h).cuda() for h in host])
+    tune = bp.tune()
+    bp.capture()
+    for _ in range(3):
+        bp.run()
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = 20
+    a.record()
+    for _ in range(reps):
+        bp.run()
+    b.record()
+    torch.cuda.synchronize()
+    ms = a.elapsed_time(b) / reps
+    errs = []
+    for (shape, op), h, out in zip(specs, host, bp.outputs):
+        u = h.astype(np.float64)
+        if op == "r2c_c2r":
+            ref = orc.c2r(orc.r2c(u), shape[2])
+        else:
+            ref = orc.spectral_op(orc.spectral_op(u, "laplace"), "inv_laplace")
+        errs.append(orc.rel_l2(out.cpu().numpy().astype(np.float64), ref))
+    line = {"metric": "64 uneven grids, transforms/s (one graph launch)", "workload": "batch",
+            "value": bp.transforms / (ms / 1000.0), "unit": "transforms/s", "higher_is_better": True,
+            "ms_per_batch": ms, "transforms_per_batch": bp.transforms, "streams": tune["streams"],
+            "schedule": tune["schedule"], "radix_plans": bp.report(),
+            "rel_l2_vs_oracle": {"max": max(errs), "median": float(np.median(errs))},
+            "data": "synthetic U[-1,1], seeded"}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         reference_arm(args)
+    elif args.workload == "precision":
+        precision_workload(args)
+    elif args.workload == "adjoint":
+        adjoint_workload(args)
+    elif args.workload == "batch":
+        batch_workload(args)
     else:
         ours(args)
 

@@ -80,6 +80,10 @@ void accfft_c_destroy_plan(accfft_c_plan* plan);
 /* kind: 1 = r2c, 2 = c2c; is_double: 1 for the double plans */
 int accfft_c_plan_info(const accfft_c_plan* plan, int n[3], int* kind, int* is_double, int* inplace,
                        long long* alloc_max);
+/* extension: how an r2c plan runs its z and y passes: 0 = one kernel per
+ * pass over the whole grid (default), 1 = one thread-block-cluster kernel per
+ * x-slab doing both (ACCFFT_C_EUNSUPPORTED when the grid has none) */
+int accfft_c_set_zy_schedule(accfft_c_plan* plan, int mode);
 /* extension: enqueue on `stream` (a cudaStream_t); blocking = 0 returns
  * without waiting (timer slots are then not updated) */
 int accfft_c_set_stream(accfft_c_plan* plan, void* stream, int blocking);
@@ -134,6 +138,18 @@ int accfft_c_divergence_slow(accfft_c_plan* plan, void* divA, const void* A_x, c
 int accfft_c_biharmonic(accfft_c_plan* plan, void* BA, const void* A, double* timer);
 int accfft_c_inv_laplace(accfft_c_plan* plan, void* invLA, const void* A, double* timer);
 int accfft_c_inv_biharmonic(accfft_c_plan* plan, void* invBA, const void* A, double* timer);
+
+/* --- spectral solvers -------------------------------------------------------
+ * No GPU counterpart in the reference.  With the operators' wave numbers
+ * (w = i, i - N above N/2, 0 at N/2 on each axis) and |k|^2 = wx^2 + wy^2 + wz^2:
+ *   heat:      out = c2r(exp(-t |k|^2) r2c(in)) / N   - the exact solution at
+ *              time t of u_t = laplace(u) from u(0) = in (as steps/step6 checks)
+ *   helmholtz: out = c2r(r2c(in) / (alpha + |k|^2)) / N - solves
+ *              (alpha - laplace) out = in; 0 where alpha + |k|^2 = 0, so alpha = 0
+ *              gives the zero-mean Poisson solution -inv_laplace (as steps/step4)
+ * Each is one fused operator: z r2c, y, x forward * symbol * x backward, y, z c2r. */
+int accfft_c_heat(accfft_c_plan* plan, void* out, const void* in, double t, double* timer);
+int accfft_c_helmholtz(accfft_c_plan* plan, void* out, const void* in, double alpha, double* timer);
 
 /* --- adjoints ------------------------------------------------------------
  * No counterpart in the reference; they are the backward passes of the

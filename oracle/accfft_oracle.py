@@ -225,7 +225,7 @@ def _waves(n, h2, nyquist_zero=True):
     return wx, wy, wz
 
 
-def symbol(kind: str, n) -> np.ndarray:
+def symbol(kind: str, n, param: float = 0.0) -> np.ndarray:
     """Multipliers applied to the r2c spectrum by the reference's operators:
     laplace/biharmonic (src/operators_cuda.cu:115-205), inv_laplace
     (src/operators.txx:276-333), inv_biharmonic (src/operators.txx:336-388),
@@ -251,6 +251,14 @@ def symbol(kind: str, n) -> np.ndarray:
         nz = w != 0
         out[nz] = 1.0 / w[nz]
         return scale * out
+    if kind == "heat":
+        return scale * np.exp(-(wx * wx + wy * wy + wz * wz).astype(np.float64) * param)
+    if kind == "helmholtz":
+        d = param + (wx * wx + wy * wy + wz * wz).astype(np.float64)
+        out = np.zeros_like(d)
+        nz = d != 0
+        out[nz] = scale / d[nz]
+        return out
     if kind in ("gradx", "grady", "gradz"):
         w = {"gradx": wx, "grady": wy, "gradz": wz}[kind]
         return 1j * scale * np.broadcast_to(w, (n0, n1, h2)).astype(np.float64)
@@ -258,11 +266,12 @@ def symbol(kind: str, n) -> np.ndarray:
 
 
 # ----------------------------------------------------------- operators
-def spectral_op(u: np.ndarray, kind: str, prec="d", nthreads=0) -> np.ndarray:
+def spectral_op(u: np.ndarray, kind: str, prec="d", nthreads=0, param: float = 0.0) -> np.ndarray:
     """r2c -> multiply -> c2r (accfft_laplace_gpu_t, src/operators_gpu.txx:281-334,
-    and its biharmonic twin :556-609; inv_laplace per src/operators.txx:1270-1322)."""
+    and its biharmonic twin :556-609; inv_laplace per src/operators.txx:1270-1322;
+    heat / helmholtz are this library's solvers on the same wave numbers)."""
     n = u.shape
-    s = r2c(u, 7, prec, nthreads) * symbol(kind, n)
+    s = r2c(u, 7, prec, nthreads) * symbol(kind, n, param)
     return c2r(s, n[2], 7, prec, nthreads)
 
 

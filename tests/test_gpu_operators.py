@@ -91,3 +91,39 @@ def test_step5_closed_forms_on_gpu(cuda, native):
     div = empty(torch, n, "float64")
     plan.divergence(div, *g)
     assert rel_l1(from_dev(div), step5_laplace(n)) < 1e-10
+
+
+@pytest.mark.parametrize("dtype", ["float64", "float32"])
+@pytest.mark.parametrize("n", [(16, 12, 10), (48, 96, 64), (128, 128, 128)])
+def test_heat_and_helmholtz(cuda, native, oracle, n, dtype):
+    torch = cuda
+    u = rng(55).standard_normal(n)
+    uq = u.astype(dtype).astype(np.float64)
+    plan = native.PlanR2C(n, dtype)
+    du = to_dev(torch, u, dtype)
+    out = empty(torch, n, dtype)
+    for t in (0.0, 1e-3, 0.1):
+        plan.heat(out, du, t)
+        assert oracle.rel_l2(from_dev(out), oracle.spectral_op(uq, "heat", param=t)) < TOL[dtype]
+    for alpha in (0.0, 1.0, 7.5):
+        plan.helmholtz(out, du, alpha)
+        assert oracle.rel_l2(from_dev(out), oracle.spectral_op(uq, "helmholtz", param=alpha)) < TOL[dtype]
+
+
+def test_heat_exact_solution_and_poisson(cuda, native, oracle):
+    """sin x sin y sin z decays as exp(-3t) under the heat propagator
+    (steps/step6/step6.cpp:31-97 checks the same kind of exact solution), and
+    solves (alpha - laplace) v = (alpha + 3) sin x sin y sin z."""
+    torch = cuda
+    n = (64, 64, 64)
+    X, Y, Z = np.meshgrid(*[2 * np.pi * np.arange(k) / k for k in n], indexing="ij")
+    s = np.sin(X) * np.sin(Y) * np.sin(Z)
+    plan = native.PlanR2C(n, "float64")
+    ds = to_dev(torch, s, "float64")
+    out = empty(torch, n, "float64")
+    plan.heat(out, ds, 0.25)
+    assert np.abs(from_dev(out) - np.exp(-0.75) * s).max() < 1e-13
+    plan.helmholtz(out, to_dev(torch, (2.0 + 3.0) * s, "float64"), 2.0)
+    assert np.abs(from_dev(out) - s).max() < 1e-13
+    plan.helmholtz(out, to_dev(torch, -3.0 * s, "float64"), 0.0)   # Poisson: -laplace v = -3 s -> v = -s
+    assert np.abs(from_dev(out) + s).max() < 1e-13
