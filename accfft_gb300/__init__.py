@@ -75,6 +75,8 @@ def lib() -> ctypes.CDLL:
         "accfft_c_plan_info": ([vp, ip, ip, ip, ip, ctypes.POINTER(ll)], i),
         "accfft_c_set_stream": ([vp, vp, i], i),
         "accfft_c_set_zy_schedule": ([vp, i], i),
+        "accfft_c_set_profiling": ([vp, i], i),
+        "accfft_c_profile_read": ([vp, i, ctypes.c_char_p, ctypes.POINTER(ll), dp], i),
         "accfft_c_execute_r2c_gpu": ([vp, vp, vp, dp, u], i),
         "accfft_c_execute_c2r_gpu": ([vp, vp, vp, dp, u], i),
         "accfft_c_execute_gpu": ([vp, i, vp, vp, dp, u], i),
@@ -187,6 +189,20 @@ class _Plan:
         """Enqueue on a CUDA stream (cudaStream_t as int, or a torch.cuda.Stream)."""
         s = getattr(stream, "cuda_stream", stream)
         _check(lib().accfft_c_set_stream(self._h, s, 1 if blocking else 0))
+
+    def set_profiling(self, on=True):
+        """bracket every kernel of this plan with CUDA events (read with profile())"""
+        _check(lib().accfft_c_set_profiling(self._h, 1 if on else 0))
+
+    def profile(self):
+        """{pass label: (launches, total ms)} since the previous call"""
+        n = 64
+        labels = ctypes.create_string_buffer(32 * n)
+        counts = (ctypes.c_longlong * n)()
+        ms = (ctypes.c_double * n)()
+        k = lib().accfft_c_profile_read(self._h, n, labels, counts, ms)
+        raw = labels.raw
+        return {raw[32 * i:32 * i + 32].split(b"\0")[0].decode(): (int(counts[i]), float(ms[i])) for i in range(k)}
 
     def set_zy_schedule(self, mode):
         """0: separate z and y passes (default); 1: cluster slab kernel (r2c plans)"""

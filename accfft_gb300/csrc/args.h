@@ -39,6 +39,14 @@ struct StridedArgs {
   long long out_slab, out_line;
   int inverse;              // MODE 0: conjugate on load and store
   SymArgs sym;              // MODE 1
+  // split layout (aligned main part + Nyquist plane): when ncols_main > 0,
+  // columns g >= ncols_main are Nyquist columns: column j = g - ncols_main
+  // reads in_nyq + j*nyq_slab and writes out_nyq + j*nyq_slab, line stride
+  // nyq_line; the main columns g < ncols_main use the fields above
+  long long ncols_main;
+  const void* in_nyq;
+  void* out_nyq;
+  long long nyq_slab, nyq_line;
 };
 
 struct ContigArgs {
@@ -53,6 +61,10 @@ struct ContigArgs {
   // adjoint weighting of the half spectrum (interior planes 0 < kz < N2/2):
   // 1 = k_zc2r reads them at weight 1/2, 2 = k_zr2c writes them at weight 2
   int weight;
+  // separate Nyquist plane: k_zr2c writes X[M] of line l to nyq_out[l] (and
+  // rows of M entries), k_zc2r reads it from nyq_in[l]
+  void* nyq_out;
+  const void* nyq_in;
   SymArgs sym;
 };
 

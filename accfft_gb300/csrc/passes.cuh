@@ -54,6 +54,15 @@ __device__ __forceinline__ SymCol sym_column(const SymArgs& s, long long g) {
   return c;
 }
 
+// a column of the Nyquist plane of the split layout: y = j, kz = N2/2
+__device__ __forceinline__ SymCol sym_column_nyq(const SymArgs& s, long long j) {
+  SymCol c{0, 0, 0, 0};
+  int y = int(j), kz = s.n2 / 2;
+  c.wy = fold_wave(y, s.n1); c.wz = fold_wave(kz, s.n2);
+  c.wy_nf = fold_wave_nofilter(y, s.n1); c.wz_nf = fold_wave_nofilter(kz, s.n2);
+  return c;
+}
+
 // multiply x (frequency p along the pass axis, column part c) by the symbol
 template <typename T, typename V>
 __device__ __forceinline__ V sym_apply(const SymArgs& s, const SymCol& c, int p, V x) {
@@ -155,16 +164,24 @@ k_strided(const StridedArgs a) {
   const long long g = (long long)blockIdx.x * TC + c;
   const bool valid = g < a.ncols;
   const long long gs = valid ? g : 0;          // idle lanes read column 0, store nothing
-  const long long slab = gs / a.cps;
-  const long long cc = gs - slab * a.cps;
+  long long slab = gs / a.cps;
+  long long cc = gs - slab * a.cps;
   const V* in = static_cast<const V*>(a.in) + slab * a.in_slab + cc;
   V* out = static_cast<V*>(a.out) + slab * a.out_slab + cc;
+  long long il = a.in_line, ol = a.out_line;
+  if (a.ncols_main > 0 && gs >= a.ncols_main) {   // a Nyquist column of the split layout
+    const long long j = gs - a.ncols_main;
+    in = static_cast<const V*>(a.in_nyq) + j * a.nyq_slab;
+    out = static_cast<V*>(a.out_nyq) + j * a.nyq_slab;
+    il = ol = a.nyq_line;
+    slab = j;
+    cc = -1;
+  }
   const V* tw = static_cast<const V*>(a.tw);
   auto xw = [&](int p, V x) { sm[p * TC + c] = x; };
   auto xr = [&](int p) { return sm[p * TC + c]; };
   if constexpr (MODE == 0) {
     const T sg = a.inverse ? T(-1) : T(1);
-    const long long il = a.in_line, ol = a.out_line;
     auto ld = [&](int p) { V x = in[p * il]; x.y *= sg; return x; };
     auto st = [&](int p, V x) { x.y *= sg; if (valid) out[p * ol] = x; };
     LN::template run<false, false>(t, tw, ld, st, xw, xr);
@@ -172,7 +189,6 @@ k_strided(const StridedArgs a) {
     // real transform along the line of column pairs (2cc, 2cc+1) packed as
     // u = a + i*b: A[k] = (U[k] + conj U[L-k])/2, B[k] = (U[k] - conj U[L-k])/(2i),
     // written to the half spectrum at complex columns 2cc and 2cc+1
-    const long long il = a.in_line, ol = a.out_line;
     V* o2 = static_cast<V*>(a.out) + slab * a.out_slab + 2 * cc;
     auto ld = [&](int p) { return in[p * il]; };
     LN::template run<true, false>(t, tw, ld, xw, xw, xr);
@@ -194,7 +210,6 @@ k_strided(const StridedArgs a) {
     // inverse of MODE 2: U[k] = A[k] + i B[k], U[L-k] = conj A[k] + i conj B[k]
     // (imaginary parts of A, B at k = 0 and k = L/2 dropped), inverse complex
     // FFT, the real pair (a, b) stored at columns (2cc, 2cc+1)
-    const long long il = a.in_line, ol = a.out_line;
     const V* i2 = static_cast<const V*>(a.in) + slab * a.in_slab + 2 * cc;
 #pragma unroll
     for (int r = 0; r < LN::E; ++r) {
@@ -211,14 +226,16 @@ k_strided(const StridedArgs a) {
     auto st = [&](int p, V x) { x.y = -x.y; if (valid) out[p * ol] = x; };
     LN::template run<false, true>(t, tw, xr, st, xw, xr);
   } else {
-    const SymCol scol = sym_column(a.sym, gs);
-    const long long il = a.in_line, ol = a.out_line;
+    // the symbol sees the column as (y, kz); Nyquist column j of the split
+    // layout is (j, N2/2)
+    const SymCol scol = cc >= 0 ? sym_column(a.sym, gs) : sym_column_nyq(a.sym, slab);
     auto ld = [&](int p) { return in[p * il]; };
     // forward result times the symbol, stored conjugated for the inverse run
     auto sst = [&](int p, V x) { sm[p * TC + c] = c_conj(sym_apply<T>(a.sym, scol, p, x)); };
     LN::template run<true, false>(t, tw, ld, sst, xw, xr);
     __syncthreads();
-    const V* acc = a.acc ? static_cast<const V*>(a.acc) + slab * a.out_slab + cc : nullptr;
+    // the accumulate input has the output's layout (main columns only)
+    const V* acc = a.acc ? static_cast<const V*>(a.acc) + (out - static_cast<V*>(a.out)) : nullptr;
     auto sld = [&](int p) { return sm[p * TC + c]; };
     auto gst = [&](int p, V x) {
       x.y = -x.y;
@@ -298,7 +315,11 @@ k_zr2c(const ContigArgs a) {
   }
   if (t == 0) {
     V z0 = xr(0);
-    if (valid) out[M] = c_make<V>(z0.x - z0.y, T(0));
+    V xn = c_make<V>(z0.x - z0.y, T(0));
+    if (valid) {
+      if (a.nyq_out) static_cast<V*>(a.nyq_out)[ls] = xn;
+      else out[M] = xn;
+    }
   }
 }
 
@@ -314,7 +335,7 @@ k_zc2r(const ContigArgs a) {
     V v[LN::E];
 #pragma unroll
     for (int r = 0; r < LN::E; ++r) v[r] = in[t + r * P];
-    V nyq = in[t == 0 ? M : 0];
+    V nyq = a.nyq_in ? static_cast<const V*>(a.nyq_in)[ls] : in[t == 0 ? M : 0];
 #pragma unroll
     for (int r = 0; r < LN::E; ++r) xw(t + r * P, v[r]);
     if (t == 0) xw(M, nyq);

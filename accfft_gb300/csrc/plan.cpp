@@ -12,6 +12,7 @@
 #include <initializer_list>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <string>
 #include <vector>
 
@@ -125,6 +126,15 @@ struct accfft_c_plan {
   cudaStream_t stream = 0;
   bool blocking = true;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  // 3-D operators keep their spectrum in the aligned split layout in scratch:
+  // main [N0][N1][M] (rows of M = N2/2 complex, 128-byte aligned) and the
+  // Nyquist plane [N0][N1] (kz = N2/2) after it
+  bool split = false;
+  // per-kernel CUDA-event profiling (accfft_c_set_profiling)
+  bool profile = false;
+  std::vector<cudaEvent_t> pev;
+  std::vector<std::pair<std::string, int>> pending;   // label, event pair index
+  std::map<std::string, std::pair<long long, double>> pstats;
 
   long long esz() const { return dbl ? 8 : 4; }
   int M() const { return n[2] / 2; }
@@ -259,6 +269,10 @@ accfft_c_plan* make_plan(int kind, bool dbl, const int* n, void* data, void* dat
       accfft_c_destroy_plan(p);
       return nullptr;
     }
+    // operators keep their spectrum in the split layout when its rows of M
+    // complex are 128-byte aligned (M a multiple of 16 for float, 8 for double)
+    const int M = n[2] / 2;
+    p->split = M >= 8 && M % (dbl ? 8 : 16) == 0;
     // ACCFFT_GB300_ZY = fused | batch<n> selects an alternative z+y schedule
     // for device-resident data (both measured slower on GB300 than the
     // default whole-grid passes; kept for comparison)
@@ -291,6 +305,38 @@ struct Exec {
     if (p->blocking || timer) cudaEventRecord(p->ev0, p->stream);
   }
   bool ok() const { return rc == ACCFFT_C_OK; }
+  // run one launcher; with profiling on, bracket it with CUDA events on its stream
+  template <class F>
+  bool timed(const char* label, cudaStream_t st, F&& launch) {
+    if (!p->profile) return launch();
+    size_t k = p->pending.size();
+    if (k >= 512) {   // fold before the event pool grows further
+      fold_profile(p);
+      k = 0;
+    }
+    while (p->pev.size() < 2 * (k + 1)) {
+      cudaEvent_t e;
+      if (cudaEventCreate(&e) != cudaSuccess) return launch();
+      p->pev.push_back(e);
+    }
+    cudaEventRecord(p->pev[2 * k], st);
+    bool r = launch();
+    cudaEventRecord(p->pev[2 * k + 1], st);
+    p->pending.emplace_back(label, (int)k);
+    return r;
+  }
+  static void fold_profile(accfft_c_plan* q) {
+    for (auto& rec : q->pending) {
+      float ms = 0;
+      cudaEventSynchronize(q->pev[2 * rec.second + 1]);
+      if (cudaEventElapsedTime(&ms, q->pev[2 * rec.second], q->pev[2 * rec.second + 1]) == cudaSuccess) {
+        auto& st = q->pstats[rec.first];
+        st.first += 1;
+        st.second += ms;
+      }
+    }
+    q->pending.clear();
+  }
   void unsupported(const char* what, int L) {
     if (ok()) rc = fail(ACCFFT_C_EUNSUPPORTED, "%s: no kernel for length %d", what, L);
   }
@@ -306,7 +352,9 @@ struct Exec {
     a.in_slab = a.out_slab = slab;
     a.in_line = a.out_line = line;
     a.inverse = inverse;
-    if (!launch_strided(p->dbl, L, 0, a, p->stream)) unsupported("strided pass", L);
+    if (!timed(tw == p->tw_x ? (inverse ? "x_inv" : "x") : (inverse ? "y_inv" : "y"), p->stream,
+               [&] { return launch_strided(p->dbl, L, 0, a, p->stream); }))
+      unsupported("strided pass", L);
   }
   void strided_sym(const void* in, void* out, const void* acc, const void* tw, int L, long long ncols, long long cps,
                    long long slab, long long line, const SymArgs& sym) {
@@ -321,7 +369,8 @@ struct Exec {
     a.in_slab = a.out_slab = slab;
     a.in_line = a.out_line = line;
     a.sym = sym;
-    if (!launch_strided(p->dbl, L, 1, a, p->stream)) unsupported("symbol pass", L);
+    if (!timed("sym", p->stream, [&] { return launch_strided(p->dbl, L, 1, a, p->stream); }))
+      unsupported("symbol pass", L);
   }
   // y pass over an [N0][N1][h] complex array, x pass over [N0][N1*h]
   void ypass(const void* in, void* out, long long h, int inverse) {
@@ -342,7 +391,8 @@ struct Exec {
     a.nlines = (long long)p->n[0] * p->n[1];
     a.in_dist = in_row;
     a.out_dist = p->H2();
-    if (!launch_zr2c(p->dbl, p->M(), a, p->stream)) unsupported("z r2c pass", p->M());
+    if (!timed("z_r2c", p->stream, [&] { return launch_zr2c(p->dbl, p->M(), a, p->stream); }))
+      unsupported("z r2c pass", p->M());
   }
   void zc2r(const void* in, void* out, long long out_row) {
     if (!ok()) return;
@@ -355,7 +405,8 @@ struct Exec {
     a.nlines = (long long)p->n[0] * p->n[1];
     a.in_dist = p->H2();
     a.out_dist = out_row;
-    if (!launch_zc2r(p->dbl, p->M(), a, p->stream)) unsupported("z c2r pass", p->M());
+    if (!timed("z_c2r", p->stream, [&] { return launch_zc2r(p->dbl, p->M(), a, p->stream); }))
+      unsupported("z c2r pass", p->M());
   }
   // z passes and y pass restricted to slabs [s0, s0 + ns) on stream st
   void zr2c_slabs(const void* in, void* out, long long in_row, long long s0, long long ns, cudaStream_t st) {
@@ -370,7 +421,7 @@ struct Exec {
     a.nlines = ns * N1;
     a.in_dist = in_row;
     a.out_dist = p->H2();
-    if (!launch_zr2c(p->dbl, p->M(), a, st)) unsupported("z r2c pass", p->M());
+    if (!timed("z_r2c", st, [&] { return launch_zr2c(p->dbl, p->M(), a, st); })) unsupported("z r2c pass", p->M());
   }
   void zc2r_slabs(const void* in, void* out, long long out_row, long long s0, long long ns, cudaStream_t st) {
     if (!ok()) return;
@@ -384,7 +435,7 @@ struct Exec {
     a.nlines = ns * N1;
     a.in_dist = p->H2();
     a.out_dist = out_row;
-    if (!launch_zc2r(p->dbl, p->M(), a, st)) unsupported("z c2r pass", p->M());
+    if (!timed("z_c2r", st, [&] { return launch_zc2r(p->dbl, p->M(), a, st); })) unsupported("z c2r pass", p->M());
   }
   void ypass_slabs(const void* in, void* out, int inverse, long long s0, long long ns, cudaStream_t st) {
     if (!ok()) return;
@@ -399,7 +450,8 @@ struct Exec {
     a.in_slab = a.out_slab = N1 * h;
     a.in_line = a.out_line = h;
     a.inverse = inverse;
-    if (!launch_strided(p->dbl, p->n[1], 0, a, st)) unsupported("strided pass", p->n[1]);
+    if (!timed(inverse ? "y_inv" : "y", st, [&] { return launch_strided(p->dbl, p->n[1], 0, a, st); }))
+      unsupported("strided pass", p->n[1]);
   }
   // z r2c then y forward (forward = true), or y backward then z c2r, over
   // the whole grid.  When the real array is in (pinned) host memory the z
@@ -447,7 +499,8 @@ struct Exec {
     a.nlines = (long long)p->n[0] * p->n[1];
     a.in_dist = a.out_dist = p->n[2];
     a.inverse = inverse;
-    if (!launch_zc2c(p->dbl, p->n[2], a, p->stream)) unsupported("z c2c pass", p->n[2]);
+    if (!timed("z_c2c", p->stream, [&] { return launch_zc2c(p->dbl, p->n[2], a, p->stream); }))
+      unsupported("z c2c pass", p->n[2]);
   }
   void zsym(const void* in, void* out, const void* acc, long long row, const SymArgs& sym) {
     if (!ok()) return;
@@ -460,7 +513,8 @@ struct Exec {
     a.nlines = (long long)p->n[0] * p->n[1];
     a.in_dist = a.out_dist = row;
     a.sym = sym;
-    if (!launch_zsym(p->dbl, p->M(), a, p->stream)) unsupported("z symbol pass", p->M());
+    if (!timed("z_sym", p->stream, [&] { return launch_zsym(p->dbl, p->M(), a, p->stream); }))
+      unsupported("z symbol pass", p->M());
   }
   void slab(bool forward, const void* in, void* out) {
     if (!ok()) return;
@@ -472,7 +526,9 @@ struct Exec {
     a.tw_post = p->tw_post;
     a.n0 = p->n[0];
     a.real_row = p->rrow();
-    if (!launch_slab(p->dbl, p->n[1], p->n[2], forward, a, p->stream)) rc = fail(ACCFFT_C_ECUDA, "slab pass launch failed");
+    if (!timed(forward ? "zy_slab" : "yz_slab", p->stream,
+               [&] { return launch_slab(p->dbl, p->n[1], p->n[2], forward, a, p->stream); }))
+      rc = fail(ACCFFT_C_ECUDA, "slab pass launch failed");
   }
   // single-axis real transform along x (axis 0) or y (axis 1) of an
   // unpadded [N0][N1][N2] real array (the reference's x-only / y-only
@@ -510,7 +566,84 @@ struct Exec {
     } else {
       a.in_slab = spec_slab; a.in_line = spec_line; a.out_slab = real_slab; a.out_line = real_line;
     }
-    if (!launch_strided(p->dbl, L, mode, a, p->stream)) unsupported("single-axis pass", L);
+    if (!timed(axis == 0 ? "x_real" : "y_real", p->stream, [&] { return launch_strided(p->dbl, L, mode, a, p->stream); }))
+      unsupported("single-axis pass", L);
+  }
+  // ---- passes through the aligned intermediate layout (p->split)
+  void* main_buf() const { return p->scratch; }
+  void* nyq_buf() const {
+    return static_cast<char*>(p->scratch) + (long long)p->n[0] * p->n[1] * p->M() * 2 * p->esz();
+  }
+  void zr2c_split(const void* in, long long in_row) {
+    if (!ok()) return;
+    ContigArgs a{};
+    a.in = in;
+    a.out = main_buf();
+    a.nyq_out = nyq_buf();
+    a.weight = weight;
+    a.tw = p->tw_z;
+    a.tw_post = p->tw_post;
+    a.nlines = (long long)p->n[0] * p->n[1];
+    a.in_dist = in_row;
+    a.out_dist = p->M();
+    if (!timed("z_r2c", p->stream, [&] { return launch_zr2c(p->dbl, p->M(), a, p->stream); }))
+      unsupported("z r2c pass", p->M());
+  }
+  void zc2r_split(void* out, long long out_row) {
+    if (!ok()) return;
+    ContigArgs a{};
+    a.in = main_buf();
+    a.nyq_in = nyq_buf();
+    a.out = out;
+    a.weight = weight;
+    a.tw = p->tw_z;
+    a.tw_post = p->tw_post;
+    a.nlines = (long long)p->n[0] * p->n[1];
+    a.in_dist = p->M();
+    a.out_dist = out_row;
+    if (!timed("z_c2r", p->stream, [&] { return launch_zc2r(p->dbl, p->M(), a, p->stream); }))
+      unsupported("z c2r pass", p->M());
+  }
+  // y lines of the main part (aligned columns) and, as extra columns of the
+  // same launch, the contiguous y lines of the Nyquist plane
+  void y_split(int inverse) {
+    if (!ok()) return;
+    const long long N0 = p->n[0], N1 = p->n[1], M = p->M();
+    StridedArgs a{};
+    a.in = a.out = main_buf();
+    a.tw = p->tw_y;
+    a.ncols_main = N0 * M;
+    a.ncols = N0 * M + N0;
+    a.cps = M;
+    a.in_slab = a.out_slab = N1 * M;
+    a.in_line = a.out_line = M;
+    a.in_nyq = a.out_nyq = nyq_buf();
+    a.nyq_slab = N1;
+    a.nyq_line = 1;
+    a.inverse = inverse;
+    if (!timed(inverse ? "y_inv" : "y", p->stream, [&] { return launch_strided(p->dbl, (int)N1, 0, a, p->stream); }))
+      unsupported("strided pass", (int)N1);
+  }
+  // fused x pass of a 3-D operator on the split layout (in place, aligned;
+  // the Nyquist plane's x lines are the launch's last N1 columns)
+  void x_split_sym(SymArgs sym) {
+    if (!ok()) return;
+    const long long N1 = p->n[1], M = p->M();
+    StridedArgs a{};
+    a.in = a.out = main_buf();
+    a.tw = p->tw_x;
+    a.ncols_main = N1 * M;
+    a.ncols = N1 * M + N1;
+    a.cps = a.ncols_main;
+    a.in_slab = a.out_slab = 0;
+    a.in_line = a.out_line = N1 * M;
+    a.in_nyq = a.out_nyq = nyq_buf();
+    a.nyq_slab = 1;
+    a.nyq_line = N1;
+    sym.h2 = (int)M;
+    a.sym = sym;
+    if (!timed("x_sym", p->stream, [&] { return launch_strided(p->dbl, p->n[0], 1, a, p->stream); }))
+      unsupported("symbol pass", p->n[0]);
   }
   int finish() {
     cudaError_t e = cudaGetLastError();
@@ -663,12 +796,20 @@ int op3d(accfft_c_plan* p, int sym_kind, void* outr, const void* inr, double* ti
   const long long h = p->H2();
   const double N = (double)p->n[0] * p->n[1] * p->n[2];
   Exec ex(p, timer);
+  SymArgs sym = make_sym(p, sym_kind, 1.0 / N);
+  sym.param = param;
+  if (p->split) {
+    ex.zr2c_split(inr, p->rrow());
+    ex.y_split(0);
+    ex.x_split_sym(sym);
+    ex.y_split(1);
+    ex.zc2r_split(outr, p->rrow());
+    return ex.finish();
+  }
   void* s = p->scratch;
   ex.zr2c(inr, s, p->rrow());
   ex.ypass(s, s, h, 0);
   long long c = (long long)p->n[1] * h;
-  SymArgs sym = make_sym(p, sym_kind, 1.0 / N);
-  sym.param = param;
   ex.strided_sym(s, s, nullptr, p->tw_x, p->n[0], c, c, 0, c, sym);
   ex.ypass(s, s, h, 1);
   ex.zc2r(s, outr, p->rrow());
@@ -746,6 +887,7 @@ void accfft_c_destroy_plan(accfft_c_plan* p) {
   if (p->ev1) cudaEventDestroy(p->ev1);
   for (cudaEvent_t e : p->evb)
     if (e) cudaEventDestroy(e);
+  for (cudaEvent_t e : p->pev) cudaEventDestroy(e);
   if (p->stream2) cudaStreamDestroy(p->stream2);
   delete p;
 }
@@ -760,6 +902,30 @@ int accfft_c_plan_info(const accfft_c_plan* p, int n[3], int* kind, int* is_doub
   if (inplace) *inplace = p->inplace;
   if (alloc_max) *alloc_max = p->alloc_max;
   return ACCFFT_C_OK;
+}
+
+int accfft_c_set_profiling(accfft_c_plan* p, int on) {
+  if (!p) return fail(ACCFFT_C_EINVAL, "set_profiling: NULL plan");
+  p->profile = on != 0;
+  return ACCFFT_C_OK;
+}
+
+int accfft_c_profile_read(accfft_c_plan* p, int max_entries, char* labels, long long* counts, double* total_ms) {
+  if (!p) return fail(ACCFFT_C_EINVAL, "profile_read: NULL plan");
+  Exec::fold_profile(p);
+  int n = 0;
+  for (auto& kv : p->pstats) {
+    if (n >= max_entries) break;
+    if (labels) {
+      memset(labels + 32 * n, 0, 32);
+      strncpy(labels + 32 * n, kv.first.c_str(), 31);
+    }
+    if (counts) counts[n] = kv.second.first;
+    if (total_ms) total_ms[n] = kv.second.second;
+    ++n;
+  }
+  p->pstats.clear();
+  return n;
 }
 
 int accfft_c_set_zy_schedule(accfft_c_plan* p, int mode) {

@@ -2,10 +2,11 @@
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--n 512]
 
-A step is one r2c + c2r pair of the 512^3 float32 field through the C ABI:
-forward z, y, x passes then inverse x, y, z passes, each pass issued by the
-public execute call with its xyz bit (AccFFT's std::bitset<3> argument), so
-every kernel is bracketed by CUDA events on the plan's stream.  Inputs
+A step is one r2c + c2r pair of the 512^3 float32 field through the C ABI
+(accfft_c_execute_r2c_gpuf then accfft_c_execute_c2r_gpuf, device arrays):
+z r2c, y, x passes then x, y, z c2r passes.  The plan's per-kernel profiling
+(accfft_c_set_profiling) brackets every pass with CUDA events on the plan's
+stream, which gives each kernel's mean launch time for the roofline.  Inputs
 (537 MB) exceed the 129 MB L2, so no flush is needed between steps.
 
 value   pairs/s with the field resident in HBM (max time over ranks)
@@ -66,27 +67,25 @@ def dist_env():
 
 
 def algorithmic_bytes(n, esz):
-    """Per-launch bytes of each pass: every pass reads its input and writes its
-    output once (the fused z+y slab passes read the real field and write the
-    spectrum, or the reverse)."""
-    N = n[0] * n[1] * n[2]
-    H = n[0] * n[1] * (n[2] // 2 + 1)
+    """Bytes each kernel launch must move (its input read once, its output
+    written once), per profiling label of the plan (accfft_c_profile_read)."""
+    N0, N1, N2 = n
+    N = N0 * N1 * N2
+    M = N2 // 2
+    H = N0 * N1 * (M + 1)
     c = 2 * esz
     return {
-        "z_r2c": N * esz + H * c,
-        "y_fwd": 2 * H * c,
-        "x_fwd": 2 * H * c,
-        "x_inv": 2 * H * c,
-        "y_inv": 2 * H * c,
+        "z_r2c": N * esz + H * c,           # real field in, half spectrum out
         "z_c2r": H * c + N * esz,
-        "zy_fwd": N * esz + H * c,
-        "zy_inv": H * c + N * esz,
+        "y": 2 * H * c, "y_inv": 2 * H * c,  # natural layout (whole spectrum)
+        "x": 2 * H * c, "x_inv": 2 * H * c,
+        "zy_slab": N * esz + H * c, "yz_slab": H * c + N * esz,
     }
 
 
-KERNEL_OF = {"z_r2c": "k_zr2c", "y_fwd": "k_strided (y)", "x_fwd": "k_strided (x)",
-             "x_inv": "k_strided (x)", "y_inv": "k_strided (y)", "z_c2r": "k_zc2r",
-             "zy_fwd": "k_slab_fwd (z+y, cluster)", "zy_inv": "k_slab_inv (y+z, cluster)"}
+KERNEL_OF = {"z_r2c": "k_zr2c", "y": "k_strided (y)", "x": "k_strided (x)", "x_inv": "k_strided (x)",
+             "y_inv": "k_strided (y)", "z_c2r": "k_zc2r",
+             "zy_slab": "k_slab_fwd (z+y, cluster)", "yz_slab": "k_slab_inv (y+z, cluster)"}
 
 
 class Clocks:
@@ -263,29 +262,9 @@ def ours(args):
     u = torch.randn(n, dtype=tdt, device="cuda", generator=g)
     spec = torch.empty((N0, N1, H2, 2), dtype=tdt, device="cuda")
     back = torch.empty(n, dtype=tdt, device="cuda")
-    # one public call per kernel: the z+y passes are a single cluster kernel
-    # when the grid has one (detected by counting launches of an xyz = z|y call)
-    l0 = ag.kernel_launches()
-    plan.r2c(u, spec, xyz=6)
-    stream.synchronize()
-    fused = ag.kernel_launches() - l0 == 1
-    if fused:
-        passes = ["zy_fwd", "x_fwd", "x_inv", "zy_inv"]
-        calls = [lambda: plan.r2c(u, spec, xyz=6), lambda: plan.r2c(spec, spec, xyz=1),
-                 lambda: plan.c2r(spec, spec, xyz=1), lambda: plan.c2r(spec, back, xyz=6)]
-    else:
-        passes = ["z_r2c", "y_fwd", "x_fwd", "x_inv", "y_inv", "z_c2r"]
-        calls = [lambda: plan.r2c(u, spec, xyz=4), lambda: plan.r2c(spec, spec, xyz=2),
-                 lambda: plan.r2c(spec, spec, xyz=1), lambda: plan.c2r(spec, spec, xyz=1),
-                 lambda: plan.c2r(spec, spec, xyz=2), lambda: plan.c2r(spec, back, xyz=4)]
-
-    def step(evs=None):
-        for i, c in enumerate(calls):
-            if evs is not None:
-                evs[i][0].record(stream)
-            c()
-            if evs is not None:
-                evs[i][1].record(stream)
+    def step():
+        plan.r2c(u, spec)
+        plan.c2r(spec, back)
 
     with torch.cuda.stream(stream):
         for _ in range(args.warmup):
@@ -295,7 +274,10 @@ def ours(args):
     err = (back / (N0 * N1 * N2) - u).norm().item() / u.norm().item()
     assert err < (1e-5 if dt == "float32" else 1e-12), err
 
-    evs = [[[torch.cuda.Event(enable_timing=True) for _ in range(2)] for _ in passes] for _ in range(args.steps)]
+    # the timed region: full r2c + c2r calls; the plan brackets each of its
+    # kernels with CUDA events on the plan's stream
+    plan.set_profiling(True)
+    plan.profile()
     launches0 = ag.kernel_launches()
     clk = Clocks(torch.cuda.current_device()) if rank == 0 else None
     if world > 1:
@@ -304,14 +286,17 @@ def ours(args):
     t0 = torch.cuda.Event(enable_timing=True)
     t1 = torch.cuda.Event(enable_timing=True)
     t0.record(stream)
-    for k in range(args.steps):
-        step(evs[k])
+    with torch.cuda.stream(stream):
+        for k in range(args.steps):
+            step()
     t1.record(stream)
     torch.cuda.synchronize()
     if world > 1:
         torch.distributed.barrier()
     clocks = clk.stop() if clk else None
     launches = ag.kernel_launches() - launches0
+    prof = plan.profile()
+    plan.set_profiling(False)
     total_ms = t0.elapsed_time(t1)
     if world > 1:
         tt = torch.tensor([total_ms], device="cuda")
@@ -320,13 +305,14 @@ def ours(args):
     ms_step = total_ms / args.steps
     value = world * args.steps / (total_ms / 1000.0)
 
-    per = {p: statistics.mean(evs[k][i][0].elapsed_time(evs[k][i][1]) for k in range(args.steps))
-           for i, p in enumerate(passes)}
     nbytes = algorithmic_bytes(n, esz)
-    dom = max(per, key=per.get)
+    per = {lab: tot / cnt for lab, (cnt, tot) in prof.items()}                 # ms per launch
+    share = {lab: tot / args.steps for lab, (cnt, tot) in prof.items()}        # ms per step
+    dom = max(share, key=share.get)
     peak, peak_kind = measured_peak()
-    achieved = nbytes[dom] / (per[dom] / 1000.0) / 1e9
-    step_bytes = sum(nbytes[p] for p in passes)
+    dom_bytes = nbytes[dom]
+    achieved = dom_bytes / (per[dom] / 1000.0) / 1e9
+    step_bytes = sum(nbytes[lab] * cnt / args.steps for lab, (cnt, tot) in prof.items())
     e2e = None if args.no_e2e else e2e_pairs_per_s(args, ag, torch, n, dt, u, stream, world)
 
     if rank != 0:
@@ -339,12 +325,13 @@ def ours(args):
         "config": {"workload": f"{label} {dt} r2c+c2r round trip", "grid": list(n),
                    "flush": "inputs_larger_than_l2", "parallelism": f"replicas{world}"},
         "gpu_launches": int(launches),
-        "roofline": {"bound": "hbm", "kernel": KERNEL_OF[dom], "pass": dom, "achieved": achieved, "peak": peak,
-                     "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": None, "bytes_per_launch": nbytes[dom], "ms_per_launch": per[dom]},
-        "passes_ms": per,
-        "fused_zy": fused,
-        "passes_frac_of_peak": {p: nbytes[p] / (per[p] / 1000.0) / 1e9 / peak for p in passes},
+        "roofline": {"bound": "hbm", "kernel": KERNEL_OF.get(dom, dom), "pass": dom, "achieved": achieved,
+                     "peak": peak, "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": None, "bytes_per_launch": dom_bytes, "ms_per_launch": per[dom]},
+        "kernel_ms_per_launch": per,
+        "kernel_ms_per_step": share,
+        "kernel_frac_of_peak": {lab: nbytes[lab] / (per[lab] / 1000.0) / 1e9 / peak
+                                for lab in per},
         "step_algorithmic_GBps": step_bytes / (ms_step / 1000.0) / 1e9,
         "gflops_5nlogn": 5 * N0 * N1 * N2 * np.log2(N0 * N1 * N2) / (ms_step / 1000.0) / 1e9,
         "e2e": e2e,

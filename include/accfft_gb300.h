@@ -84,6 +84,14 @@ int accfft_c_plan_info(const accfft_c_plan* plan, int n[3], int* kind, int* is_d
  * pass over the whole grid (default), 1 = one thread-block-cluster kernel per
  * x-slab doing both (ACCFFT_C_EUNSUPPORTED when the grid has none) */
 int accfft_c_set_zy_schedule(accfft_c_plan* plan, int mode);
+/* extension: per-kernel device times.  With profiling on, every kernel the
+ * plan launches is bracketed by CUDA events on its stream;
+ * accfft_c_profile_read waits for them and returns, per pass label ("z_r2c",
+ * "y", "y_nyq", "x", "x_nyq", "z_c2r", "x_sym", ...), the launch count and
+ * total milliseconds since the previous read (labels: 32 bytes each).  The
+ * return value is the number of labels written. */
+int accfft_c_set_profiling(accfft_c_plan* plan, int on);
+int accfft_c_profile_read(accfft_c_plan* plan, int max_entries, char* labels, long long* counts, double* total_ms);
 /* extension: enqueue on `stream` (a cudaStream_t); blocking = 0 returns
  * without waiting (timer slots are then not updated) */
 int accfft_c_set_stream(accfft_c_plan* plan, void* stream, int blocking);

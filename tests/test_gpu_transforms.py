@@ -143,6 +143,18 @@ def test_kernel_launch_counter(cuda, native):
     before = native.kernel_launches()
     plan.r2c(du, dh)
     assert native.kernel_launches() - before == 3      # z, y and x passes
+    # a 3-D operator: z r2c, y, fused x (forward, symbol, inverse), y, z c2r;
+    # at N2/2 = 16 through the aligned split layout, whose Nyquist plane
+    # rides along in the y and x launches
+    out = torch.empty_like(du)
+    before = native.kernel_launches()
+    plan.laplace(out, du)
+    assert native.kernel_launches() - before == 5
+    plan2 = native.PlanR2C((32, 32, 40), "float32")      # N2/2 = 20: natural layout
+    du2 = torch.randn((32, 32, 40), device="cuda")
+    before = native.kernel_launches()
+    plan2.laplace(torch.empty_like(du2), du2)
+    assert native.kernel_launches() - before == 5
 
 
 AXIS_SHAPES = [(8, 6, 4), (16, 12, 10), (5, 9, 4), (48, 96, 64), (128, 128, 128), (160, 180, 200), (9, 5, 6)]
@@ -242,3 +254,28 @@ def test_unregistered_host_memory_is_refused(cuda, native):
     with pytest.raises(native.AccfftError) as e:
         plan.r2c(host.ctypes.data, spec)
     assert e.value.code == native.EINVAL and "pinned host memory" in str(e.value)
+
+
+def test_kernel_profiling_labels(cuda, native):
+    """accfft_c_set_profiling / accfft_c_profile_read: per-pass event times of
+    a full r2c + c2r and of a 3-D operator."""
+    torch = cuda
+    n = (64, 64, 64)
+    plan = native.PlanR2C(n, "float32")
+    u = torch.randn(n, device="cuda")
+    spec = torch.empty((64, 64, 33, 2), device="cuda")
+    back = torch.empty(n, device="cuda")
+    plan.set_profiling(True)
+    for _ in range(3):
+        plan.r2c(u, spec)
+        plan.c2r(spec, back)
+    prof = plan.profile()
+    assert set(prof) == {"z_r2c", "y", "x", "x_inv", "y_inv", "z_c2r"}
+    assert all(cnt == 3 and ms > 0 for cnt, ms in prof.values())
+    assert plan.profile() == {}
+    assert torch.allclose(back / 64 ** 3, u, atol=1e-5)
+    plan.laplace(back, u)
+    prof = plan.profile()
+    assert set(prof) == {"z_r2c", "y", "x_sym", "y_inv", "z_c2r"}
+    plan.set_profiling(False)
+    assert plan.profile() == {}
