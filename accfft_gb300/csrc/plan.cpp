@@ -12,6 +12,7 @@
 #include <initializer_list>
 #include <cstdio>
 #include <cstring>
+#include <algorithm>
 #include <map>
 #include <string>
 #include <vector>
@@ -122,6 +123,11 @@ struct accfft_c_plan {
   int zy_batches = 1;
   cudaStream_t stream2 = nullptr;
   static constexpr int kMaxBatches = 64;
+  // pinned-host real arrays: slab batches staged through a device ring
+  static constexpr int kHostBatches = 16, kHostSlots = 3;
+  void* hstage = nullptr;
+  long long hstage_bytes = 0;
+  static_assert(1 + kHostBatches + kHostSlots <= kMaxBatches + 1, "host path events fit evb");
   cudaEvent_t evb[kMaxBatches + 2] = {};
   cudaStream_t stream = 0;
   bool blocking = true;
@@ -409,12 +415,13 @@ struct Exec {
       unsupported("z c2r pass", p->M());
   }
   // z passes and y pass restricted to slabs [s0, s0 + ns) on stream st
+  // (the real side `in` / `out` points at the batch's first row)
   void zr2c_slabs(const void* in, void* out, long long in_row, long long s0, long long ns, cudaStream_t st) {
     if (!ok()) return;
     const long long N1 = p->n[1];
     ContigArgs a{};
     a.weight = weight;
-    a.in = static_cast<const char*>(in) + s0 * N1 * in_row * p->esz();
+    a.in = in;
     a.out = static_cast<char*>(out) + s0 * N1 * p->H2() * 2 * p->esz();
     a.tw = p->tw_z;
     a.tw_post = p->tw_post;
@@ -429,7 +436,7 @@ struct Exec {
     ContigArgs a{};
     a.weight = weight;
     a.in = static_cast<const char*>(in) + s0 * N1 * p->H2() * 2 * p->esz();
-    a.out = static_cast<char*>(out) + s0 * N1 * out_row * p->esz();
+    a.out = out;
     a.tw = p->tw_z;
     a.tw_post = p->tw_post;
     a.nlines = ns * N1;
@@ -454,18 +461,17 @@ struct Exec {
       unsupported("strided pass", p->n[1]);
   }
   // z r2c then y forward (forward = true), or y backward then z c2r, over
-  // the whole grid.  When the real array is in (pinned) host memory the z
-  // kernels read or write it directly over the host link, slab batch by slab
-  // batch on the plan's stream, while the y pass of the previous batch runs
-  // on a second stream.
-  void zy(bool forward, const void* in, void* mid, void* out, long long row, bool host_real) {
+  // the whole grid of device arrays (mid: the spectrum the inverse y pass
+  // writes).  Alternative schedules: the cluster slab kernel (zy_mode 1) or
+  // slab batches with z and y on two streams (zy_mode 2).
+  void zy(bool forward, const void* in, void* mid, void* out, long long row) {
     if (!ok()) return;
-    if (p->zy_mode == 1 && !host_real && weight == 0) {
+    if (p->zy_mode == 1 && weight == 0) {
       slab(forward, in, out);
       return;
     }
     const long long N0 = p->n[0];
-    int nb = host_real ? 8 : (p->zy_mode == 2 ? p->zy_batches : 1);
+    int nb = p->zy_mode == 2 ? p->zy_batches : 1;
     if (nb > N0) nb = (int)N0;
     cudaStream_t A = p->stream, B = nb > 1 ? p->stream2 : p->stream;
     if (B != A) {
@@ -474,21 +480,102 @@ struct Exec {
     }
     for (int b = 0; b < nb; ++b) {
       const long long s0 = N0 * b / nb, s1 = N0 * (b + 1) / nb;
-      // forward: z (reads the real array) on A, y on B; inverse: y on A,
-      // z (writes the real array) on B
-      if (forward) zr2c_slabs(in, out, row, s0, s1 - s0, A);
+      // forward: z on A, y on B; inverse: y on A, z on B
+      if (forward) zr2c_slabs(real_at(in, s0, row), out, row, s0, s1 - s0, A);
       else ypass_slabs(in, mid, 1, s0, s1 - s0, A);
       if (B != A) {
         cudaEventRecord(p->evb[1 + b], A);
         cudaStreamWaitEvent(B, p->evb[1 + b], 0);
       }
       if (forward) ypass_slabs(out, out, 0, s0, s1 - s0, B);
-      else zc2r_slabs(mid, out, row, s0, s1 - s0, B);
+      else zc2r_slabs(mid, real_at(out, s0, row), row, s0, s1 - s0, B);
     }
     if (B != A) {
       cudaEventRecord(p->evb[nb + 1], B);
       cudaStreamWaitEvent(A, p->evb[nb + 1], 0);
     }
+  }
+  static const void* real_at(const void* base, long long s0, long long row, long long N1, long long esz) {
+    return static_cast<const char*>(base) + s0 * N1 * row * esz;
+  }
+  const void* real_at(const void* base, long long s0, long long row) const {
+    return real_at(base, s0, row, p->n[1], p->esz());
+  }
+  void* real_at(void* base, long long s0, long long row) const {
+    return const_cast<void*>(real_at(static_cast<const void*>(base), s0, row, p->n[1], p->esz()));
+  }
+  // The same z+y work when the real array lives in pinned host memory: the
+  // copy engine moves slab batches between the host array and a ring of
+  // kHostSlots device staging slots on the plan's second stream, while the
+  // plan's stream runs the z and y kernels of the batches already staged.
+  // Host-to-device and device-to-host copies use separate engines, so an
+  // r2c on one plan overlaps a c2r on another.
+  void zy_host(bool forward, const void* in, void* mid, void* out, long long row) {
+    if (!ok()) return;
+    const long long N0 = p->n[0], N1 = p->n[1];
+    const int nb = (int)std::min<long long>(N0, accfft_c_plan::kHostBatches);
+    const long long slab_rows = (N0 + nb - 1) / nb;                 // largest batch, in slabs
+    const long long slot_bytes = slab_rows * N1 * row * p->esz();
+    if (!ensure_stage(slot_bytes)) return;
+    auto slot = [&](int b) { return static_cast<char*>(p->hstage) + (b % accfft_c_plan::kHostSlots) * slot_bytes; };
+    cudaStream_t A = p->stream, C = p->stream2;
+    cudaEvent_t* ev_start = &p->evb[0];
+    cudaEvent_t* ev_copy = &p->evb[1];                               // nb events: batch b moved
+    cudaEvent_t* ev_free = &p->evb[1 + accfft_c_plan::kHostBatches]; // kHostSlots: slot reusable
+    cudaEventRecord(*ev_start, A);
+    cudaStreamWaitEvent(C, *ev_start, 0);
+    for (int b = 0; b < nb && ok(); ++b) {
+      const long long s0 = N0 * b / nb, s1 = N0 * (b + 1) / nb, ns = s1 - s0;
+      const size_t bytes = (size_t)(ns * N1 * row * p->esz());
+      const int k = b % accfft_c_plan::kHostSlots;
+      if (forward) {
+        if (b >= accfft_c_plan::kHostSlots) cudaStreamWaitEvent(C, ev_free[k], 0);
+        copy("h2d", C, slot(b), real_at(in, s0, row), bytes);
+        cudaEventRecord(ev_copy[b], C);
+        cudaStreamWaitEvent(A, ev_copy[b], 0);
+        zr2c_slabs(slot(b), out, row, s0, ns, A);
+        cudaEventRecord(ev_free[k], A);
+        ypass_slabs(out, out, 0, s0, ns, A);
+      } else {
+        ypass_slabs(in, mid, 1, s0, ns, A);
+        if (b >= accfft_c_plan::kHostSlots) cudaStreamWaitEvent(A, ev_free[k], 0);
+        zc2r_slabs(mid, slot(b), row, s0, ns, A);
+        cudaEventRecord(ev_copy[b], A);
+        cudaStreamWaitEvent(C, ev_copy[b], 0);
+        copy("d2h", C, real_at(out, s0, row), slot(b), bytes);
+        cudaEventRecord(ev_free[k], C);
+      }
+    }
+    // the plan's stream ends after the last copy
+    cudaEventRecord(p->evb[accfft_c_plan::kMaxBatches + 1], C);
+    cudaStreamWaitEvent(A, p->evb[accfft_c_plan::kMaxBatches + 1], 0);
+  }
+  bool ensure_stage(long long slot_bytes) {
+    const long long need = slot_bytes * accfft_c_plan::kHostSlots;
+    if (p->hstage_bytes >= need) return true;
+    // the old ring may still be in use by earlier calls on the plan's streams
+    cudaStreamSynchronize(p->stream);
+    cudaStreamSynchronize(p->stream2);
+    if (p->hstage) cudaFree(p->hstage);
+    p->hstage = nullptr;
+    p->hstage_bytes = 0;
+    cudaError_t e = cudaMalloc(&p->hstage, (size_t)need);
+    if (e != cudaSuccess) {
+      p->hstage = nullptr;
+      rc = cuda_fail(e, "execute: staging buffer for host arrays");
+      return false;
+    }
+    p->hstage_bytes = need;
+    return true;
+  }
+  void copy(const char* label, cudaStream_t st, void* dst, const void* src, size_t bytes) {
+    if (!ok()) return;
+    cudaError_t e = cudaSuccess;
+    timed(label, st, [&] {
+      e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDefault, st);
+      return true;
+    });
+    if (e != cudaSuccess) rc = cuda_fail(e, "execute: host copy");
   }
   void zc2c(const void* in, void* out, int inverse) {
     if (!ok()) return;
@@ -717,7 +804,8 @@ int exec_r2c_plan(accfft_c_plan* p, int direction, void* in, void* out, double* 
   if (direction == -1) {
     void* work = in;   // with z skipped the reference transforms the input in place
     if ((xyz & ZB) && (xyz & YB)) {
-      ex.zy(true, in, nullptr, out, p->rrow(), host_in);
+      if (host_in) ex.zy_host(true, in, nullptr, out, p->rrow());
+      else ex.zy(true, in, nullptr, out, p->rrow());
       work = out;
     } else {
       if (xyz & ZB) {
@@ -737,7 +825,8 @@ int exec_r2c_plan(accfft_c_plan* p, int direction, void* in, void* out, double* 
       src = buf;
     }
     if ((xyz & YB) && (xyz & ZB)) {
-      ex.zy(false, src, buf, out, p->rrow(), host_out);
+      if (host_out) ex.zy_host(false, src, buf, out, p->rrow());
+      else ex.zy(false, src, buf, out, p->rrow());
     } else {
       if (xyz & YB) {
         ex.ypass(src, buf, h, 1);
@@ -883,6 +972,7 @@ void accfft_c_destroy_plan(accfft_c_plan* p) {
   if (!p) return;
   if (p->tw_block) cudaFree(p->tw_block);
   if (p->scratch) cudaFree(p->scratch);
+  if (p->hstage) cudaFree(p->hstage);
   if (p->ev0) cudaEventDestroy(p->ev0);
   if (p->ev1) cudaEventDestroy(p->ev1);
   for (cudaEvent_t e : p->evb)

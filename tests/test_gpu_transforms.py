@@ -226,8 +226,8 @@ def test_fused_slab_pass_float(cuda, native, oracle, n, monkeypatch):
 @pytest.mark.parametrize("n", [(64, 48, 80), (128, 128, 128)])
 def test_pinned_host_real_arrays(cuda, native, oracle, n, dtype):
     """r2c reading its real input from pinned host memory and c2r writing its
-    real output to pinned host memory (slab-batch pipeline over the host
-    link) give the device-path results."""
+    real output to pinned host memory (slab batches staged through the
+    plan's device ring by the copy engines) give the device-path results."""
     torch = cuda
     u = rng(90).standard_normal(n)
     plan = native.PlanR2C(n, dtype)
@@ -243,6 +243,37 @@ def test_pinned_host_real_arrays(cuda, native, oracle, n, dtype):
     plan.c2r(s_dev, db)
     assert torch.equal(hb, db.cpu())
     assert oracle.rel_l2(hb.numpy().astype(np.float64) / np.prod(n), u) < TOL[dtype] * 10
+
+
+def test_pinned_host_pipelines_in_flight(cuda, native):
+    """Two plans on two non-blocking streams with pinned host arrays, several
+    pairs in flight: every result equals the device path's; the copies show
+    up in the profile as 16 slab batches each way."""
+    torch = cuda
+    n = (48, 40, 64)
+    hu = [torch.randn(n).pin_memory() for _ in range(4)]
+    hb = [torch.empty(n).pin_memory() for _ in range(4)]
+    streams = [torch.cuda.Stream() for _ in range(2)]
+    plans = [native.PlanR2C(n, "float32") for _ in range(2)]
+    specs = [torch.empty((48, 40, 33, 2), device="cuda") for _ in range(2)]
+    for p, s in zip(plans, streams):
+        p.set_stream(s.cuda_stream, blocking=False)
+    plans[0].set_profiling(True)
+    for k in range(4):
+        p, spec = plans[k % 2], specs[k % 2]
+        p.r2c(hu[k], spec)
+        p.c2r(spec, hb[k])
+    torch.cuda.synchronize()
+    prof = plans[0].profile()
+    assert prof["h2d"][0] == 2 * 16 and prof["d2h"][0] == 2 * 16
+    ref = native.PlanR2C(n, "float32")
+    for k in range(4):
+        du = hu[k].cuda()
+        spec = torch.empty((48, 40, 33, 2), device="cuda")
+        back = torch.empty(n, device="cuda")
+        ref.r2c(du, spec)
+        ref.c2r(spec, back)
+        assert torch.equal(hb[k], back.cpu())
 
 
 def test_unregistered_host_memory_is_refused(cuda, native):
