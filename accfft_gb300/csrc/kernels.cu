@@ -2,7 +2,7 @@
 // compiles this file with -DAFG_PREC=<0|1> -DAFG_KIND=<0..4> -DAFG_GROUP=<0|1>
 // so the template instantiations spread over parallel nvcc processes.
 //   AFG_PREC 0 = float, 1 = double
-//   AFG_KIND 0 = strided (MODE 0 and 1), 1 = zc2c, 2 = zr2c, 3 = zc2r, 4 = zsym
+//   AFG_KIND 0 = strided (MODE 0..4), 1 = zc2c, 2 = zr2c, 3 = zc2r, 4 = zsym (with and without accumulate)
 #include "passes.cuh"
 #include "launch.h"
 
@@ -70,7 +70,8 @@ bool AFG_NAME(int L, int mode, const StridedArgs& a, cudaStream_t s) {
       case 0: run_strided<n, 0>(a, s); break; \
       case 1: run_strided<n, 1>(a, s); break; \
       case 2: run_strided<n, 2>(a, s); break; \
-      default: run_strided<n, 3>(a, s); break; \
+      case 3: run_strided<n, 3>(a, s); break; \
+      default: run_strided<n, 4>(a, s); break; \
     }                                      \
     return true;
     AFG_LIST(AFG_CASE)
@@ -79,7 +80,7 @@ bool AFG_NAME(int L, int mode, const StridedArgs& a, cudaStream_t s) {
   }
 }
 #else
-template <int L>
+template <int L, bool ACC = false>
 static void run_contig(const ContigArgs& a, cudaStream_t s) {
   typedef ContigShape<Real, L> SH;
 #if AFG_KIND == 1
@@ -89,7 +90,7 @@ static void run_contig(const ContigArgs& a, cudaStream_t s) {
 #elif AFG_KIND == 3
   auto k = k_zc2r<Real, L>;
 #else
-  auto k = k_zsym<Real, L>;
+  auto k = k_zsym<Real, L, 0, 0, ACC>;
 #endif
   static bool done = false;
   prepare(k, SH::smem, done);
@@ -99,7 +100,15 @@ static void run_contig(const ContigArgs& a, cudaStream_t s) {
 }
 bool AFG_NAME(int L, const ContigArgs& a, cudaStream_t s) {
   switch (L) {
+#if AFG_KIND == 4
+#define AFG_CASE(n)                                   \
+  case n:                                             \
+    if (a.acc) run_contig<n, true>(a, s);             \
+    else run_contig<n, false>(a, s);                  \
+    return true;
+#else
 #define AFG_CASE(n) case n: run_contig<n>(a, s); return true;
+#endif
     AFG_LIST(AFG_CASE)
 #undef AFG_CASE
     default: return false;

@@ -8,8 +8,8 @@
 //               across slabs (g -> slab g/cps, column g%cps), so ragged column
 //               counts (e.g. N2/2+1) never leave idle tiles.  MODE 1 fuses
 //               forward FFT -> spectral symbol -> inverse FFT on the same line
-//               (operators, single-axis derivatives) with an optional
-//               accumulate input.
+//               (operators, single-axis derivatives); MODE 4 is MODE 1
+//               plus an accumulate input of the output's layout.
 //   k_zc2c      contiguous complex lines (the z axis of a c2c transform).
 //   k_zr2c      contiguous real lines of length 2M: one M-point complex FFT
 //               of the even/odd packed samples + split to M+1 outputs.
@@ -151,8 +151,15 @@ template <typename T, int L, int EF = 0, int TLF = 0> struct ContigShape {
 };
 
 // ------------------------------------------------------------------ kernels
+// float tiles of up to 256 threads keep two CTAs per SM (while one CTA
+// computes, the other's loads are in flight); larger or double tiles would
+// spill under that register cap
+template <typename T, int L, int EF, int TCF>
+constexpr int strided_min_blocks() {
+  return (sizeof(T) == 4 && StridedShape<T, L, EF, TCF>::threads <= 256) ? 2 : 1;
+}
 template <typename T, int L, int MODE, int EF = 0, int TCF = 0>
-__global__ void __launch_bounds__(StridedShape<T, L, EF, TCF>::threads)
+__global__ void __launch_bounds__(StridedShape<T, L, EF, TCF>::threads, (strided_min_blocks<T, L, EF, TCF>()))
 k_strided(const StridedArgs a) {
   typedef LineFFT<T, L, EF> LN;
   typedef typename CT<T>::V V;
@@ -234,18 +241,129 @@ k_strided(const StridedArgs a) {
     auto sst = [&](int p, V x) { sm[p * TC + c] = c_conj(sym_apply<T>(a.sym, scol, p, x)); };
     LN::template run<true, false>(t, tw, ld, sst, xw, xr);
     __syncthreads();
-    // the accumulate input has the output's layout (main columns only)
-    const V* acc = a.acc ? static_cast<const V*>(a.acc) + (out - static_cast<V*>(a.out)) : nullptr;
     auto sld = [&](int p) { return sm[p * TC + c]; };
-    auto gst = [&](int p, V x) {
-      x.y = -x.y;
-      if (valid) {
-        if (acc) x = c_add(x, acc[p * ol]);
-        out[p * ol] = x;
+    if constexpr (MODE == 1) {
+      auto gst = [&](int p, V x) {
+        x.y = -x.y;
+        if (valid) out[p * ol] = x;
+      };
+      LN::template run<false, true>(t, tw, sld, gst, xw, xr);
+    } else {
+      // the accumulate input has the output's layout (main columns only);
+      // the result is staged in shared memory so that all of this thread's
+      // accumulate loads are in flight together
+      const V* acc = static_cast<const V*>(a.acc) + (out - static_cast<V*>(a.out));
+      auto sst2 = [&](int p, V x) { sm[p * TC + c] = c_conj(x); };
+      LN::template run<true, true>(t, tw, sld, sst2, xw, xr);
+      __syncthreads();
+      constexpr int CH = LN::E < 8 ? LN::E : 8;   // loads in flight per chunk (last chunk may be partial)
+#pragma unroll
+      for (int r0 = 0; r0 < LN::E; r0 += CH) {
+        V av[CH];
+#pragma unroll
+        for (int j = 0; j < CH; ++j)
+          if (r0 + j < LN::E) av[j] = acc[(t + (r0 + j) * LN::P) * ol];
+#pragma unroll
+        for (int j = 0; j < CH; ++j)
+          if (valid && r0 + j < LN::E)
+            out[(t + (r0 + j) * LN::P) * ol] = c_add(sm[(t + (r0 + j) * LN::P) * TC + c], av[j]);
       }
-    };
-    LN::template run<false, true>(t, tw, sld, gst, xw, xr);
+    }
   }
+}
+
+// ------------------------------------------------- pipelined strided pass
+// Asynchronous copies (cp.async) of one element into shared memory; 16-byte
+// elements bypass L1.
+template <int B>
+__device__ __forceinline__ void cp_async_elem(void* smem, const void* gmem) {
+  const unsigned sa = static_cast<unsigned>(__cvta_generic_to_shared(smem));
+  if constexpr (B == 16)
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
+  else
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+// Shape of the pipelined strided pass: NB shared-memory tile buffers of
+// L x TC complex (row p, column c at p*TC + c); one CTA per SM.
+template <typename T, int L, int EF = 0, int TCF = 0, int NB = 2> struct PipeShape {
+  typedef StridedShape<T, L, EF, TCF> S;
+  static constexpr int TC = S::TC, threads = S::threads, nbuf = NB;
+  static constexpr int tile = L * TC;
+  static constexpr size_t smem = size_t(NB) * tile * sizeof(typename CT<T>::V);
+};
+
+// k_strided (MODE 0) as a persistent, software-pipelined kernel: CTA k
+// transforms column tiles k, k + grid, k + 2*grid, ... and keeps the next
+// NB-1 tiles' loads in flight (cp.async into the spare buffers) while it
+// transforms the current one, so HBM reads never wait for a CTA's compute
+// and store phases.  Each thread's stage-0 loads are exactly the elements it
+// copied, so only the thread's own copies must have landed before the first
+// stage; the Stockham exchanges reuse the current tile's buffer.
+template <typename T, int L, int EF = 0, int TCF = 0, int NB = 2>
+__global__ void __launch_bounds__(PipeShape<T, L, EF, TCF, NB>::threads, 1)
+k_strided_pipe(const StridedArgs a) {
+  typedef LineFFT<T, L, EF> LN;
+  typedef typename CT<T>::V V;
+  typedef PipeShape<T, L, EF, TCF, NB> SH;
+  constexpr int TC = SH::TC, TILE = SH::tile;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  V* sm = reinterpret_cast<V*>(smraw);
+  const int c = threadIdx.x % TC;
+  const int t = threadIdx.x / TC;
+  const long long ntiles = (a.ncols + TC - 1) / TC;
+  const long long step = gridDim.x;
+  const V* tw = static_cast<const V*>(a.tw);
+  const T sg = a.inverse ? T(-1) : T(1);
+  // line starts of this thread's column in a tile (idle lanes use column 0
+  // and store nothing)
+  auto column = [&](long long tile, const V*& in, V*& out) {
+    const long long g = tile * TC + c;
+    const long long gs = g < a.ncols ? g : 0;
+    const long long slab = gs / a.cps, cc = gs - slab * a.cps;
+    in = static_cast<const V*>(a.in) + slab * a.in_slab + cc;
+    out = static_cast<V*>(a.out) + slab * a.out_slab + cc;
+    return g < a.ncols;
+  };
+  auto issue = [&](long long tile, int b) {
+    if (tile < ntiles) {
+      const V* in;
+      V* out;
+      column(tile, in, out);
+      V* buf = sm + b * TILE;
+#pragma unroll
+      for (int r = 0; r < LN::E; ++r) {
+        const int p = t + r * LN::P;
+        cp_async_elem<sizeof(V)>(buf + p * TC + c, in + p * a.in_line);
+      }
+    }
+    cp_async_commit();   // empty groups keep the group count uniform
+  };
+  long long tile = blockIdx.x;
+#pragma unroll
+  for (int s = 0; s < NB - 1; ++s) issue(tile + s * step, s);
+  int b = 0;
+  for (; tile < ntiles; tile += step) {
+    // refill the buffer the previous tile released, then wait for this tile
+    issue(tile + (NB - 1) * step, (b + NB - 1) % NB);
+    cp_async_wait<NB - 1>();
+    V* buf = sm + b * TILE;
+    const V* in;
+    V* out;
+    const bool valid = column(tile, in, out);
+    const long long ol = a.out_line;
+    auto ld = [&](int p) { V x = buf[p * TC + c]; x.y *= sg; return x; };
+    auto st = [&](int p, V x) { x.y *= sg; if (valid) out[p * ol] = x; };
+    auto xw = [&](int p, V x) { buf[p * TC + c] = x; };
+    auto xr = [&](int p) { return buf[p * TC + c]; };
+    LN::template run<false, true>(t, tw, ld, st, xw, xr);
+    __syncthreads();   // every thread is done with buffer b
+    b = b + 1 == NB ? 0 : b + 1;
+  }
+  cp_async_wait<0>();
 }
 
 // Contiguous-line kernels share this prologue: thread t of line li of the
@@ -358,21 +476,25 @@ k_zc2r(const ContigArgs a) {
   LN::template run<false, true>(t, static_cast<const V*>(a.tw), ld, st, xw, xr);
 }
 
-// real line r2c -> symbol(k) -> c2r, one pass (z-direction derivative)
-template <typename T, int M, int EF = 0, int TLF = 0>
+// real line r2c -> symbol(k) -> c2r, one pass (z-direction derivative);
+// ACC adds the accumulate input a.acc
+template <typename T, int M, int EF = 0, int TLF = 0, bool ACC = false>
 __global__ void __launch_bounds__(ContigShape<T, M, EF, TLF>::threads)
 k_zsym(const ContigArgs a) {
   AFG_CONTIG_PROLOGUE(M)
   const V* in = reinterpret_cast<const V*>(static_cast<const T*>(a.in) + ls * a.in_dist);
   V* out = reinterpret_cast<V*>(static_cast<T*>(a.out) + ls * a.out_dist);
-  const V* acc = a.acc ? reinterpret_cast<const V*>(static_cast<const T*>(a.acc) + ls * a.out_dist) : nullptr;
+  const V* acc = ACC ? reinterpret_cast<const V*>(static_cast<const T*>(a.acc) + ls * a.out_dist) : nullptr;
   const V* tw = static_cast<const V*>(a.tw);
   auto ld = [&](int p) { return in[p]; };
   LN::template run<true, false>(t, tw, ld, xw, xw, xr);
   __syncthreads();
   const V* twp = static_cast<const V*>(a.tw_post);
   const SymCol none{0, 0, 0, 0};
-  for (int k = t; 2 * k <= M; k += P) {
+#pragma unroll
+  for (int r = 0; r <= LN::E / 2; ++r) {
+    const int k = t + r * P;
+    if (2 * k > M) continue;
     if (k == 0) {
       V z0 = xr(0);
       V x0 = sym_apply<T>(a.sym, none, 0, c_make<V>(z0.x + z0.y, T(0)));
@@ -393,14 +515,31 @@ k_zsym(const ContigArgs a) {
     }
   }
   __syncthreads();
-  auto gst = [&](int p, V x) {
-    x.y = -x.y;
-    if (valid) {
-      if (acc) x = c_add(x, acc[p]);
-      out[p] = x;
-    }
-  };
-  LN::template run<false, true>(t, tw, xr, gst, xw, xr);
+  if constexpr (!ACC) {
+    auto gst = [&](int p, V x) {
+      x.y = -x.y;
+      if (valid) out[p] = x;
+    };
+    LN::template run<false, true>(t, tw, xr, gst, xw, xr);
+    return;
+  }
+  // accumulate: stage the result in shared memory, then read all of this
+  // thread's accumulate entries at once (one memory latency, not one per
+  // element) and store result + accumulate
+  auto sst = [&](int p, V x) { xw(p, c_conj(x)); };
+  LN::template run<true, true>(t, tw, xr, sst, xw, xr);
+  __syncthreads();
+  constexpr int CH = LN::E < 8 ? LN::E : 8;   // loads in flight per chunk (last chunk may be partial)
+#pragma unroll
+  for (int r0 = 0; r0 < LN::E; r0 += CH) {
+    V av[CH];
+#pragma unroll
+    for (int j = 0; j < CH; ++j)
+      if (r0 + j < LN::E) av[j] = acc[t + (r0 + j) * P];
+#pragma unroll
+    for (int j = 0; j < CH; ++j)
+      if (valid && r0 + j < LN::E) out[t + (r0 + j) * P] = c_add(xr(t + (r0 + j) * P), av[j]);
+  }
 }
 
 #undef AFG_CONTIG_PROLOGUE

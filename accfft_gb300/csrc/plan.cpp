@@ -363,7 +363,7 @@ struct Exec {
       unsupported("strided pass", L);
   }
   void strided_sym(const void* in, void* out, const void* acc, const void* tw, int L, long long ncols, long long cps,
-                   long long slab, long long line, const SymArgs& sym) {
+                   long long slab, long long line, const SymArgs& sym, const char* label) {
     if (!ok()) return;
     StridedArgs a{};
     a.in = in;
@@ -375,7 +375,8 @@ struct Exec {
     a.in_slab = a.out_slab = slab;
     a.in_line = a.out_line = line;
     a.sym = sym;
-    if (!timed("sym", p->stream, [&] { return launch_strided(p->dbl, L, 1, a, p->stream); }))
+    const int mode = acc ? 4 : 1;   // fused pass, with the accumulate input when given
+    if (!timed(label, p->stream, [&] { return launch_strided(p->dbl, L, mode, a, p->stream); }))
       unsupported("symbol pass", L);
   }
   // y pass over an [N0][N1][h] complex array, x pass over [N0][N1*h]
@@ -600,7 +601,7 @@ struct Exec {
     a.nlines = (long long)p->n[0] * p->n[1];
     a.in_dist = a.out_dist = row;
     a.sym = sym;
-    if (!timed("z_sym", p->stream, [&] { return launch_zsym(p->dbl, p->M(), a, p->stream); }))
+    if (!timed("z_deriv", p->stream, [&] { return launch_zsym(p->dbl, p->M(), a, p->stream); }))
       unsupported("z symbol pass", p->M());
   }
   void slab(bool forward, const void* in, void* out) {
@@ -899,7 +900,7 @@ int op3d(accfft_c_plan* p, int sym_kind, void* outr, const void* inr, double* ti
   ex.zr2c(inr, s, p->rrow());
   ex.ypass(s, s, h, 0);
   long long c = (long long)p->n[1] * h;
-  ex.strided_sym(s, s, nullptr, p->tw_x, p->n[0], c, c, 0, c, sym);
+  ex.strided_sym(s, s, nullptr, p->tw_x, p->n[0], c, c, 0, c, sym, "x_sym");
   ex.ypass(s, s, h, 1);
   ex.zc2r(s, outr, p->rrow());
   return ex.finish();
@@ -921,10 +922,10 @@ void deriv_axis(Exec& ex, accfft_c_plan* p, int axis, void* out, const void* in,
   const long long cols = N2 / 2;          // pairs holding data
   if (axis == 1) {
     ex.strided_sym(in, out, acc, p->tw_y, N1, (long long)N0 * cols, cols, (long long)N1 * cr, cr,
-                   make_sym(p, SYM_DERIV1, alpha / N1, N1));
+                   make_sym(p, SYM_DERIV1, alpha / N1, N1), "y_deriv");
   } else {
     ex.strided_sym(in, out, acc, p->tw_x, N0, (long long)N1 * cols, cols, cr, (long long)N1 * cr,
-                   make_sym(p, SYM_DERIV1, alpha / N0, N0));
+                   make_sym(p, SYM_DERIV1, alpha / N0, N0), "x_deriv");
   }
 }
 

@@ -47,9 +47,10 @@ def parse():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="pairs", choices=["pairs", "precision", "adjoint", "batch"],
+    ap.add_argument("--workload", default="pairs", choices=["pairs", "precision", "adjoint", "batch", "operators"],
                     help="pairs: the 512^3 r2c+c2r headline; precision: 1024^3 float32 vs the FP64 "
-                         "drop-in against the oracle; adjoint: 256^3 differentiation; batch: 64 uneven grids")
+                         "drop-in against the oracle; adjoint: 256^3 differentiation; batch: 64 uneven grids; "
+                         "operators: 512^3 laplace/biharmonic/inv_laplace/grad/divergence and the c2c pair")
     ap.add_argument("--n", type=int, default=512)
     ap.add_argument("--grid", type=int, nargs=3, default=None,
                     help="non-cubic grid N0 N1 N2 (smaller cases of the same kernels for profiling)")
@@ -236,7 +237,7 @@ def e2e_pairs_per_s(args, ag, torch, n, dt, u, stream, world, inflight=3):
     stream.synchronize()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
-    ksteps = max(3, min(args.steps, 30))
+    ksteps = max(3, min(args.steps, 100))
     e0.record(stream)
     run(ksteps)
     e1.record(stream)
@@ -541,6 +542,126 @@ def batch_workload(args):
     print(json.dumps(line), flush=True)
 
 
+def operators_workload(args):
+    """512^3 spectral operators and the c2c pair (float32 by default) on an
+    analytic field u = sin x cos 2y sin 3z + 0.5 cos 5x (grid x_i = 2 pi i / N),
+    whose exact derivatives check every result at full size.  Reports per
+    operator the mean time of K calls, the bytes its passes move (each pass
+    one read + one write of its arrays) against the measured HBM peak, and the
+    bytes the reference's pipeline moves for the same operator (r2c, a separate
+    multiply pass over the half spectrum, c2r)."""
+    import torch
+
+    import accfft_gb300 as ag
+
+    n = tuple(args.grid) if args.grid else (args.n,) * 3
+    N0, N1, N2 = n
+    dt = args.dtype
+    tdt = getattr(torch, dt)
+    esz = 4 if dt == "float32" else 8
+    N = N0 * N1 * N2
+    H = N0 * N1 * (N2 // 2 + 1)
+    peak, peak_kind = measured_peak()
+    ax = [torch.arange(m, device="cuda", dtype=torch.float64) * (2 * np.pi / m) for m in n]
+    x, y, z = ax[0][:, None, None], ax[1][None, :, None], ax[2][None, None, :]
+    u64 = torch.sin(x) * torch.cos(2 * y) * torch.sin(3 * z) + 0.5 * torch.cos(5 * x) + 0 * y * z
+    exact = {
+        "laplace": -14 * torch.sin(x) * torch.cos(2 * y) * torch.sin(3 * z) - 12.5 * torch.cos(5 * x) + 0 * y * z,
+        "biharmonic": 196 * torch.sin(x) * torch.cos(2 * y) * torch.sin(3 * z) + 312.5 * torch.cos(5 * x) + 0 * y * z,
+        "inv_laplace": -torch.sin(x) * torch.cos(2 * y) * torch.sin(3 * z) / 14 - 0.02 * torch.cos(5 * x) + 0 * y * z,
+    }
+    gx = torch.cos(x) * torch.cos(2 * y) * torch.sin(3 * z) - 2.5 * torch.sin(5 * x) + 0 * y * z
+    gy = -2 * torch.sin(x) * torch.sin(2 * y) * torch.sin(3 * z) + 0 * x
+    gz = 3 * torch.sin(x) * torch.cos(2 * y) * torch.cos(3 * z) + 0 * x
+    exact["grad"] = (gx, gy, gz)
+    exact["divergence"] = gx + gy + gz
+    u = u64.to(tdt)
+    del u64
+    plan = ag.PlanR2C(n, dt)
+    stream = torch.cuda.Stream()
+    plan.set_stream(stream, blocking=False)
+    outs = [torch.empty_like(u) for _ in range(3)]
+    spec = torch.empty((N0, N1, N2 // 2 + 1, 2), dtype=tdt, device="cuda")
+    back = torch.empty_like(u)
+    # pass structure of each call: bytes moved, and the reference's bytes
+    transform = esz * N + 10 * esz * H          # z (real in, half out) + y + x passes
+    fused_op = 2 * esz * N + 16 * esz * H       # z r2c, y, fused x, y^-1, z c2r
+    ref_op = 2 * transform + 4 * esz * H        # r2c, multiply pass, c2r
+    calls = {
+        "r2c+c2r": (lambda: (plan.r2c(u, spec), plan.c2r(spec, back)), 2 * transform, 2 * transform),
+        "laplace": (lambda: plan.laplace(outs[0], u), fused_op, ref_op),
+        "biharmonic": (lambda: plan.biharmonic(outs[0], u), fused_op, ref_op),
+        "inv_laplace": (lambda: plan.inv_laplace(outs[0], u), fused_op, ref_op),
+        # one real-to-real pass per component (single-axis derivative)
+        "grad": (lambda: plan.grad(outs[0], outs[1], outs[2], u), 3 * 2 * esz * N,
+                 3 * (2 * transform + 4 * esz * H)),
+        # x pass, then y and z passes accumulating into the result
+        "divergence": (lambda: plan.divergence(back, u, u, u), 8 * esz * N,
+                       3 * (2 * transform + 4 * esz * H) + 2 * 3 * esz * N),
+    }
+    K = max(5, min(args.steps, 50))
+    res = {}
+    for name, (fn, nbytes, ref_bytes) in calls.items():
+        with torch.cuda.stream(stream):
+            for _ in range(max(3, args.warmup)):
+                fn()
+        stream.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        with torch.cuda.stream(stream):
+            for _ in range(K):
+                fn()
+        b.record(stream)
+        stream.synchronize()
+        ms = a.elapsed_time(b) / K
+        if name == "r2c+c2r":
+            err = ((back.double() / N - u.double()).norm() / u.double().norm()).item()
+        elif name == "grad":
+            err = max(((o.double() - e).norm() / e.norm()).item() for o, e in zip(outs, exact["grad"]))
+        elif name == "divergence":
+            err = ((back.double() - exact[name]).norm() / exact[name].norm()).item()
+        else:
+            err = ((outs[0].double() - exact[name]).norm() / exact[name].norm()).item()
+        res[name] = {"ms": ms, "bytes": nbytes, "GBps": nbytes / ms / 1e6, "frac_of_peak": nbytes / ms / 1e6 / peak,
+                     "reference_pipeline_bytes": ref_bytes, "rel_l2_vs_exact": err}
+    # c2c pair on its own plan (complex field, 2 arrays)
+    del outs, spec, back
+    plan.destroy()
+    cu = torch.view_as_real(torch.polar(torch.ones(n, dtype=torch.float64, device="cuda"),
+                                        2 * np.pi * torch.rand(n, dtype=torch.float64, device="cuda",
+                                                               generator=torch.Generator(device="cuda").manual_seed(5))
+                                        )).to(tdt)
+    cs, cb = torch.empty_like(cu), torch.empty_like(cu)
+    pc = ag.PlanC2C(n, dt)
+    pc.set_stream(stream, blocking=False)
+    with torch.cuda.stream(stream):
+        for _ in range(3):
+            pc.c2c(-1, cu, cs)
+            pc.c2c(1, cs, cb)
+    stream.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    with torch.cuda.stream(stream):
+        for _ in range(K):
+            pc.c2c(-1, cu, cs)
+            pc.c2c(1, cs, cb)
+    b.record(stream)
+    stream.synchronize()
+    ms = a.elapsed_time(b) / K
+    nbytes = 2 * 3 * 2 * 2 * esz * N
+    err = ((cb.double() / N - cu.double()).norm() / cu.double().norm()).item()
+    res["c2c pair"] = {"ms": ms, "bytes": nbytes, "GBps": nbytes / ms / 1e6, "frac_of_peak": nbytes / ms / 1e6 / peak,
+                       "reference_pipeline_bytes": nbytes, "rel_l2_vs_exact": err}
+    pc.destroy()
+    label = "x".join(map(str, n))
+    line = {"metric": f"{label} {dt} spectral operators ms per call", "workload": "operators",
+            "value": res["laplace"]["ms"], "unit": "ms (laplace)", "higher_is_better": False,
+            "dtype": "f32" if dt == "float32" else "f64", "peak_GBps": peak, "peak_kind": peak_kind,
+            "calls": res, "steps": K,
+            "data": "analytic u = sin x cos 2y sin 3z + 0.5 cos 5x (exact derivatives); c2c: unit-modulus random phases"}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -551,6 +672,8 @@ def main():
         adjoint_workload(args)
     elif args.workload == "batch":
         batch_workload(args)
+    elif args.workload == "operators":
+        operators_workload(args)
     else:
         ours(args)
 
