@@ -47,10 +47,12 @@ def parse():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="pairs", choices=["pairs", "precision", "adjoint", "batch", "operators"],
+    ap.add_argument("--workload", default="pairs", choices=["pairs", "precision", "adjoint", "batch", "operators", "call"],
                     help="pairs: the 512^3 r2c+c2r headline; precision: 1024^3 float32 vs the FP64 "
                          "drop-in against the oracle; adjoint: 256^3 differentiation; batch: 64 uneven grids; "
-                         "operators: 512^3 laplace/biharmonic/inv_laplace/grad/divergence and the c2c pair")
+                         "operators: 512^3 laplace/biharmonic/inv_laplace/grad/divergence and the c2c pair; "
+                         "call: one public call (--call) repeated on --grid, for profiling")
+    ap.add_argument("--call", default="r2c", choices=["r2c", "c2r", "laplace", "grad", "divergence", "c2c"])
     ap.add_argument("--n", type=int, default=512)
     ap.add_argument("--grid", type=int, nargs=3, default=None,
                     help="non-cubic grid N0 N1 N2 (smaller cases of the same kernels for profiling)")
@@ -83,6 +85,17 @@ def algorithmic_bytes(n, esz):
         "x": 2 * H * c, "x_inv": 2 * H * c,
         "zy_slab": N * esz + H * c, "yz_slab": H * c + N * esz,
     }
+
+
+# dram__bytes_read.sum + dram__bytes_write.sum per launch from one ncu capture
+# of this bench (profiles/launches_512cube_f32_r2c_c2r.md); writes still in L2
+# at the end of a launch reach DRAM during the next one
+TRAFFIC = {
+    ((512, 512, 512), "float32"): {
+        "z_r2c": 536912128 + 480083712, "y": 539023616 + 480406016, "x": 539007744 + 475365632,
+        "x_inv": 539016448 + 484857344, "y_inv": 539123968 + 480226560, "z_c2r": 539004928 + 482352640,
+    },
+}
 
 
 KERNEL_OF = {"z_r2c": "k_zr2c", "y": "k_strided (y)", "x": "k_strided (x)", "x_inv": "k_strided (x)",
@@ -345,7 +358,8 @@ def ours(args):
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "kernel": KERNEL_OF.get(dom, dom), "pass": dom, "achieved": achieved,
                      "peak": peak, "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": None, "bytes_per_launch": dom_bytes, "ms_per_launch": per[dom]},
+                     "traffic": TRAFFIC.get((n, dt), {}).get(dom), "bytes_per_launch": dom_bytes,
+                     "ms_per_launch": per[dom]},
         "kernel_ms_per_launch": per,
         "kernel_ms_per_step": share,
         "kernel_frac_of_peak": {lab: nbytes[lab] / (per[lab] / 1000.0) / 1e9 / peak
@@ -662,6 +676,45 @@ def operators_workload(args):
     print(json.dumps(line), flush=True)
 
 
+def call_workload(args):
+    """One public call repeated (warmup + steps times) on an N(0,1) field of
+    --grid: the small cases the kernel profiles in profiles/ capture."""
+    import torch
+
+    import accfft_gb300 as ag
+
+    n = tuple(args.grid) if args.grid else (args.n,) * 3
+    dt = args.dtype
+    tdt = getattr(torch, dt)
+    g = torch.Generator(device="cuda").manual_seed(7)
+    u = torch.randn(n, generator=g, device="cuda", dtype=tdt)
+    outs = [torch.empty_like(u) for _ in range(3)]
+    spec = torch.empty((n[0], n[1], n[2] // 2 + 1, 2), dtype=tdt, device="cuda")
+    if args.call == "c2c":
+        plan = ag.PlanC2C(n, dt)
+        cu = torch.randn((*n, 2), generator=g, device="cuda", dtype=tdt)
+        cs = torch.empty_like(cu)
+        fn = lambda: plan.c2c(-1, cu, cs)
+    else:
+        plan = ag.PlanR2C(n, dt)
+        plan.r2c(u, spec)
+        fn = {"r2c": lambda: plan.r2c(u, spec), "c2r": lambda: plan.c2r(spec, outs[0]),
+              "laplace": lambda: plan.laplace(outs[0], u),
+              "grad": lambda: plan.grad(outs[0], outs[1], outs[2], u),
+              "divergence": lambda: plan.divergence(outs[0], u, outs[1], outs[2])}[args.call]
+    for _ in range(args.warmup):
+        fn()
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(args.steps):
+        fn()
+    b.record()
+    torch.cuda.synchronize()
+    print(json.dumps({"workload": "call", "call": args.call, "grid": list(n), "dtype": dt,
+                      "ms_per_call": a.elapsed_time(b) / max(1, args.steps)}), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -674,6 +727,8 @@ def main():
         batch_workload(args)
     elif args.workload == "operators":
         operators_workload(args)
+    elif args.workload == "call":
+        call_workload(args)
     else:
         ours(args)
 
