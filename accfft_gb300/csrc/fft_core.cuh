@@ -269,8 +269,17 @@ struct LineFFT {
 #pragma unroll
     for (int r = 0; r < E; ++r) v[r] = load(t + r * P);
     after_load();
+    stages(t, tw, xw, xr, [] {}, v);
+  }
+
+  // every stage on inputs already in v[r] = x[t + r*P] (stage-0 order);
+  // before_exchange() runs once before the first shared-memory exchange
+  template <class XW, class XR, class Sync>
+  __device__ __forceinline__ static void stages(int t, const V* __restrict__ tw, XW&& xw, XR&& xr,
+                                                Sync&& before_exchange, V (&v)[E]) {
     if constexpr (NS >= 1) Dft<E, 1>::run(v);
     if constexpr (NS >= 2) {
+      before_exchange();
       static_for<1, NS>([&](auto s_) {
         constexpr int s = decltype(s_)::value;
         constexpr int Rp = pl.radix[s - 1];
@@ -302,6 +311,44 @@ struct LineFFT {
           Dft<R, 1>::run(v + b * R);
         }
       });
+    }
+  }
+
+  // visit the outputs of compute() in place: f(p, value&), p = frequency index
+  template <class F>
+  __device__ __forceinline__ static void for_outputs(int t, V (&v)[E], F&& f) {
+    if constexpr (NS == 0) {
+      f(t, v[0]);
+    } else if constexpr (NS == 1) {
+#pragma unroll
+      for (int r = 0; r < E; ++r) f(r, v[r]);
+    } else {
+      constexpr int R = pl.radix[NS - 1];
+      constexpr int Ns = plan_ns_before(pl, NS - 1);
+#pragma unroll
+      for (int b = 0; b < E / R; ++b)
+#pragma unroll
+        for (int r = 0; r < R; ++r) f(t + b * P + r * Ns, v[b * R + r]);
+    }
+  }
+
+  // Reorder the outputs of compute() into stage-0 input order.  The last
+  // stage leaves thread t with frequencies t + b*P + r*(L/R) (b < E/R, r < R)
+  // in v[b*R + r]; since L/R = (E/R)*P these are exactly t + r'*P with
+  // r' = b + r*(E/R), the elements stage 0 of a following transform of the
+  // same line loads on this thread.  A compile-time register permutation:
+  // a transform, a per-frequency multiply and an inverse transform need no
+  // shared-memory round trip in between.
+  __device__ __forceinline__ static void to_load_order(V (&v)[E]) {
+    if constexpr (NS >= 2) {
+      constexpr int R = pl.radix[NS - 1];
+      V tmp[E];
+#pragma unroll
+      for (int b = 0; b < E / R; ++b)
+#pragma unroll
+        for (int r = 0; r < R; ++r) tmp[b + r * (E / R)] = v[b * R + r];
+#pragma unroll
+      for (int i = 0; i < E; ++i) v[i] = tmp[i];
     }
   }
 

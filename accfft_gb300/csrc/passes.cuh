@@ -237,24 +237,28 @@ k_strided(const StridedArgs a) {
     // layout is (j, N2/2)
     const SymCol scol = cc >= 0 ? sym_column(a.sym, gs) : sym_column_nyq(a.sym, slab);
     auto ld = [&](int p) { return in[p * il]; };
-    // forward result times the symbol, stored conjugated for the inverse run
-    auto sst = [&](int p, V x) { sm[p * TC + c] = c_conj(sym_apply<T>(a.sym, scol, p, x)); };
-    LN::template run<true, false>(t, tw, ld, sst, xw, xr);
-    __syncthreads();
-    auto sld = [&](int p) { return sm[p * TC + c]; };
+    // forward transform; the symbol is applied in registers and the result
+    // conjugated for the inverse run, which starts from the same registers
+    // (LineFFT::to_load_order) instead of a shared-memory round trip
+    V v[LN::E];
+    LN::compute(t, tw, ld, xw, xr, [] {}, v);
+    LN::for_outputs(t, v, [&](int p, V& x) { x = c_conj(sym_apply<T>(a.sym, scol, p, x)); });
+    LN::to_load_order(v);
+    // the inverse's first exchange waits until every thread has read the
+    // forward's last one
+    LN::stages(t, tw, xw, xr, [] { __syncthreads(); }, v);
     if constexpr (MODE == 1) {
-      auto gst = [&](int p, V x) {
+      LN::emit(t, v, [&](int p, V x) {
         x.y = -x.y;
         if (valid) out[p * ol] = x;
-      };
-      LN::template run<false, true>(t, tw, sld, gst, xw, xr);
+      });
     } else {
       // the accumulate input has the output's layout (main columns only);
       // the result is staged in shared memory so that all of this thread's
       // accumulate loads are in flight together
       const V* acc = static_cast<const V*>(a.acc) + (out - static_cast<V*>(a.out));
-      auto sst2 = [&](int p, V x) { sm[p * TC + c] = c_conj(x); };
-      LN::template run<true, true>(t, tw, sld, sst2, xw, xr);
+      if constexpr (LN::NS >= 2) __syncthreads();   // last exchange read before the staging writes
+      LN::emit(t, v, [&](int p, V x) { sm[p * TC + c] = c_conj(x); });
       __syncthreads();
       constexpr int CH = LN::E < 8 ? LN::E : 8;   // loads in flight per chunk (last chunk may be partial)
 #pragma unroll
@@ -270,100 +274,6 @@ k_strided(const StridedArgs a) {
       }
     }
   }
-}
-
-// ------------------------------------------------- pipelined strided pass
-// Asynchronous copies (cp.async) of one element into shared memory; 16-byte
-// elements bypass L1.
-template <int B>
-__device__ __forceinline__ void cp_async_elem(void* smem, const void* gmem) {
-  const unsigned sa = static_cast<unsigned>(__cvta_generic_to_shared(smem));
-  if constexpr (B == 16)
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
-  else
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gmem) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
-
-// Shape of the pipelined strided pass: NB shared-memory tile buffers of
-// L x TC complex (row p, column c at p*TC + c); one CTA per SM.
-template <typename T, int L, int EF = 0, int TCF = 0, int NB = 2> struct PipeShape {
-  typedef StridedShape<T, L, EF, TCF> S;
-  static constexpr int TC = S::TC, threads = S::threads, nbuf = NB;
-  static constexpr int tile = L * TC;
-  static constexpr size_t smem = size_t(NB) * tile * sizeof(typename CT<T>::V);
-};
-
-// k_strided (MODE 0) as a persistent, software-pipelined kernel: CTA k
-// transforms column tiles k, k + grid, k + 2*grid, ... and keeps the next
-// NB-1 tiles' loads in flight (cp.async into the spare buffers) while it
-// transforms the current one, so HBM reads never wait for a CTA's compute
-// and store phases.  Each thread's stage-0 loads are exactly the elements it
-// copied, so only the thread's own copies must have landed before the first
-// stage; the Stockham exchanges reuse the current tile's buffer.
-template <typename T, int L, int EF = 0, int TCF = 0, int NB = 2>
-__global__ void __launch_bounds__(PipeShape<T, L, EF, TCF, NB>::threads, 1)
-k_strided_pipe(const StridedArgs a) {
-  typedef LineFFT<T, L, EF> LN;
-  typedef typename CT<T>::V V;
-  typedef PipeShape<T, L, EF, TCF, NB> SH;
-  constexpr int TC = SH::TC, TILE = SH::tile;
-  extern __shared__ __align__(16) unsigned char smraw[];
-  V* sm = reinterpret_cast<V*>(smraw);
-  const int c = threadIdx.x % TC;
-  const int t = threadIdx.x / TC;
-  const long long ntiles = (a.ncols + TC - 1) / TC;
-  const long long step = gridDim.x;
-  const V* tw = static_cast<const V*>(a.tw);
-  const T sg = a.inverse ? T(-1) : T(1);
-  // line starts of this thread's column in a tile (idle lanes use column 0
-  // and store nothing)
-  auto column = [&](long long tile, const V*& in, V*& out) {
-    const long long g = tile * TC + c;
-    const long long gs = g < a.ncols ? g : 0;
-    const long long slab = gs / a.cps, cc = gs - slab * a.cps;
-    in = static_cast<const V*>(a.in) + slab * a.in_slab + cc;
-    out = static_cast<V*>(a.out) + slab * a.out_slab + cc;
-    return g < a.ncols;
-  };
-  auto issue = [&](long long tile, int b) {
-    if (tile < ntiles) {
-      const V* in;
-      V* out;
-      column(tile, in, out);
-      V* buf = sm + b * TILE;
-#pragma unroll
-      for (int r = 0; r < LN::E; ++r) {
-        const int p = t + r * LN::P;
-        cp_async_elem<sizeof(V)>(buf + p * TC + c, in + p * a.in_line);
-      }
-    }
-    cp_async_commit();   // empty groups keep the group count uniform
-  };
-  long long tile = blockIdx.x;
-#pragma unroll
-  for (int s = 0; s < NB - 1; ++s) issue(tile + s * step, s);
-  int b = 0;
-  for (; tile < ntiles; tile += step) {
-    // refill the buffer the previous tile released, then wait for this tile
-    issue(tile + (NB - 1) * step, (b + NB - 1) % NB);
-    cp_async_wait<NB - 1>();
-    V* buf = sm + b * TILE;
-    const V* in;
-    V* out;
-    const bool valid = column(tile, in, out);
-    const long long ol = a.out_line;
-    auto ld = [&](int p) { V x = buf[p * TC + c]; x.y *= sg; return x; };
-    auto st = [&](int p, V x) { x.y *= sg; if (valid) out[p * ol] = x; };
-    auto xw = [&](int p, V x) { buf[p * TC + c] = x; };
-    auto xr = [&](int p) { return buf[p * TC + c]; };
-    LN::template run<false, true>(t, tw, ld, st, xw, xr);
-    __syncthreads();   // every thread is done with buffer b
-    b = b + 1 == NB ? 0 : b + 1;
-  }
-  cp_async_wait<0>();
 }
 
 // Contiguous-line kernels share this prologue: thread t of line li of the
