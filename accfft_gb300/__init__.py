@@ -30,6 +30,9 @@ ACCFFT_FORWARD = -1
 ACCFFT_BACKWARD = +1
 ACCFFT_ESTIMATE = 1
 ACCFFT_MEASURE = 2
+# float r2c plans with radix-16 stages on the tensor cores (include/accfft_gb300.h)
+TC_TF32 = 0x100
+TC_BF16 = 0x200
 
 OK, EINVAL, EUNSUPPORTED, ECUDA, ENOTBAKED, EOVERFLOW = range(6)
 

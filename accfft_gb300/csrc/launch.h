@@ -41,6 +41,13 @@ bool launch_zsym(bool dbl, int M, const ContigArgs& a, cudaStream_t s);
 bool slab_available(bool dbl, int N1, int N2);
 bool launch_slab(bool dbl, int N1, int N2, bool forward, const SlabArgs& a, cudaStream_t s);
 
+// tensor-core forms of the r2c/c2r passes (float; form 1 = 3xTF32, 2 = split
+// BF16): lengths 128, 256, 512, 1024 (strided) and 128, 256, 512 (z half
+// length); err is a device word set when a completion wait timed out
+bool tc_length_supported(int len, bool contig);
+bool launch_strided_tc(int form, int L, const StridedArgs& a, int* err, cudaStream_t s);
+bool launch_z_tc(int form, bool r2c, int M, const ContigArgs& a, int* err, cudaStream_t s);
+
 // number of kernel launches issued by this process through the launchers
 unsigned long long launch_count();
 void count_launch();

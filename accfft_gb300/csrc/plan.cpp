@@ -68,8 +68,8 @@ void twiddle(long long m, long long d, long double* c, long double* s) {
 }
 
 // stage twiddles of a line length (layout fixed by plan_tw_offset)
-std::vector<long double> stage_table(int L, bool dbl) {
-  LinePlan pl = plan_for(L, dbl);
+std::vector<long double> stage_table(int L, bool dbl, int first_radix = 0) {
+  LinePlan pl = plan_select(L, dbl, first_radix);
   int n = plan_tw_size(pl);
   std::vector<long double> t(2 * (size_t)(n > 0 ? n : 1), 0.0L);
   for (int s = 1; s < pl.ns; ++s) {
@@ -136,6 +136,10 @@ struct accfft_c_plan {
   // main [N0][N1][M] (rows of M = N2/2 complex, 128-byte aligned) and the
   // Nyquist plane [N0][N1] (kz = N2/2) after it
   bool split = false;
+  // tensor-core form (ACCFFT_C_TC_*): 0 none, 1 3xTF32, 2 split BF16; its
+  // kernels set *tc_err when a completion wait timed out
+  int tc = 0;
+  int* tc_err = nullptr;
   // per-kernel CUDA-event profiling (accfft_c_set_profiling)
   bool profile = false;
   std::vector<cudaEvent_t> pev;
@@ -191,7 +195,7 @@ long long local_size_c2c(const int* n, int* isize, int* istart, int* osize, int*
 }
 
 // -------------------------------------------------------------- plan make
-accfft_c_plan* make_plan(int kind, bool dbl, const int* n, void* data, void* data_out) {
+accfft_c_plan* make_plan(int kind, bool dbl, const int* n, void* data, void* data_out, unsigned flags = 0) {
   g_err.clear();
   if (!n) {
     fail(ACCFFT_C_EINVAL, "plan: NULL size array");
@@ -214,8 +218,21 @@ accfft_c_plan* make_plan(int kind, bool dbl, const int* n, void* data, void* dat
            i == 0 ? "x" : i == 1 ? "y" : "z", lens[i], n[0], n[1], n[2]);
       return nullptr;
     }
+  const unsigned tcf = flags & (ACCFFT_C_TC_TF32 | ACCFFT_C_TC_BF16);
+  if (tcf) {
+    if (tcf == (ACCFFT_C_TC_TF32 | ACCFFT_C_TC_BF16) || kind != 1 || dbl) {
+      fail(ACCFFT_C_EUNSUPPORTED, "plan: tensor-core forms are float r2c plans with one of the two flags");
+      return nullptr;
+    }
+    if (!tc_length_supported(n[0], false) || !tc_length_supported(n[1], false) || !tc_length_supported(zlen, true)) {
+      fail(ACCFFT_C_EUNSUPPORTED, "plan: no tensor-core kernels for %dx%dx%d (x, y in 128..1024, N2/2 in 128..512, "
+           "powers of two)", n[0], n[1], n[2]);
+      return nullptr;
+    }
+  }
   auto* p = new accfft_c_plan;
   p->kind = kind;
+  p->tc = tcf == ACCFFT_C_TC_TF32 ? 1 : tcf == ACCFFT_C_TC_BF16 ? 2 : 0;
   p->dbl = dbl;
   for (int i = 0; i < 3; ++i) p->n[i] = n[i];
   // in place when the plan-time pointers are equal (the reference's rule);
@@ -230,9 +247,11 @@ accfft_c_plan* make_plan(int kind, bool dbl, const int* n, void* data, void* dat
 
   // twiddle tables, rounded from long double to the plan's precision
   std::vector<std::vector<long double>> tabs;
-  tabs.push_back(stage_table(n[0], dbl));
-  tabs.push_back(stage_table(n[1], dbl));
-  tabs.push_back(stage_table(zlen, dbl));
+  // the tensor-core forms run every line as radix 16 first (16 x 16 x ...)
+  const int er = p->tc ? 16 : 0;
+  tabs.push_back(stage_table(n[0], dbl, er));
+  tabs.push_back(stage_table(n[1], dbl, er));
+  tabs.push_back(stage_table(zlen, dbl, er));
   if (kind == 1) tabs.push_back(post_table(n[2] / 2));
   const size_t cbytes = dbl ? 16 : 8;
   std::vector<size_t> off;
@@ -257,6 +276,8 @@ accfft_c_plan* make_plan(int kind, bool dbl, const int* n, void* data, void* dat
   cudaError_t e = cudaMalloc(&p->tw_block, total);
   if (e == cudaSuccess) e = cudaMemcpy(p->tw_block, host.data(), total, cudaMemcpyHostToDevice);
   if (e == cudaSuccess && kind == 1) e = cudaMalloc(&p->scratch, (size_t)p->alloc_max);
+  if (e == cudaSuccess && p->tc) e = cudaMalloc(&p->tc_err, sizeof(int));
+  if (e == cudaSuccess && p->tc) e = cudaMemset(p->tc_err, 0, sizeof(int));
   if (e == cudaSuccess) e = cudaEventCreate(&p->ev0);
   if (e == cudaSuccess) e = cudaEventCreate(&p->ev1);
   if (e != cudaSuccess) {
@@ -358,8 +379,9 @@ struct Exec {
     a.in_slab = a.out_slab = slab;
     a.in_line = a.out_line = line;
     a.inverse = inverse;
-    if (!timed(tw == p->tw_x ? (inverse ? "x_inv" : "x") : (inverse ? "y_inv" : "y"), p->stream,
-               [&] { return launch_strided(p->dbl, L, 0, a, p->stream); }))
+    if (!timed(tw == p->tw_x ? (inverse ? "x_inv" : "x") : (inverse ? "y_inv" : "y"), p->stream, [&] {
+          return p->tc ? launch_strided_tc(p->tc, L, a, p->tc_err, p->stream) : launch_strided(p->dbl, L, 0, a, p->stream);
+        }))
       unsupported("strided pass", L);
   }
   void strided_sym(const void* in, void* out, const void* acc, const void* tw, int L, long long ncols, long long cps,
@@ -398,7 +420,10 @@ struct Exec {
     a.nlines = (long long)p->n[0] * p->n[1];
     a.in_dist = in_row;
     a.out_dist = p->H2();
-    if (!timed("z_r2c", p->stream, [&] { return launch_zr2c(p->dbl, p->M(), a, p->stream); }))
+    if (!timed("z_r2c", p->stream, [&] {
+          return p->tc ? launch_z_tc(p->tc, true, p->M(), a, p->tc_err, p->stream)
+                       : launch_zr2c(p->dbl, p->M(), a, p->stream);
+        }))
       unsupported("z r2c pass", p->M());
   }
   void zc2r(const void* in, void* out, long long out_row) {
@@ -412,7 +437,10 @@ struct Exec {
     a.nlines = (long long)p->n[0] * p->n[1];
     a.in_dist = p->H2();
     a.out_dist = out_row;
-    if (!timed("z_c2r", p->stream, [&] { return launch_zc2r(p->dbl, p->M(), a, p->stream); }))
+    if (!timed("z_c2r", p->stream, [&] {
+          return p->tc ? launch_z_tc(p->tc, false, p->M(), a, p->tc_err, p->stream)
+                       : launch_zc2r(p->dbl, p->M(), a, p->stream);
+        }))
       unsupported("z c2r pass", p->M());
   }
   // z passes and y pass restricted to slabs [s0, s0 + ns) on stream st
@@ -558,6 +586,7 @@ struct Exec {
     cudaStreamSynchronize(p->stream);
     cudaStreamSynchronize(p->stream2);
     if (p->hstage) cudaFree(p->hstage);
+  if (p->tc_err) cudaFree(p->tc_err);
     p->hstage = nullptr;
     p->hstage_bytes = 0;
     cudaError_t e = cudaMalloc(&p->hstage, (size_t)need);
@@ -745,6 +774,14 @@ struct Exec {
         cudaEventElapsedTime(&ms, p->ev0, p->ev1);
         timer[4] += ms / 1000.0;
       }
+      if (ok() && p->tc) {
+        int flag = 0;
+        cudaMemcpy(&flag, p->tc_err, sizeof(int), cudaMemcpyDeviceToHost);
+        if (flag) {
+          cudaMemset(p->tc_err, 0, sizeof(int));
+          rc = fail(ACCFFT_C_ECUDA, "execute: a tensor-core stage gave up waiting for its matrix products");
+        }
+      }
     }
     return rc;
   }
@@ -787,6 +824,8 @@ int check_plan(accfft_c_plan* p, int kind, int dbl, const char* fn) {
     return fail(ACCFFT_C_ENOTBAKED, "%s: the plan was made for a %s transform", fn, p->kind == 1 ? "r2c" : "c2c");
   if (dbl >= 0 && (int)p->dbl != dbl)
     return fail(ACCFFT_C_EINVAL, "%s: precision mismatch (plan is %s)", fn, p->dbl ? "double" : "float");
+  if (p->tc && strcmp(fn, "execute_r2c") && strcmp(fn, "execute_c2r") && strcmp(fn, "execute"))
+    return fail(ACCFFT_C_EUNSUPPORTED, "%s: tensor-core plans run full r2c / c2r transforms only", fn);
   return ACCFFT_C_OK;
 }
 
@@ -800,6 +839,24 @@ int exec_r2c_plan(accfft_c_plan* p, int direction, void* in, void* out, double* 
   if (int rc = check_addressable("execute", {in, out})) return rc;
   const bool host_in = classify(in) == 1, host_out = classify(out) == 1;
   const long long h = p->H2();
+  if (p->tc) {
+    if ((xyz & 7) != 7 || host_in || host_out || weight)
+      return fail(ACCFFT_C_EUNSUPPORTED, "execute: tensor-core plans run full transforms (xyz = 7) of device arrays");
+    if (direction != -1 && direction != 1)
+      return fail(ACCFFT_C_EINVAL, "execute: direction must be -1 or +1 (got %d)", direction);
+    Exec ex(p, timer);
+    if (direction == -1) {
+      ex.zr2c(in, out, p->rrow());
+      ex.ypass(out, out, h, 0);
+      ex.xpass(out, out, h, 0);
+    } else {
+      void* buf = p->inplace ? in : p->scratch;
+      ex.xpass(in, buf, h, 1);
+      ex.ypass(buf, buf, h, 1);
+      ex.zc2r(buf, out, p->rrow());
+    }
+    return ex.finish();
+  }
   Exec ex(p, timer);
   ex.weight = weight;
   if (direction == -1) {
@@ -956,17 +1013,17 @@ long long accfft_c_local_size_dft_c2c(const int n[3], int isize[3], int istart[3
   return local_size_c2c(n, isize, istart, osize, ostart, real_bytes);
 }
 
-accfft_c_plan* accfft_c_plan_dft_3d_r2c_gpu(const int n[3], double* data, double* data_out, unsigned) {
-  return make_plan(1, true, n, data, data_out);
+accfft_c_plan* accfft_c_plan_dft_3d_r2c_gpu(const int n[3], double* data, double* data_out, unsigned flags) {
+  return make_plan(1, true, n, data, data_out, flags);
 }
-accfft_c_plan* accfft_c_plan_dft_3d_r2c_gpuf(const int n[3], float* data, float* data_out, unsigned) {
-  return make_plan(1, false, n, data, data_out);
+accfft_c_plan* accfft_c_plan_dft_3d_r2c_gpuf(const int n[3], float* data, float* data_out, unsigned flags) {
+  return make_plan(1, false, n, data, data_out, flags);
 }
-accfft_c_plan* accfft_c_plan_dft_3d_c2c_gpu(const int n[3], double* data, double* data_out, unsigned) {
-  return make_plan(2, true, n, data, data_out);
+accfft_c_plan* accfft_c_plan_dft_3d_c2c_gpu(const int n[3], double* data, double* data_out, unsigned flags) {
+  return make_plan(2, true, n, data, data_out, flags);
 }
-accfft_c_plan* accfft_c_plan_dft_3d_c2c_gpuf(const int n[3], float* data, float* data_out, unsigned) {
-  return make_plan(2, false, n, data, data_out);
+accfft_c_plan* accfft_c_plan_dft_3d_c2c_gpuf(const int n[3], float* data, float* data_out, unsigned flags) {
+  return make_plan(2, false, n, data, data_out, flags);
 }
 
 void accfft_c_destroy_plan(accfft_c_plan* p) {
@@ -974,6 +1031,7 @@ void accfft_c_destroy_plan(accfft_c_plan* p) {
   if (p->tw_block) cudaFree(p->tw_block);
   if (p->scratch) cudaFree(p->scratch);
   if (p->hstage) cudaFree(p->hstage);
+  if (p->tc_err) cudaFree(p->tc_err);
   if (p->ev0) cudaEventDestroy(p->ev0);
   if (p->ev1) cudaEventDestroy(p->ev1);
   for (cudaEvent_t e : p->evb)
