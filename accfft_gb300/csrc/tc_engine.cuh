@@ -105,6 +105,14 @@ __device__ __forceinline__ bool mbar_try(uint32_t mbar, uint32_t parity) {
   return done != 0;
 }
 
+// cos(2 pi m / 16), m = 0..15, evaluated by the compiler (sin(2 pi m / 16) =
+// cos(2 pi (m - 4) / 16)); the device reads them, it never evaluates them
+__constant__ double kTcCos16[16] = {
+    ce_trig2pi(0, 16, false),  ce_trig2pi(1, 16, false),  ce_trig2pi(2, 16, false),  ce_trig2pi(3, 16, false),
+    ce_trig2pi(4, 16, false),  ce_trig2pi(5, 16, false),  ce_trig2pi(6, 16, false),  ce_trig2pi(7, 16, false),
+    ce_trig2pi(8, 16, false),  ce_trig2pi(9, 16, false),  ce_trig2pi(10, 16, false), ce_trig2pi(11, 16, false),
+    ce_trig2pi(12, 16, false), ce_trig2pi(13, 16, false), ce_trig2pi(14, 16, false), ce_trig2pi(15, 16, false)};
+
 // ----------------------------------------------------------- per-CTA context
 // Shared-memory state of the engine; tc_begin() sets it up, tc_end() frees
 // the tensor memory.  All threads of the CTA take part in every call.
@@ -149,15 +157,17 @@ __device__ __forceinline__ void tc_store4(unsigned char* base, int row, int k0, 
   }
 }
 
-// split x into the form's high and low parts
+// split x into the form's high and low parts, both rounded to the form's
+// type (the MMA would otherwise truncate the low part's tf32 mantissa)
 template <TcForm F>
 __device__ __forceinline__ void tc_split(float x, float& hi, float& lo) {
   if constexpr (F == TcForm::TF32x3) {
     hi = tf32_round(x);
+    lo = tf32_round(x - hi);
   } else {
     hi = __bfloat162float(__float2bfloat16_rn(x));
+    lo = x - hi;
   }
-  lo = x - hi;
 }
 
 // set up: W^T operands, mbarrier, tensor memory (cols >= 32 * blocks, a power
@@ -180,7 +190,7 @@ __device__ __forceinline__ void tc_begin(TcCtx& c, unsigned char* exchange, unsi
   for (int e = threadIdx.x; e < 32 * 32; e += THREADS) {
     const int n = e >> 5, k = e & 31;
     const int m = ((n & 15) * (k & 15)) & 15;
-    const double cs = ce_trig2pi(m, 16, false), sn = ce_trig2pi(m, 16, true);
+    const double cs = kTcCos16[m], sn = kTcCos16[(m + 12) & 15];
     double w;
     if (n < 16) w = k < 16 ? cs : sn;       // Wr | -Wi  (Wi = -sin)
     else w = k < 16 ? -sn : cs;             // Wi | Wr
@@ -188,6 +198,7 @@ __device__ __forceinline__ void tc_begin(TcCtx& c, unsigned char* exchange, unsi
     float hi, lo;
     tc_split<F>(wf, hi, lo);
     lo = static_cast<float>(w - static_cast<double>(hi));
+    if constexpr (F == TcForm::TF32x3) lo = tf32_round(lo);
     if constexpr (F == TcForm::TF32x3) {
       *reinterpret_cast<float*>(c.b_hi + tc_off<F>(n, k * 4)) = hi;
       *reinterpret_cast<float*>(c.b_lo + tc_off<F>(n, k * 4)) = lo;

@@ -11,11 +11,12 @@
 
 namespace afg {
 
-// strided tiles: TC columns x L; 512 threads at most (the tensor-core
-// operands take 2 x threads x 128 B of shared memory)
+// strided tiles: TC columns x L, 256 threads for L <= 512 (512 for 1024):
+// the tensor-core operands take 2 x threads x 128 B of shared memory, and
+// two CTAs per SM let one CTA's loads run while the other waits on its MMAs
 template <int L, TcForm F> struct TcStridedShape {
   static constexpr int P = L / 16;
-  static constexpr int TC = P >= 64 ? 8 : 16;
+  static constexpr int TC = P >= 32 ? 8 : 16;
   static constexpr int threads = P * TC;
   static constexpr size_t exch = size_t(L) * TC * sizeof(float2);   // = threads * 128 B
   static constexpr size_t smem = exch + tc_extra_smem<F>(threads);

@@ -53,6 +53,8 @@ def parse():
                          "operators: 512^3 laplace/biharmonic/inv_laplace/grad/divergence and the c2c pair; "
                          "call: one public call (--call) repeated on --grid, for profiling")
     ap.add_argument("--call", default="r2c", choices=["r2c", "c2r", "laplace", "grad", "divergence", "c2c"])
+    ap.add_argument("--tc", default="none", choices=["none", "tf32", "bf16"],
+                    help="call workload: r2c/c2r through a tensor-core plan")
     ap.add_argument("--n", type=int, default=512)
     ap.add_argument("--grid", type=int, nargs=3, default=None,
                     help="non-cubic grid N0 N1 N2 (smaller cases of the same kernels for profiling)")
@@ -60,6 +62,7 @@ def parse():
     ap.add_argument("--inflight", type=int, default=3, help="e2e: pairs in flight (plans on their own streams)")
     ap.add_argument("--dtype", default="float32", choices=["float32", "float64"])
     ap.add_argument("--no-baseline", action="store_true")
+    ap.add_argument("--no-variants", action="store_true", help="skip the tensor-core and FP64 forms of the pair")
     return ap.parse_args()
 
 
@@ -216,6 +219,53 @@ def reference_arm(args):
     print(json.dumps(line), flush=True)
 
 
+def precision_variants(ag, torch, n, u, stream, reps=10):
+    """The same pairs in the other precision forms: the radix-16 stages on the
+    tensor cores (3xTF32, split BF16) and the FP64 drop-in; pairs/s and the
+    forward spectrum's rel-L2 against the FP64 drop-in's (which the tests pin
+    to the oracle at 1e-12) on the same float32-rounded input."""
+    N0, N1, N2 = n
+    u64 = u.double()
+    out = {}
+    spec64 = None
+    for name, dt, flags in (("fp64_drop_in", "float64", 0), ("fp32_cuda_core", "float32", 0),
+                            ("fp32_tensor_core_3xtf32", "float32", ag.TC_TF32),
+                            ("fp32_tensor_core_split_bf16", "float32", ag.TC_BF16)):
+        try:
+            plan = ag.PlanR2C(n, dt, flags=flags) if flags else ag.PlanR2C(n, dt)
+        except ag.AccfftError as e:
+            out[name] = f"unavailable for this grid: {e}"
+            continue
+        plan.set_stream(stream, blocking=False)
+        x = u64 if dt == "float64" else u
+        spec = torch.empty((N0, N1, N2 // 2 + 1, 2), dtype=x.dtype, device="cuda")
+        back = torch.empty(n, dtype=x.dtype, device="cuda")
+        with torch.cuda.stream(stream):
+            for _ in range(2):
+                plan.r2c(x, spec)
+                plan.c2r(spec, back)
+        stream.synchronize()
+        k = 2 if dt == "float64" else reps
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        with torch.cuda.stream(stream):
+            for _ in range(k):
+                plan.r2c(x, spec)
+                plan.c2r(spec, back)
+        b.record(stream)
+        stream.synchronize()
+        ms = a.elapsed_time(b) / k
+        plan.r2c(x, spec)
+        stream.synchronize()
+        if spec64 is None:
+            spec64 = spec.clone()
+        err = ((spec.double() - spec64).norm() / spec64.norm()).item()
+        out[name] = {"pairs_per_s": 1000.0 / ms, "ms_per_pair": ms, "r2c_rel_l2_vs_fp64": err}
+        plan.destroy()
+        del spec, back
+    return out
+
+
 def e2e_pairs_per_s(args, ag, torch, n, dt, u, stream, world, inflight=3):
     """pairs/s through the public r2c / c2r calls with the real field in pinned
     host memory: every step the r2c reads the field from the host and the c2r
@@ -349,6 +399,7 @@ def ours(args):
     achieved = dom_bytes / (per[dom] / 1000.0) / 1e9
     step_bytes = sum(nbytes[lab] * cnt / args.steps for lab, (cnt, tot) in prof.items())
     e2e = None if args.no_e2e else e2e_pairs_per_s(args, ag, torch, n, dt, u, stream, world, args.inflight)
+    variants = None if args.no_variants or dt != "float32" else precision_variants(ag, torch, n, u, stream)
 
     if rank != 0:
         return
@@ -373,6 +424,7 @@ def ours(args):
         "e2e": e2e,
         "clocks": clocks,
         "roundtrip_rel_l2": err,
+        "variants": variants,
     }
     if not args.no_baseline and world == 1:
         v, sample, th = cpu_pairs_per_s(n)
@@ -392,8 +444,10 @@ def _oracle():
 def precision_workload(args):
     """1024^3 real field from a turbulence-like random Fourier series
     (amplitude N(0,1)|k|^-5/3 for 0 < |k| <= 256, uniform phases), rounded to
-    float32; r2c + c2r in float32 and with the FP64 drop-in, each result
-    against the oracle (double, host cores) applied to the same input."""
+    float32; r2c + c2r in float32 with CUDA-core radix stages, with the
+    radix-16 stages on the tensor cores (3xTF32 and split BF16), and with the
+    FP64 drop-in, each result against the oracle (double, host cores) applied
+    to the same input."""
     import torch
 
     import accfft_gb300 as ag
@@ -425,8 +479,14 @@ def precision_workload(args):
     t0 = time.perf_counter()
     ref_spec = orc.r2c(host_u)
     oracle_s = time.perf_counter() - t0
-    for name, dt in (("fp32_cuda_core", "float32"), ("fp64_drop_in", "float64")):
-        plan = ag.PlanR2C(n, dt)
+    variants = (("fp32_cuda_core", "float32", 0), ("fp32_tensor_core_3xtf32", "float32", ag.TC_TF32),
+                ("fp32_tensor_core_split_bf16", "float32", ag.TC_BF16), ("fp64_drop_in", "float64", 0))
+    for name, dt, flags in variants:
+        try:
+            plan = ag.PlanR2C(n, dt, flags=flags) if flags else ag.PlanR2C(n, dt)
+        except ag.AccfftError as e:
+            res[name] = f"unavailable for this grid: {e}"
+            continue
         x = u32 if dt == "float32" else uq
         spec = torch.empty((N0, N1, N2 // 2 + 1, 2), dtype=x.dtype, device="cuda")
         back = torch.empty(n, dtype=x.dtype, device="cuda")
@@ -449,7 +509,6 @@ def precision_workload(args):
                      "pairs_per_s": 1000.0 / ms}
         plan.destroy()
         del spec, back
-    res["tensor_core_split_bf16_3xtf32"] = "not built: the float32 path is HBM-bound with CUDA-core radix stages"
     line = {"metric": f"{N0}x{N1}x{N2} precision (rel-L2 vs FP64 oracle)", "workload": "precision",
             "value": res["fp32_cuda_core"]["r2c_rel_l2_vs_oracle"], "unit": "rel-L2", "higher_is_better": False,
             "variants": res, "oracle_seconds_r2c": oracle_s, "oracle_threads": os.cpu_count(),
@@ -700,7 +759,8 @@ def call_workload(args):
         cs = torch.empty_like(cu)
         fn = lambda: plan.c2c(-1, cu, cs)
     else:
-        plan = ag.PlanR2C(n, dt)
+        flags = {"none": 0, "tf32": ag.TC_TF32, "bf16": ag.TC_BF16}[args.tc]
+        plan = ag.PlanR2C(n, dt, flags=flags) if flags else ag.PlanR2C(n, dt)
         plan.r2c(u, spec)
         fn = {"r2c": lambda: plan.r2c(u, spec), "c2r": lambda: plan.c2r(spec, outs[0]),
               "laplace": lambda: plan.laplace(outs[0], u),
@@ -715,7 +775,7 @@ def call_workload(args):
         fn()
     b.record()
     torch.cuda.synchronize()
-    print(json.dumps({"workload": "call", "call": args.call, "grid": list(n), "dtype": dt,
+    print(json.dumps({"workload": "call", "call": args.call, "tc": args.tc, "grid": list(n), "dtype": dt,
                       "ms_per_call": a.elapsed_time(b) / max(1, args.steps)}), flush=True)
 
 
