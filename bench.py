@@ -73,6 +73,25 @@ def dist_env():
     return rank, world, local
 
 
+def max_over_ranks(value, world):
+    """The slowest rank's time: every rank runs an independent replica, the
+    job's time is the maximum (NCCL ranks reduce on the GPU, gloo on the host)."""
+    if world == 1:
+        return value
+    import torch
+    import torch.distributed as dist
+
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(value)], device=dev, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return t.item()
+
+
+def replicas_value(steps, world, max_ms):
+    """Whole-job pairs/s: all ranks' pairs over the slowest rank's time."""
+    return world * steps / (max_ms / 1000.0)
+
+
 def algorithmic_bytes(n, esz):
     """Bytes each kernel launch must move (its input read once, its output
     written once), per profiling label of the plan (accfft_c_profile_read)."""
@@ -382,13 +401,9 @@ def ours(args):
     launches = ag.kernel_launches() - launches0
     prof = plan.profile()
     plan.set_profiling(False)
-    total_ms = t0.elapsed_time(t1)
-    if world > 1:
-        tt = torch.tensor([total_ms], device="cuda")
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        total_ms = tt.item()
+    total_ms = max_over_ranks(t0.elapsed_time(t1), world)
     ms_step = total_ms / args.steps
-    value = world * args.steps / (total_ms / 1000.0)
+    value = replicas_value(args.steps, world, total_ms)
 
     nbytes = algorithmic_bytes(n, esz)
     per = {lab: tot / cnt for lab, (cnt, tot) in prof.items()}                 # ms per launch
