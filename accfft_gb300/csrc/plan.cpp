@@ -796,8 +796,9 @@ int check_align(const accfft_c_plan* p, const char* fn, std::initializer_list<co
   return ACCFFT_C_OK;
 }
 
-// 0: device (or managed) memory, 1: pinned host memory (kernels reach it
-// over the host link), -1: memory the GPU cannot address
+// 0: device (or managed) memory, 1: pinned host memory (copied through the
+// staging ring, or reached by kernels over the host link), -1: memory the
+// GPU cannot address
 int classify(const void* q) {
   if (!q) return 0;
   cudaPointerAttributes at;

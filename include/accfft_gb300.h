@@ -24,9 +24,11 @@
  *     contract).  accfft_c_set_stream() makes a plan enqueue asynchronously.
  *   - Arrays may be device memory or pinned host memory (cudaHostAlloc /
  *     cudaHostRegister); other host memory is rejected with ACCFFT_C_EINVAL.
- *     When an r2c input or a c2r output is pinned host memory, the z passes
- *     read or write it directly over the host link in slab batches that
- *     overlap with the y passes, so no device copy of the real array is made.
+ *     When an r2c input or a c2r output is pinned host memory, the plan
+ *     moves it with the copy engines in 16 slab batches through a ring of
+ *     three device staging slots, overlapped with the z and y kernels of the
+ *     batches already staged; other arrays in host memory are reached by the
+ *     kernels over the host link.
  *   - Plans are not thread-safe (one plan, one host thread at a time).
  */
 #ifndef ACCFFT_GB300_H
@@ -97,7 +99,8 @@ int accfft_c_set_zy_schedule(accfft_c_plan* plan, int mode);
 /* extension: per-kernel device times.  With profiling on, every kernel the
  * plan launches is bracketed by CUDA events on its stream;
  * accfft_c_profile_read waits for them and returns, per pass label ("z_r2c",
- * "y", "y_nyq", "x", "x_nyq", "z_c2r", "x_sym", ...), the launch count and
+ * "y", "x", "x_inv", "y_inv", "z_c2r", "x_sym", "x_deriv", "h2d", ...;
+ * host copies are included), the launch count and
  * total milliseconds since the previous read (labels: 32 bytes each).  The
  * return value is the number of labels written. */
 int accfft_c_set_profiling(accfft_c_plan* plan, int on);
