@@ -310,3 +310,24 @@ def test_kernel_profiling_labels(cuda, native):
     assert set(prof) == {"z_r2c", "y", "x_sym", "y_inv", "z_c2r"}
     plan.set_profiling(False)
     assert plan.profile() == {}
+
+
+@pytest.mark.parametrize("dtype", ["float64", "float32"])
+@pytest.mark.parametrize("n", [(1, 1, 2), (2, 1, 2), (1, 3, 4), (3, 1, 6), (1, 1, 16), (16, 1, 1 * 2)])
+def test_degenerate_sizes(cuda, native, oracle, n, dtype):
+    """Axes of length one and N2 = 2 (a single z pair) through r2c, c2r and
+    laplace."""
+    torch = cuda
+    u = rng(95).standard_normal(n)
+    plan = native.PlanR2C(n, dtype)
+    du = to_dev(torch, u, dtype)
+    spec = empty(torch, (n[0], n[1], n[2] // 2 + 1, 2), dtype)
+    plan.r2c(du, spec)
+    assert oracle.rel_l2(from_dev(spec, True), oracle.r2c(u.astype(dtype).astype(np.float64))) < TOL[dtype]
+    back = empty(torch, n, dtype)
+    plan.c2r(spec, back)
+    assert oracle.rel_l2(from_dev(back) / np.prod(n), u.astype(dtype)) < TOL[dtype]
+    lap = empty(torch, n, dtype)
+    plan.laplace(lap, du)
+    ref = oracle.spectral_op(u.astype(dtype).astype(np.float64), "laplace")
+    assert np.abs(from_dev(lap) - ref).max() <= TOL[dtype] * max(1.0, np.abs(ref).max())
