@@ -116,8 +116,8 @@ def algorithmic_bytes(n, esz):
 # at the end of a launch reach DRAM during the next one
 TRAFFIC = {
     ((512, 512, 512), "float32"): {
-        "z_r2c": 536912128 + 480083712, "y": 539023616 + 480406016, "x": 539007744 + 475365632,
-        "x_inv": 539016448 + 484857344, "y_inv": 539123968 + 480226560, "z_c2r": 539004928 + 482352640,
+        "z_r2c": 537037056 + 479984384, "y": 539036672 + 480273664, "x": 539024384 + 475256320,
+        "x_inv": 539027712 + 484878080, "y_inv": 539026176 + 480036096, "z_c2r": 539017728 + 481038080,
     },
 }
 
