@@ -601,6 +601,27 @@ def adjoint_workload(args):
     b.record()
     torch.cuda.synchronize()
     ms = a.elapsed_time(b) / 10
+    # the same step captured once as a CUDA graph (the plans' calls are
+    # capturable; static input and gradient tensors) and replayed
+    xs = u32.clone().requires_grad_(True)
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(side):
+        for _ in range(3):
+            torch.autograd.grad(loss(p32, xs, f32), xs)
+    torch.cuda.current_stream().wait_stream(side)
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph, capture_error_mode="relaxed"):
+        (g_graph,) = torch.autograd.grad(loss(p32, xs, f32), xs)
+    graph.replay()
+    torch.cuda.synchronize()
+    a.record()
+    for _ in range(10):
+        graph.replay()
+    b.record()
+    torch.cuda.synchronize()
+    graph_ms = a.elapsed_time(b) / 10
+    graph_err = ((g_graph - g32).norm() / g32.norm()).item()
     xd = u64.clone().requires_grad_(True)
     (g64,) = torch.autograd.grad(loss(p64, xd, f64), xd)
     gen = torch.Generator(device="cuda").manual_seed(13)
@@ -613,6 +634,7 @@ def adjoint_workload(args):
             w32 = max(w32, abs((g32.double() * v).sum().item() - fd) / abs(fd))
     line = {"metric": "256^3 float32 loss forward+backward ms (adjoint kernels)", "workload": "adjoint",
             "value": ms, "unit": "ms", "higher_is_better": False,
+            "graph_replay_ms": graph_ms, "graph_vs_eager_rel_l2": graph_err,
             "fd64_rel_err_worst_of_16": {"fp64_backward": w64, "fp32_backward": w32},
             "note": "fp32 directional derivatives along random N(0,1) directions are bounded by ~eps32*sqrt(N)",
             "data": "synthetic Gaussian-smoothed N(0,1) field, seeded"}
