@@ -322,13 +322,27 @@ accfft_c_plan* make_plan(int kind, bool dbl, const int* n, void* data, void* dat
 }
 
 // ------------------------------------------------------------ execution
+// Makes the plan's device current for the lifetime of a call and restores the
+// caller's afterwards, so a plan works from any current device of the process.
+struct DeviceGuard {
+  int prev = -1;
+  explicit DeviceGuard(int dev) {
+    int cur = 0;
+    if (cudaGetDevice(&cur) == cudaSuccess && cur != dev && cudaSetDevice(dev) == cudaSuccess) prev = cur;
+  }
+  ~DeviceGuard() {
+    if (prev >= 0) cudaSetDevice(prev);
+  }
+};
+
 struct Exec {
+  DeviceGuard guard;   // first member: constructed before anything touches the device
   accfft_c_plan* p;
   double* timer;
   int rc = ACCFFT_C_OK;
   int weight = 0;   // adjoint weighting of the z passes (ContigArgs::weight)
 
-  Exec(accfft_c_plan* plan, double* t) : p(plan), timer(t) {
+  Exec(accfft_c_plan* plan, double* t) : guard(plan->device), p(plan), timer(t) {
     if (p->blocking || timer) cudaEventRecord(p->ev0, p->stream);
   }
   bool ok() const { return rc == ACCFFT_C_OK; }
@@ -1029,6 +1043,7 @@ accfft_c_plan* accfft_c_plan_dft_3d_c2c_gpuf(const int n[3], float* data, float*
 
 void accfft_c_destroy_plan(accfft_c_plan* p) {
   if (!p) return;
+  DeviceGuard guard(p->device);
   if (p->tw_block) cudaFree(p->tw_block);
   if (p->scratch) cudaFree(p->scratch);
   if (p->hstage) cudaFree(p->hstage);
@@ -1062,6 +1077,7 @@ int accfft_c_set_profiling(accfft_c_plan* p, int on) {
 
 int accfft_c_profile_read(accfft_c_plan* p, int max_entries, char* labels, long long* counts, double* total_ms) {
   if (!p) return fail(ACCFFT_C_EINVAL, "profile_read: NULL plan");
+  DeviceGuard guard(p->device);
   Exec::fold_profile(p);
   int n = 0;
   for (auto& kv : p->pstats) {
