@@ -64,6 +64,7 @@ def lib() -> ctypes.CDLL:
     ll, i, u = ctypes.c_longlong, ctypes.c_int, ctypes.c_uint
     sig = {
         "accfft_c_last_error": ([], ctypes.c_char_p),
+        "accfft_c_last_error_code": ([], i),
         "accfft_c_version": ([], i),
         "accfft_c_length_supported": ([i], i),
         "accfft_c_kernel_launches": ([], ctypes.c_ulonglong),
@@ -176,7 +177,7 @@ class _Plan:
         d, o = _ptr(data), _ptr(data_out)
         self._h = fn(_ints(self.n), d, o, flags)
         if not self._h:
-            raise AccfftError(EINVAL, last_error())
+            raise AccfftError(L.accfft_c_last_error_code() or EINVAL, last_error())
         kind, dbl, inplace = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
         amax = ctypes.c_longlong()
         _check(L.accfft_c_plan_info(self._h, None, ctypes.byref(kind), ctypes.byref(dbl), ctypes.byref(inplace),

@@ -27,6 +27,7 @@ using namespace afg;
 namespace {
 
 thread_local std::string g_err;
+thread_local int g_err_code = ACCFFT_C_OK;
 
 int fail(int code, const char* fmt, ...) {
   char buf[512];
@@ -35,6 +36,7 @@ int fail(int code, const char* fmt, ...) {
   vsnprintf(buf, sizeof buf, fmt, ap);
   va_end(ap);
   g_err = buf;
+  g_err_code = code;
   return code;
 }
 
@@ -197,6 +199,7 @@ long long local_size_c2c(const int* n, int* isize, int* istart, int* osize, int*
 // -------------------------------------------------------------- plan make
 accfft_c_plan* make_plan(int kind, bool dbl, const int* n, void* data, void* data_out, unsigned flags = 0) {
   g_err.clear();
+  g_err_code = ACCFFT_C_OK;
   if (!n) {
     fail(ACCFFT_C_EINVAL, "plan: NULL size array");
     return nullptr;
@@ -834,6 +837,7 @@ int check_addressable(const char* fn, std::initializer_list<const void*> ptrs) {
 
 int check_plan(accfft_c_plan* p, int kind, int dbl, const char* fn) {
   g_err.clear();
+  g_err_code = ACCFFT_C_OK;
   if (!p) return fail(ACCFFT_C_EINVAL, "%s: NULL plan", fn);
   if (kind && p->kind != kind)
     return fail(ACCFFT_C_ENOTBAKED, "%s: the plan was made for a %s transform", fn, p->kind == 1 ? "r2c" : "c2c");
@@ -1012,6 +1016,7 @@ void set_last_error(int code, const char* msg) { fail(code, "%s", msg); }
 extern "C" {
 
 const char* accfft_c_last_error(void) { return g_err.c_str(); }
+int accfft_c_last_error_code(void) { return g_err_code; }
 int accfft_c_version(void) { return 1; }
 int accfft_c_length_supported(int len) { return length_supported(len) ? 1 : 0; }
 unsigned long long accfft_c_kernel_launches(void) { return launch_count(); }

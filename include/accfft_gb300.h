@@ -59,6 +59,9 @@ typedef struct accfft_c_plan accfft_c_plan; /* opaque */
 
 /* --- library --------------------------------------------------------- */
 const char* accfft_c_last_error(void);
+/* the ACCFFT_C_E* code of that failure (ACCFFT_C_OK after a successful
+ * call): plan creation reports failure by returning NULL, this says why */
+int accfft_c_last_error_code(void);
 int accfft_c_version(void);
 /* 1 if an axis of this length has compiled kernels (complex length for
  * c2c axes; for the real z axis of an r2c plan the check is on N2/2) */

@@ -68,8 +68,26 @@ def test_plan_rejects_bad_sizes(native):
     n = (ctypes.c_int * 3)(8, 13, 8)
     assert not L.accfft_c_plan_dft_3d_c2c_gpu(n, None, None, 2)
     assert "length 13" in native.last_error()
+    assert L.accfft_c_last_error_code() == native.EUNSUPPORTED
     n = (ctypes.c_int * 3)(0, 8, 8)
     assert not L.accfft_c_plan_dft_3d_r2c_gpu(n, None, None, 2)
+    assert L.accfft_c_last_error_code() == native.EINVAL
+    # the tensor-core forms are float r2c plans only (rejected before any device call)
+    n = (ctypes.c_int * 3)(128, 128, 256)
+    assert not L.accfft_c_plan_dft_3d_r2c_gpu(n, None, None, native.TC_TF32)
+    assert L.accfft_c_last_error_code() == native.EUNSUPPORTED
+    n = (ctypes.c_int * 3)(96, 128, 256)
+    assert not L.accfft_c_plan_dft_3d_r2c_gpuf(n, None, None, native.TC_BF16)
+    assert "tensor-core" in native.last_error()
+
+
+def test_python_plan_errors_carry_the_code(native):
+    with pytest.raises(native.AccfftError) as e:
+        native.PlanR2C((8, 13, 8), "float32")
+    assert e.value.code == native.EUNSUPPORTED
+    with pytest.raises(native.AccfftError) as e:
+        native.PlanC2C((0, 8, 8), "float64")
+    assert e.value.code == native.EINVAL
 
 
 def test_null_plan_is_an_error(native):
