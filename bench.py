@@ -360,7 +360,7 @@ def e2e_pairs_per_s(args, ag, torch, n, dt, u, stream, world, inflight=3):
     for *_, hb in lanes:
         err = ((hb / (n[0] * n[1] * n[2]) - hu).norm() / hu.norm()).item()
         assert err < (1e-5 if dt == "float32" else 1e-12), err
-    e2e_ms = e0.elapsed_time(e1) / ksteps
+    e2e_ms = max_over_ranks(e0.elapsed_time(e1) / ksteps, world)
     esz = hu.element_size()
     for _, plan, *_ in lanes:
         plan.destroy()
