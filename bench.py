@@ -353,10 +353,14 @@ def e2e_pairs_per_s(args, ag, torch, n, dt, u, stream, world, inflight=3):
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     ksteps = max(3, min(args.steps, 100))
+    if world > 1:
+        torch.distributed.barrier()
     e0.record(stream)
     run(ksteps)
     e1.record(stream)
     stream.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
     for *_, hb in lanes:
         err = ((hb / (n[0] * n[1] * n[2]) - hu).norm() / hu.norm()).item()
         assert err < (1e-5 if dt == "float32" else 1e-12), err
