@@ -75,3 +75,46 @@ def test_full_size_analytic_modes(cuda, native, dtype):
         Xc[i, j, k] = 0
     # everything else is rounding noise
     assert Xc.abs().max().item() < TOL[dtype] * scale * 10
+
+
+def test_full_size_c2c(cuda, native):
+    torch = cuda
+    n = (512, 512, 512)
+    g = torch.Generator(device="cuda").manual_seed(19)
+    a = torch.randn((*n, 2), generator=g, device="cuda")
+    plan = native.PlanC2C(n, "float32")
+    A = torch.empty_like(a)
+    plan.c2c(-1, a, A)
+    N = n[0] * n[1] * n[2]
+    e_a = (a.double() ** 2).sum().item()
+    assert abs((A.double() ** 2).sum().item() / N - e_a) / e_a < TOL["float32"]
+    back = torch.empty_like(a)
+    plan.c2c(1, A, back)
+    assert ((back.double() / N - a.double()).norm() / a.double().norm()).item() < TOL["float32"]
+
+
+def test_full_size_operators_fp64(cuda, native):
+    """512^3 double: laplace, inv_laplace and grad of
+    u = sin x cos 2y sin 3z + 0.5 cos 5x against their exact values."""
+    torch = cuda
+    n = (512, 512, 512)
+    ax = [torch.arange(m, device="cuda", dtype=torch.float64) * (2 * math.pi / m) for m in n]
+    x, y, z = ax[0][:, None, None], ax[1][None, :, None], ax[2][None, None, :]
+    s = torch.sin(x) * torch.cos(2 * y) * torch.sin(3 * z)
+    c5 = torch.cos(5 * x) + 0 * y * z
+    u = s + 0.5 * c5
+    plan = native.PlanR2C(n, "float64")
+    out = torch.empty_like(u)
+    plan.laplace(out, u)
+    ref = -14 * s - 12.5 * c5
+    assert ((out - ref).norm() / ref.norm()).item() < 1e-10
+    plan.inv_laplace(out, u)
+    ref = -s / 14 - 0.02 * c5
+    assert ((out - ref).norm() / ref.norm()).item() < 1e-12
+    gx, gy, gz = (torch.empty_like(u) for _ in range(3))
+    plan.grad(gx, gy, gz, u)
+    refs = (torch.cos(x) * torch.cos(2 * y) * torch.sin(3 * z) - 2.5 * torch.sin(5 * x) + 0 * y * z,
+            -2 * torch.sin(x) * torch.sin(2 * y) * torch.sin(3 * z),
+            3 * torch.sin(x) * torch.cos(2 * y) * torch.cos(3 * z))
+    for got, r in zip((gx, gy, gz), refs):
+        assert ((got - r).norm() / r.norm()).item() < 1e-11
