@@ -102,6 +102,7 @@ def lib() -> ctypes.CDLL:
         "accfft_c_laplace_gpuf_noalloc": ([ip, vp, vp, vp], i),
         "accfft_c_heat": ([vp, vp, vp, ctypes.c_double, dp], i),
         "accfft_c_helmholtz": ([vp, vp, vp, ctypes.c_double, dp], i),
+        "accfft_c_poisson": ([vp, vp, vp, i, dp], i),
         "accfft_c_r2c_adjoint": ([vp, vp, vp, dp], i),
         "accfft_c_c2r_adjoint": ([vp, vp, vp, dp], i),
         "accfft_c_grad_adjoint": ([vp, vp, vp, vp, vp, dp], i),
@@ -293,6 +294,13 @@ class PlanR2C(_Plan):
         """solve (alpha - laplace) out = a (zero mean part dropped where alpha + |k|^2 = 0)"""
         buf, tp = self._timer(timer)
         _check(lib().accfft_c_helmholtz(self._h, _ptr(out), _ptr(a), float(alpha), tp))
+        self._timer_back(buf, timer)
+
+    def poisson(self, phi, rho, method=0, timer=None):
+        """steps/step4's Poisson solve on the unit cube: method 0 uses the
+        finite-difference Laplacian's eigenvalues, method 1 -4 pi^2 |k|^2"""
+        buf, tp = self._timer(timer)
+        _check(lib().accfft_c_poisson(self._h, _ptr(phi), _ptr(rho), int(method), tp))
         self._timer_back(buf, timer)
 
     # ---- adjoints (backward passes of accfft_gb300.autograd)

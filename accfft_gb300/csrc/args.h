@@ -16,7 +16,11 @@ enum SymKind {
   SYM_DERIV1 = 8,       // i * w(p) * scale (1-D symbol along the pass axis)
   SYM_DERIV2 = 9,       // -w(p)^2 * scale
   SYM_HEAT = 10,        // exp(-(wx^2+wy^2+wz^2) * param) * scale
-  SYM_HELMHOLTZ = 11    // scale / (param + wx^2+wy^2+wz^2), 0 where that is 0
+  SYM_HELMHOLTZ = 11,   // scale / (param + wx^2+wy^2+wz^2), 0 where that is 0
+  SYM_POISSON_FD = 12,  // scale / (Dx + Dy + Dz), D_i = 2 (cos(2 pi k_i/N_i) - 1) N_i^2 (unit cube,
+                        // finite-difference Laplacian); 0 at k = 0
+  SYM_POISSON_SPEC = 13 // scale / (-4 pi^2 (kx^2+ky^2+kz^2)), k folded above N/2 without the
+                        // Nyquist filter; 0 at k = 0
 };
 
 struct SymArgs {
@@ -26,6 +30,10 @@ struct SymArgs {
   int axis_len;     // line length for the 1-D symbols
   double scale;
   double param;     // time (SYM_HEAT) or shift (SYM_HELMHOLTZ)
+  // SYM_POISSON_FD: tables D_i(|k|), |k| = 0..N_i/2, in the plan's precision,
+  // for x at fd_tab, y at fd_tab + fd_y, z at fd_tab + fd_z
+  const void* fd_tab;
+  int fd_y, fd_z;
 };
 
 struct StridedArgs {

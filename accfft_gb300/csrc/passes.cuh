@@ -46,7 +46,7 @@ struct SymCol {
 };
 __device__ __forceinline__ SymCol sym_column(const SymArgs& s, long long g) {
   SymCol c{0, 0, 0, 0};
-  if ((s.kind >= SYM_LAPLACE && s.kind <= SYM_GRADZ) || s.kind == SYM_HEAT || s.kind == SYM_HELMHOLTZ) {
+  if ((s.kind >= SYM_LAPLACE && s.kind <= SYM_GRADZ) || s.kind >= SYM_HEAT) {
     int y = int(g / s.h2), kz = int(g - (long long)y * s.h2);
     c.wy = fold_wave(y, s.n1); c.wz = fold_wave(kz, s.n2);
     c.wy_nf = fold_wave_nofilter(y, s.n1); c.wz_nf = fold_wave_nofilter(kz, s.n2);
@@ -113,6 +113,20 @@ __device__ __forceinline__ V sym_apply(const SymArgs& s, const SymCol& c, int p,
       int wx = fold_wave(p, s.n0);
       T d = T(s.param) + T(wx * wx + c.wy * c.wy + c.wz * c.wz);
       return c_scale(x, d == T(0) ? T(0) : sc / d);
+    }
+    case SYM_POISSON_FD: {
+      const int wx = fold_wave_nofilter(p, s.n0);
+      if (wx == 0 && c.wy_nf == 0 && c.wz_nf == 0) return c_make<V>(T(0), T(0));
+      const T* tab = static_cast<const T*>(s.fd_tab);
+      const T d = __ldg(tab + abs(wx)) + __ldg(tab + s.fd_y + abs(c.wy_nf)) + __ldg(tab + s.fd_z + abs(c.wz_nf));
+      return c_scale(x, sc / d);
+    }
+    case SYM_POISSON_SPEC: {
+      const int wx = fold_wave_nofilter(p, s.n0);
+      const int k2 = wx * wx + c.wy_nf * c.wy_nf + c.wz_nf * c.wz_nf;
+      if (k2 == 0) return c_make<V>(T(0), T(0));
+      // 4 pi^2
+      return c_scale(x, sc / (T(-39.4784176043574344753379639995) * T(k2)));
     }
     default:
       return x;

@@ -115,6 +115,7 @@ struct accfft_c_plan {
   const void* tw_y = nullptr;
   const void* tw_z = nullptr;
   const void* tw_post = nullptr;
+  const void* fd_tab = nullptr;   // finite-difference Laplacian eigenvalues per axis (r2c plans)
   // spectrum-sized scratch (r2c plans): out-of-place c2r and operators
   void* scratch = nullptr;
   // how the z and y passes of r2c/c2r run: 0 = one kernel each over the whole
@@ -256,6 +257,21 @@ accfft_c_plan* make_plan(int kind, bool dbl, const int* n, void* data, void* dat
   tabs.push_back(stage_table(n[1], dbl, er));
   tabs.push_back(stage_table(zlen, dbl, er));
   if (kind == 1) tabs.push_back(post_table(n[2] / 2));
+  // finite-difference Laplacian eigenvalues D(k) = 2 (cos(2 pi k / N) - 1) N^2
+  // for |k| = 0..N/2 of each axis (x, then y, then z; the Poisson solver's
+  // method 0), padded to an even count
+  if (kind == 1) {
+    std::vector<long double> fd;
+    for (int a = 0; a < 3; ++a) {
+      for (int k = 0; k <= n[a] / 2; ++k) {
+        long double c, sn;
+        twiddle(k, n[a], &c, &sn);
+        fd.push_back(2.0L * (c - 1.0L) * (long double)n[a] * (long double)n[a]);
+      }
+    }
+    if (fd.size() % 2) fd.push_back(0.0L);
+    tabs.push_back(fd);
+  }
   const size_t cbytes = dbl ? 16 : 8;
   std::vector<size_t> off;
   size_t total = 0;
@@ -321,6 +337,7 @@ accfft_c_plan* make_plan(int kind, bool dbl, const int* n, void* data, void* dat
   p->tw_y = base + off[1];
   p->tw_z = base + off[2];
   if (kind == 1) p->tw_post = base + off[3];
+  if (kind == 1) p->fd_tab = base + off[4];
   return p;
 }
 
@@ -950,6 +967,9 @@ SymArgs make_sym(const accfft_c_plan* p, int kind, double scale, int axis_len = 
   s.h2 = (int)p->H2();
   s.axis_len = axis_len;
   s.scale = scale;
+  s.fd_tab = p->fd_tab;
+  s.fd_y = p->n[0] / 2 + 1;
+  s.fd_z = s.fd_y + p->n[1] / 2 + 1;
   return s;
 }
 
@@ -1282,6 +1302,15 @@ int accfft_c_heat(accfft_c_plan* p, void* out, const void* in, double t, double*
 int accfft_c_helmholtz(accfft_c_plan* p, void* out, const void* in, double alpha, double* timer) {
   int rc = check_plan(p, 1, -1, "helmholtz");
   return rc ? rc : op3d(p, SYM_HELMHOLTZ, out, in, timer, alpha);
+}
+
+// steps/step4 (steps/step4/kernels.cu:24-110, steps/step4/step4_gpu.cpp:620-650):
+// r2c -> Poisson filter -> c2r as one fused operator on the unit cube
+int accfft_c_poisson(accfft_c_plan* p, void* phi, const void* rho, int method, double* timer) {
+  int rc = check_plan(p, 1, -1, "poisson");
+  if (rc) return rc;
+  if (method != 0 && method != 1) return fail(ACCFFT_C_EINVAL, "poisson: method must be 0 or 1 (got %d)", method);
+  return op3d(p, method == 0 ? SYM_POISSON_FD : SYM_POISSON_SPEC, phi, rho, timer);
 }
 
 }  // extern "C"

@@ -174,6 +174,13 @@ int accfft_c_inv_biharmonic(accfft_c_plan* plan, void* invBA, const void* A, dou
  * Each is one fused operator: z r2c, y, x forward * symbol * x backward, y, z c2r. */
 int accfft_c_heat(accfft_c_plan* plan, void* out, const void* in, double t, double* timer);
 int accfft_c_helmholtz(accfft_c_plan* plan, void* out, const void* in, double alpha, double* timer);
+/* extension: the Poisson solve of steps/step4 (steps/step4/step4_gpu.cpp:620-650,
+ * filter steps/step4/kernels.cu:24-110) as one fused operator on the unit
+ * cube (grid x_i = i / N_i): phi = c2r(r2c(rho) / S) / N with the zero mode
+ * set to 0.  method 0: S = 2 sum_i (cos(2 pi k_i / N_i) - 1) N_i^2, the
+ * finite-difference Laplacian; method 1: S = -4 pi^2 |k|^2 with k_i folded
+ * above N_i / 2 (no Nyquist filter). */
+int accfft_c_poisson(accfft_c_plan* plan, void* phi, const void* rho, int method, double* timer);
 
 /* --- adjoints ------------------------------------------------------------
  * No counterpart in the reference; they are the backward passes of the

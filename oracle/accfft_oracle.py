@@ -262,6 +262,25 @@ def symbol(kind: str, n, param: float = 0.0) -> np.ndarray:
     if kind in ("gradx", "grady", "gradz"):
         w = {"gradx": wx, "grady": wy, "gradz": wz}[kind]
         return 1j * scale * np.broadcast_to(w, (n0, n1, h2)).astype(np.float64)
+    if kind in ("poisson_fd", "poisson_spec"):
+        # steps/step4/kernels.cu:24-110: Poisson filter on the unit cube.
+        # method 0 (poisson_fd): finite-difference Laplacian eigenvalues
+        #   2 * sum_i (cos(2 pi k_i / N_i) - 1) / dx_i^2, dx_i = 1 / N_i
+        # method 1 (poisson_spec): -4 pi^2 |k|^2 with k_i folded above N_i/2
+        #   (no Nyquist filter); the zero mode is set to 0 (zero mean)
+        ix = np.arange(n0)[:, None, None]
+        iy = np.arange(n1)[None, :, None]
+        iz = np.arange(h2)[None, None, :]
+        if kind == "poisson_fd":
+            d = sum(2.0 * (np.cos(2 * np.pi * i / m) - 1.0) * m * m for i, m in ((ix, n0), (iy, n1), (iz, n2)))
+        else:
+            fx, fy, fz = (np.where(i > m // 2, i - m, i) for i, m in ((ix, n0), (iy, n1), (iz, n2)))
+            d = -4.0 * np.pi ** 2 * (fx * fx + fy * fy + fz * fz).astype(np.float64)
+        d = np.broadcast_to(d, (n0, n1, h2)).astype(np.float64)
+        out = np.zeros_like(d)
+        nz = np.broadcast_to((ix != 0) | (iy != 0) | (iz != 0), d.shape)
+        out[nz] = scale / d[nz]
+        return out
     raise ValueError(kind)
 
 

@@ -130,3 +130,17 @@ def test_heat_exact_solution_and_poisson(cuda, native, oracle):
     assert np.abs(from_dev(out) - s).max() < 1e-13
     plan.helmholtz(out, to_dev(torch, -3.0 * s, "float64"), 0.0)   # Poisson: -laplace v = -3 s -> v = -s
     assert np.abs(from_dev(out) + s).max() < 1e-13
+
+
+@pytest.mark.parametrize("dtype", ["float64", "float32"])
+@pytest.mark.parametrize("n", [(16, 12, 10), (48, 96, 64), (128, 128, 128), (160, 180, 200)])
+@pytest.mark.parametrize("method", [0, 1])
+def test_poisson_step4(cuda, native, oracle, n, dtype, method):
+    torch = cuda
+    u = rng(57).standard_normal(n)
+    plan = native.PlanR2C(n, dtype)
+    du = to_dev(torch, u, dtype)
+    out = empty(torch, n, dtype)
+    plan.poisson(out, du, method)
+    ref = oracle.spectral_op(u.astype(dtype).astype(np.float64), "poisson_fd" if method == 0 else "poisson_spec")
+    assert oracle.rel_l2(from_dev(out), ref) < TOL[dtype]

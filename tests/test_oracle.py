@@ -184,3 +184,17 @@ def test_golden_fixtures(oracle):
         else:
             got = oracle.spectral_op(x, op)
         assert oracle.rel_l2(got, y) < 1e-14, name
+
+
+def test_step4_poisson_sine_case(oracle):
+    """steps/step4/step4_gpu.cpp:100-115 (testcase sine on the unit cube):
+    method 1 returns the exact solution -rhs / (12 pi^2); method 0 returns the
+    discrete solution rhs / (6 N^2 (cos(2 pi / N) - 1)) of the same mode."""
+    N = 32
+    x = np.arange(N) / N
+    X, Y, Z = np.meshgrid(x, x, x, indexing="ij")
+    rhs = np.sin(2 * np.pi * X) * np.sin(2 * np.pi * Y) * np.sin(2 * np.pi * Z)
+    exact = -rhs / (3 * 4 * np.pi ** 2)
+    assert oracle.rel_l2(oracle.spectral_op(rhs, "poisson_spec"), exact) < 1e-13
+    discrete = rhs / (3 * 2 * N * N * (np.cos(2 * np.pi / N) - 1))
+    assert oracle.rel_l2(oracle.spectral_op(rhs, "poisson_fd"), discrete) < 1e-13
