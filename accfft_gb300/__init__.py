@@ -210,7 +210,8 @@ class _Plan:
         return {raw[32 * i:32 * i + 32].split(b"\0")[0].decode(): (int(counts[i]), float(ms[i])) for i in range(k)}
 
     def set_zy_schedule(self, mode):
-        """0: separate z and y passes (default); 1: cluster slab kernel (r2c plans)"""
+        """0: separate z and y passes (default); 1: cluster slab kernel;
+        2: persistent z+y kernel (r2c plans, where the grid has the kernel)"""
         _check(lib().accfft_c_set_zy_schedule(self._h, int(mode)))
 
     def destroy(self):

@@ -19,8 +19,9 @@ so instances can run concurrently: the capture forks the work over
 size) and joins them before the graph ends.
 
 The autotuner times, per distinct grid, the z+y schedules the library offers
-for it (separate z and y passes, or the cluster slab kernel where the grid has
-one; accfft_c_set_zy_schedule) and then the number of capture streams, and
+for it (separate z and y passes, the cluster slab kernel or the persistent z+y
+kernel where the grid has one; accfft_c_set_zy_schedule) and then the number
+of capture streams, and
 keeps the fastest; schedules are cached per (dtype, shape) in a JSON file if
 `cache` is given.  report() lists the compiled radix plan of every axis.
 """
@@ -81,7 +82,7 @@ class _Instance:
     def make_plan(self, schedule):
         if self.plan is None:
             self.plan = PlanR2C(self.shape, self.dtype)
-        self.plan.set_zy_schedule(1 if schedule == "fused" else 0)
+        self.plan.set_zy_schedule({"split": 0, "fused": 1, "persistent": 2}[schedule])
 
     def enqueue(self, stream):
         p = self.plan
@@ -183,7 +184,7 @@ class BatchPlan:
             probe = _Instance(-1, shape, "r2c_c2r", self.dtype, self.instances[0].inp.device)
             probe.inp.uniform_(-1, 1)
             best = None
-            for sched in ("split", "fused"):
+            for sched in ("split", "fused", "persistent"):
                 try:
                     probe.make_plan(sched)
                 except AccfftError:

@@ -48,6 +48,12 @@ bool tc_length_supported(int len, bool contig);
 bool launch_strided_tc(int form, int L, const StridedArgs& a, int* err, cudaStream_t s);
 bool launch_z_tc(int form, bool r2c, int M, const ContigArgs& a, int* err, cudaStream_t s);
 
+// persistent z+y kernels (zy_fused.cu): grids whose z rows and y columns
+// run on the same tile shape; ctl holds 2 + n0 zeroed words
+bool zy_persistent_available(bool dbl, int M, int L);
+bool launch_zy_persistent(bool dbl, bool forward, int M, int L, const ContigArgs& z, const StridedArgs& y,
+                          unsigned* ctl, int n0, int lead, cudaStream_t s);
+
 // number of kernel launches issued by this process through the launchers
 unsigned long long launch_count();
 void count_launch();

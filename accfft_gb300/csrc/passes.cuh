@@ -172,9 +172,10 @@ template <typename T, int L, int EF, int TCF>
 constexpr int strided_min_blocks() {
   return (sizeof(T) == 4 && StridedShape<T, L, EF, TCF>::threads <= 256) ? 2 : 1;
 }
-template <typename T, int L, int MODE, int EF = 0, int TCF = 0>
-__global__ void __launch_bounds__(StridedShape<T, L, EF, TCF>::threads, (strided_min_blocks<T, L, EF, TCF>()))
-k_strided(const StridedArgs a) {
+// One column tile of the strided pass (the body of k_strided; also run by the
+// persistent z+y kernels).  CG loads the input through L2 only.
+template <typename T, int L, int MODE, int EF = 0, int TCF = 0, bool CG = false>
+__device__ __forceinline__ void strided_tile(const StridedArgs& a, long long tile) {
   typedef LineFFT<T, L, EF> LN;
   typedef typename CT<T>::V V;
   constexpr int TC = StridedShape<T, L, EF, TCF>::TC;
@@ -182,7 +183,7 @@ k_strided(const StridedArgs a) {
   V* sm = reinterpret_cast<V*>(smraw);
   const int c = threadIdx.x % TC;
   const int t = threadIdx.x / TC;
-  const long long g = (long long)blockIdx.x * TC + c;
+  const long long g = tile * TC + c;
   const bool valid = g < a.ncols;
   const long long gs = valid ? g : 0;          // idle lanes read column 0, store nothing
   long long slab = gs / a.cps;
@@ -203,7 +204,13 @@ k_strided(const StridedArgs a) {
   auto xr = [&](int p) { return sm[p * TC + c]; };
   if constexpr (MODE == 0) {
     const T sg = a.inverse ? T(-1) : T(1);
-    auto ld = [&](int p) { V x = in[p * il]; x.y *= sg; return x; };
+    auto ld = [&](int p) {
+      V x;
+      if constexpr (CG) x = __ldcg(in + p * il);
+      else x = in[p * il];
+      x.y *= sg;
+      return x;
+    };
     auto st = [&](int p, V x) { x.y *= sg; if (valid) out[p * ol] = x; };
     LN::template run<false, false>(t, tw, ld, st, xw, xr);
   } else if constexpr (MODE == 2) {
@@ -290,6 +297,12 @@ k_strided(const StridedArgs a) {
   }
 }
 
+template <typename T, int L, int MODE, int EF = 0, int TCF = 0>
+__global__ void __launch_bounds__(StridedShape<T, L, EF, TCF>::threads, (strided_min_blocks<T, L, EF, TCF>()))
+k_strided(const StridedArgs a) {
+  strided_tile<T, L, MODE, EF, TCF>(a, blockIdx.x);
+}
+
 // Contiguous-line kernels share this prologue: thread t of line li of the
 // CTA, the line's padded shared-memory row and the validity of the line.
 #define AFG_CONTIG_PROLOGUE(L_)                                                \
@@ -300,7 +313,7 @@ k_strided(const StridedArgs a) {
   extern __shared__ __align__(16) unsigned char smraw[];                       \
   V* sm = reinterpret_cast<V*>(smraw);                                         \
   const int t = threadIdx.x % P, li = threadIdx.x / P;                         \
-  const long long line = (long long)blockIdx.x * TL + li;                      \
+  const long long line = tile * TL + li;                                       \
   const bool valid = line < a.nlines;                                          \
   const long long ls = valid ? line : 0;                                       \
   V* sl = sm + li * SH::LP;                                                    \
@@ -310,6 +323,7 @@ k_strided(const StridedArgs a) {
 template <typename T, int L, int EF = 0, int TLF = 0>
 __global__ void __launch_bounds__(ContigShape<T, L, EF, TLF>::threads)
 k_zc2c(const ContigArgs a) {
+  const long long tile = blockIdx.x;
   AFG_CONTIG_PROLOGUE(L)
   const V* in = static_cast<const V*>(a.in) + ls * a.in_dist;
   V* out = static_cast<V*>(a.out) + ls * a.out_dist;
@@ -337,8 +351,7 @@ __device__ __forceinline__ V c2r_merge(V xk, V xm, V wc) {
 }
 
 template <typename T, int M, int EF = 0, int TLF = 0>
-__global__ void __launch_bounds__(ContigShape<T, M, EF, TLF>::threads)
-k_zr2c(const ContigArgs a) {
+__device__ __forceinline__ void zr2c_tile(const ContigArgs& a, long long tile) {
   AFG_CONTIG_PROLOGUE(M)
   const V* in = reinterpret_cast<const V*>(static_cast<const T*>(a.in) + ls * a.in_dist);
   V* out = static_cast<V*>(a.out) + ls * a.out_dist;
@@ -367,7 +380,13 @@ k_zr2c(const ContigArgs a) {
 
 template <typename T, int M, int EF = 0, int TLF = 0>
 __global__ void __launch_bounds__(ContigShape<T, M, EF, TLF>::threads)
-k_zc2r(const ContigArgs a) {
+k_zr2c(const ContigArgs a) {
+  zr2c_tile<T, M, EF, TLF>(a, blockIdx.x);
+}
+
+// the body of k_zc2r for one tile of TL lines
+template <typename T, int M, int EF = 0, int TLF = 0, bool CG = false>
+__device__ __forceinline__ void zc2r_tile(const ContigArgs& a, long long tile) {
   AFG_CONTIG_PROLOGUE(M)
   const V* in = static_cast<const V*>(a.in) + ls * a.in_dist;
   V* out = reinterpret_cast<V*>(static_cast<T*>(a.out) + ls * a.out_dist);
@@ -375,9 +394,16 @@ k_zc2r(const ContigArgs a) {
     // stage the M+1 input entries: E independent loads per thread, then the
     // Nyquist entry by thread 0
     V v[LN::E];
+    V nyq;
+    if constexpr (CG) {
 #pragma unroll
-    for (int r = 0; r < LN::E; ++r) v[r] = in[t + r * P];
-    V nyq = a.nyq_in ? static_cast<const V*>(a.nyq_in)[ls] : in[t == 0 ? M : 0];
+      for (int r = 0; r < LN::E; ++r) v[r] = __ldcg(in + t + r * P);
+      nyq = __ldcg(in + (t == 0 ? M : 0));
+    } else {
+#pragma unroll
+      for (int r = 0; r < LN::E; ++r) v[r] = in[t + r * P];
+      nyq = a.nyq_in ? static_cast<const V*>(a.nyq_in)[ls] : in[t == 0 ? M : 0];
+    }
 #pragma unroll
     for (int r = 0; r < LN::E; ++r) xw(t + r * P, v[r]);
     if (t == 0) xw(M, nyq);
@@ -400,11 +426,18 @@ k_zc2r(const ContigArgs a) {
   LN::template run<false, true>(t, static_cast<const V*>(a.tw), ld, st, xw, xr);
 }
 
+template <typename T, int M, int EF = 0, int TLF = 0>
+__global__ void __launch_bounds__(ContigShape<T, M, EF, TLF>::threads)
+k_zc2r(const ContigArgs a) {
+  zc2r_tile<T, M, EF, TLF>(a, blockIdx.x);
+}
+
 // real line r2c -> symbol(k) -> c2r, one pass (z-direction derivative);
 // ACC adds the accumulate input a.acc
 template <typename T, int M, int EF = 0, int TLF = 0, bool ACC = false>
 __global__ void __launch_bounds__(ContigShape<T, M, EF, TLF>::threads)
 k_zsym(const ContigArgs a) {
+  const long long tile = blockIdx.x;
   AFG_CONTIG_PROLOGUE(M)
   const V* in = reinterpret_cast<const V*>(static_cast<const T*>(a.in) + ls * a.in_dist);
   V* out = reinterpret_cast<V*>(static_cast<T*>(a.out) + ls * a.out_dist);

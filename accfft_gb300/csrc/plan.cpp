@@ -126,6 +126,9 @@ struct accfft_c_plan {
   int zy_batches = 1;
   cudaStream_t stream2 = nullptr;
   static constexpr int kMaxBatches = 64;
+  // control words of the persistent z+y kernels (2 + N0, zeroed per launch)
+  unsigned* zy_ctl = nullptr;
+  int zy_lead = 32;   // slabs between a slab's first and second pass (ACCFFT_GB300_ZY_LEAD)
   // pinned-host real arrays: slab batches staged through a device ring
   static constexpr int kHostBatches = 16, kHostSlots = 3;
   void* hstage = nullptr;
@@ -326,6 +329,9 @@ accfft_c_plan* make_plan(int kind, bool dbl, const int* n, void* data, void* dat
     std::string zy = env ? env : "";
     if (zy == "fused" && slab_available(dbl, n[1], n[2])) {
       p->zy_mode = 1;
+    } else if (zy == "persistent") {
+      p->zy_mode = 3;
+      if (const char* le = getenv("ACCFFT_GB300_ZY_LEAD")) p->zy_lead = atoi(le) > 0 ? atoi(le) : 1;
     } else if (zy.rfind("batch", 0) == 0) {
       int nb = atoi(zy.c_str() + 5);
       p->zy_mode = 2;
@@ -533,6 +539,10 @@ struct Exec {
       slab(forward, in, out);
       return;
     }
+    if (p->zy_mode == 3 && weight == 0 && zy_persistent_available(p->dbl, p->M(), p->n[1])) {
+      zy_persistent(forward, in, mid, out, row);
+      return;
+    }
     const long long N0 = p->n[0];
     int nb = p->zy_mode == 2 ? p->zy_batches : 1;
     if (nb > N0) nb = (int)N0;
@@ -557,6 +567,52 @@ struct Exec {
       cudaEventRecord(p->evb[nb + 1], B);
       cudaStreamWaitEvent(A, p->evb[nb + 1], 0);
     }
+  }
+  // z and y in one persistent kernel (zy_fused.cu); mid is the spectrum the
+  // backward y pass writes and the z c2r pass reads
+  void zy_persistent(bool forward, const void* in, void* mid, void* out, long long row) {
+    const long long N0 = p->n[0], H = p->H2();
+    const size_t ctl_bytes = size_t(2 + N0) * sizeof(unsigned);
+    if (!p->zy_ctl) {
+      cudaError_t e = cudaMalloc(&p->zy_ctl, ctl_bytes);
+      if (e != cudaSuccess) {
+        p->zy_ctl = nullptr;
+        rc = cuda_fail(e, "execute: control words of the persistent z+y kernel");
+        return;
+      }
+    }
+    cudaError_t e = cudaMemsetAsync(p->zy_ctl, 0, ctl_bytes, p->stream);
+    if (e != cudaSuccess) {
+      rc = cuda_fail(e, "execute: clearing the persistent kernel's control words");
+      return;
+    }
+    ContigArgs z{};
+    z.tw = p->tw_z;
+    z.tw_post = p->tw_post;
+    StridedArgs y{};
+    y.tw = p->tw_y;
+    y.in_line = y.out_line = H;
+    if (forward) {
+      z.in = in;
+      z.in_dist = row;
+      z.out = out;
+      z.out_dist = H;
+      y.in = y.out = out;
+    } else {
+      y.in = in;
+      y.out = mid;
+      y.inverse = 1;
+      z.in = mid;
+      z.in_dist = H;
+      z.out = out;
+      z.out_dist = row;
+    }
+    int lead = p->zy_lead;
+    if (lead > N0) lead = int(N0);
+    if (!timed(forward ? "zy_persistent" : "yz_persistent", p->stream, [&] {
+          return launch_zy_persistent(p->dbl, forward, p->M(), p->n[1], z, y, p->zy_ctl, int(N0), lead, p->stream);
+        }))
+      unsupported("persistent z+y pass", p->M());
   }
   static const void* real_at(const void* base, long long s0, long long row, long long N1, long long esz) {
     return static_cast<const char*>(base) + s0 * N1 * row * esz;
@@ -621,6 +677,7 @@ struct Exec {
     cudaStreamSynchronize(p->stream2);
     if (p->hstage) cudaFree(p->hstage);
   if (p->tc_err) cudaFree(p->tc_err);
+  if (p->zy_ctl) cudaFree(p->zy_ctl);
     p->hstage = nullptr;
     p->hstage_bytes = 0;
     cudaError_t e = cudaMalloc(&p->hstage, (size_t)need);
@@ -1073,6 +1130,7 @@ void accfft_c_destroy_plan(accfft_c_plan* p) {
   if (p->scratch) cudaFree(p->scratch);
   if (p->hstage) cudaFree(p->hstage);
   if (p->tc_err) cudaFree(p->tc_err);
+  if (p->zy_ctl) cudaFree(p->zy_ctl);
   if (p->ev0) cudaEventDestroy(p->ev0);
   if (p->ev1) cudaEventDestroy(p->ev1);
   for (cudaEvent_t e : p->evb)
@@ -1132,7 +1190,15 @@ int accfft_c_set_zy_schedule(accfft_c_plan* p, int mode) {
     p->zy_mode = 1;
     return ACCFFT_C_OK;
   }
-  return fail(ACCFFT_C_EINVAL, "set_zy_schedule: mode must be 0 (separate passes) or 1 (cluster slab kernel)");
+  if (mode == 2) {
+    if (!zy_persistent_available(p->dbl, p->M(), p->n[1]))
+      return fail(ACCFFT_C_EUNSUPPORTED, "set_zy_schedule: no persistent z+y kernel for N1 = %d, N2 = %d",
+                  p->n[1], p->n[2]);
+    p->zy_mode = 3;
+    return ACCFFT_C_OK;
+  }
+  return fail(ACCFFT_C_EINVAL,
+              "set_zy_schedule: mode must be 0 (separate passes), 1 (cluster slab kernel) or 2 (persistent z+y kernel)");
 }
 
 int accfft_c_set_stream(accfft_c_plan* p, void* stream, int blocking) {

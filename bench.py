@@ -108,6 +108,8 @@ def algorithmic_bytes(n, esz):
         "y": 2 * H * c, "y_inv": 2 * H * c,  # natural layout (whole spectrum)
         "x": 2 * H * c, "x_inv": 2 * H * c,
         "zy_slab": N * esz + H * c, "yz_slab": H * c + N * esz,
+        # persistent z+y kernels: both passes' algorithmic bytes
+        "zy_persistent": N * esz + H * c + 2 * H * c, "yz_persistent": 2 * H * c + H * c + N * esz,
     }
 
 
@@ -124,6 +126,7 @@ TRAFFIC = {
 
 KERNEL_OF = {"z_r2c": "k_zr2c", "y": "k_strided (y)", "x": "k_strided (x)", "x_inv": "k_strided (x)",
              "y_inv": "k_strided (y)", "z_c2r": "k_zc2r",
+             "zy_persistent": "k_zy_persistent (z r2c + y)", "yz_persistent": "k_zy_persistent (y + z c2r)",
              "zy_slab": "k_slab_fwd (z+y, cluster)", "yz_slab": "k_slab_inv (y+z, cluster)"}
 
 

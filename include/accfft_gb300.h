@@ -97,7 +97,10 @@ int accfft_c_plan_info(const accfft_c_plan* plan, int n[3], int* kind, int* is_d
                        long long* alloc_max);
 /* extension: how an r2c plan runs its z and y passes: 0 = one kernel per
  * pass over the whole grid (default), 1 = one thread-block-cluster kernel per
- * x-slab doing both (ACCFFT_C_EUNSUPPORTED when the grid has none) */
+ * x-slab doing both, 2 = one persistent kernel whose CTAs take z rows and y
+ * columns slab by slab with per-slab dependency counters, so the second pass
+ * of a slab reads it from L2 (ACCFFT_C_EUNSUPPORTED when the grid has no
+ * such kernel) */
 int accfft_c_set_zy_schedule(accfft_c_plan* plan, int mode);
 /* extension: per-kernel device times.  With profiling on, every kernel the
  * plan launches is bracketed by CUDA events on its stream;

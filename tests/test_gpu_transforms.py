@@ -331,3 +331,26 @@ def test_degenerate_sizes(cuda, native, oracle, n, dtype):
     plan.laplace(lap, du)
     ref = oracle.spectral_op(u.astype(dtype).astype(np.float64), "laplace")
     assert np.abs(from_dev(lap) - ref).max() <= TOL[dtype] * max(1.0, np.abs(ref).max())
+
+
+@pytest.mark.parametrize("n", [(256, 256, 256), (128, 512, 512), (4, 512, 512), (512, 512, 512)])
+def test_persistent_zy_schedule(cuda, native, monkeypatch, n):
+    """ACCFFT_GB300_ZY=persistent: z and y passes in one persistent kernel with
+    per-slab dependency counters; results equal the separate passes' bit for bit."""
+    torch = cuda
+    u = torch.randn(n, device="cuda")
+    ref = native.PlanR2C(n, "float32")
+    monkeypatch.setenv("ACCFFT_GB300_ZY", "persistent")
+    plan = native.PlanR2C(n, "float32")
+    h = (n[0], n[1], n[2] // 2 + 1, 2)
+    a, b = torch.empty(h, device="cuda"), torch.empty(h, device="cuda")
+    ref.r2c(u, a)
+    before = native.kernel_launches()
+    plan.r2c(u, b)
+    assert native.kernel_launches() - before == 2           # z+y, then x
+    assert torch.equal(a, b)
+    ra, rb = torch.empty_like(u), torch.empty_like(u)
+    ref.c2r(a, ra)
+    plan.c2r(b, rb)
+    assert torch.equal(ra, rb)
+    assert torch.allclose(rb / u.numel(), u, atol=1e-5)
