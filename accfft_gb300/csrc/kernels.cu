@@ -80,12 +80,13 @@ bool AFG_NAME(int L, int mode, const StridedArgs& a, cudaStream_t s) {
   }
 }
 #else
-// float z c2r tiles hold half the default lines per CTA (more, smaller CTAs
-// per SM: measured 5 % faster at N2/2 = 256; the r2c pass prefers the default)
+// float z c2r tiles of 256-point (and longer) half lines hold half the
+// default lines per CTA (more, smaller CTAs per SM: measured 5 % faster at
+// N2/2 = 256; the r2c pass prefers the default)
 template <int L>
 constexpr int contig_tl() {
 #if AFG_KIND == 3
-  return sizeof(Real) == 4 && ContigShape<Real, L>::TL >= 2 ? ContigShape<Real, L>::TL / 2 : 0;
+  return sizeof(Real) == 4 && L >= 256 && ContigShape<Real, L>::TL >= 2 ? ContigShape<Real, L>::TL / 2 : 0;
 #else
   return 0;
 #endif

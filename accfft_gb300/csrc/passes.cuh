@@ -64,72 +64,90 @@ __device__ __forceinline__ SymCol sym_column_nyq(const SymArgs& s, long long j) 
 }
 
 // multiply x (frequency p along the pass axis, column part c) by the symbol
-template <typename T, typename V>
-__device__ __forceinline__ V sym_apply(const SymArgs& s, const SymCol& c, int p, V x) {
+// of kind K (a compile-time kind: the element loops that call it are
+// specialised per kind by with_symbol(), so no per-element dispatch remains)
+template <typename T, int K, typename V>
+__device__ __forceinline__ V sym_apply_k(const SymArgs& s, const SymCol& c, int p, V x) {
   const T sc = T(s.scale);
+  if constexpr (K == SYM_LAPLACE) {
+    int wx = fold_wave(p, s.n0);
+    T w = T(-(wx * wx + c.wy * c.wy + c.wz * c.wz)) * sc;
+    return c_scale(x, w);
+  } else if constexpr (K == SYM_BIHARM) {
+    int wx = fold_wave(p, s.n0);
+    T w = T(wx * wx + c.wy * c.wy + c.wz * c.wz);
+    return c_scale(x, w * w * sc);
+  } else if constexpr (K == SYM_INVLAP) {
+    int wx = fold_wave(p, s.n0);
+    int w = -(wx * wx + c.wy * c.wy + c.wz * c.wz);
+    T m = (w == 0) ? T(0) : sc / T(w);
+    return c_scale(x, m);
+  } else if constexpr (K == SYM_INVBIHARM) {
+    int wx = fold_wave_nofilter(p, s.n0);
+    T w = T(wx * wx + c.wy_nf * c.wy_nf + c.wz_nf * c.wz_nf);
+    w = w * w;
+    if (w == T(0)) w = T(1);
+    return c_scale(x, sc / w);
+  } else if constexpr (K == SYM_GRADX || K == SYM_GRADY || K == SYM_GRADZ) {
+    int w = K == SYM_GRADX ? fold_wave(p, s.n0) : (K == SYM_GRADY ? c.wy : c.wz);
+    T m = T(w) * sc;
+    return c_make<V>(-m * x.y, m * x.x);
+  } else if constexpr (K == SYM_DERIV1) {
+    T m = T(fold_wave_line(p, s.axis_len)) * sc;
+    return c_make<V>(-m * x.y, m * x.x);
+  } else if constexpr (K == SYM_DERIV2) {
+    int w = fold_wave_line(p, s.axis_len);
+    return c_scale(x, -T(w * w) * sc);
+  } else if constexpr (K == SYM_HEAT) {
+    int wx = fold_wave(p, s.n0);
+    T k2 = T(wx * wx + c.wy * c.wy + c.wz * c.wz);
+    return c_scale(x, exp(-k2 * T(s.param)) * sc);
+  } else if constexpr (K == SYM_HELMHOLTZ) {
+    int wx = fold_wave(p, s.n0);
+    T d = T(s.param) + T(wx * wx + c.wy * c.wy + c.wz * c.wz);
+    return c_scale(x, d == T(0) ? T(0) : sc / d);
+  } else if constexpr (K == SYM_POISSON_FD) {
+    const int wx = fold_wave_nofilter(p, s.n0);
+    if (wx == 0 && c.wy_nf == 0 && c.wz_nf == 0) return c_make<V>(T(0), T(0));
+    const T* tab = static_cast<const T*>(s.fd_tab);
+    const T d = __ldg(tab + abs(wx)) + __ldg(tab + s.fd_y + abs(c.wy_nf)) + __ldg(tab + s.fd_z + abs(c.wz_nf));
+    return c_scale(x, sc / d);
+  } else if constexpr (K == SYM_POISSON_SPEC) {
+    const int wx = fold_wave_nofilter(p, s.n0);
+    const int k2 = wx * wx + c.wy_nf * c.wy_nf + c.wz_nf * c.wz_nf;
+    if (k2 == 0) return c_make<V>(T(0), T(0));
+    return c_scale(x, sc / (T(-39.4784176043574344753379639995) * T(k2)));   // -4 pi^2 k^2
+  } else {
+    return x;
+  }
+}
+
+template <typename T, int K> struct SymFn {
+  const SymArgs& s;
+  template <typename V>
+  __device__ __forceinline__ V operator()(const SymCol& c, int p, V x) const {
+    return sym_apply_k<T, K>(s, c, p, x);
+  }
+};
+
+// call f(SymFn<T, kind>) once, with the launch's (uniform) symbol kind
+template <typename T, class F>
+__device__ __forceinline__ void with_symbol(const SymArgs& s, F&& f) {
   switch (s.kind) {
-    case SYM_LAPLACE: {
-      int wx = fold_wave(p, s.n0);
-      T w = T(-(wx * wx + c.wy * c.wy + c.wz * c.wz)) * sc;
-      return c_scale(x, w);
-    }
-    case SYM_BIHARM: {
-      int wx = fold_wave(p, s.n0);
-      T w = T(wx * wx + c.wy * c.wy + c.wz * c.wz);
-      return c_scale(x, w * w * sc);
-    }
-    case SYM_INVLAP: {
-      int wx = fold_wave(p, s.n0);
-      int w = -(wx * wx + c.wy * c.wy + c.wz * c.wz);
-      T m = (w == 0) ? T(0) : sc / T(w);
-      return c_scale(x, m);
-    }
-    case SYM_INVBIHARM: {
-      int wx = fold_wave_nofilter(p, s.n0);
-      T w = T(wx * wx + c.wy_nf * c.wy_nf + c.wz_nf * c.wz_nf);
-      w = w * w;
-      if (w == T(0)) w = T(1);
-      return c_scale(x, sc / w);
-    }
-    case SYM_GRADX: case SYM_GRADY: case SYM_GRADZ: {
-      int w = s.kind == SYM_GRADX ? fold_wave(p, s.n0) : (s.kind == SYM_GRADY ? c.wy : c.wz);
-      T m = T(w) * sc;
-      return c_make<V>(-m * x.y, m * x.x);
-    }
-    case SYM_DERIV1: {
-      T m = T(fold_wave_line(p, s.axis_len)) * sc;
-      return c_make<V>(-m * x.y, m * x.x);
-    }
-    case SYM_DERIV2: {
-      int w = fold_wave_line(p, s.axis_len);
-      return c_scale(x, -T(w * w) * sc);
-    }
-    case SYM_HEAT: {
-      int wx = fold_wave(p, s.n0);
-      T k2 = T(wx * wx + c.wy * c.wy + c.wz * c.wz);
-      return c_scale(x, exp(-k2 * T(s.param)) * sc);
-    }
-    case SYM_HELMHOLTZ: {
-      int wx = fold_wave(p, s.n0);
-      T d = T(s.param) + T(wx * wx + c.wy * c.wy + c.wz * c.wz);
-      return c_scale(x, d == T(0) ? T(0) : sc / d);
-    }
-    case SYM_POISSON_FD: {
-      const int wx = fold_wave_nofilter(p, s.n0);
-      if (wx == 0 && c.wy_nf == 0 && c.wz_nf == 0) return c_make<V>(T(0), T(0));
-      const T* tab = static_cast<const T*>(s.fd_tab);
-      const T d = __ldg(tab + abs(wx)) + __ldg(tab + s.fd_y + abs(c.wy_nf)) + __ldg(tab + s.fd_z + abs(c.wz_nf));
-      return c_scale(x, sc / d);
-    }
-    case SYM_POISSON_SPEC: {
-      const int wx = fold_wave_nofilter(p, s.n0);
-      const int k2 = wx * wx + c.wy_nf * c.wy_nf + c.wz_nf * c.wz_nf;
-      if (k2 == 0) return c_make<V>(T(0), T(0));
-      // 4 pi^2
-      return c_scale(x, sc / (T(-39.4784176043574344753379639995) * T(k2)));
-    }
-    default:
-      return x;
+    case SYM_LAPLACE: f(SymFn<T, SYM_LAPLACE>{s}); break;
+    case SYM_BIHARM: f(SymFn<T, SYM_BIHARM>{s}); break;
+    case SYM_INVLAP: f(SymFn<T, SYM_INVLAP>{s}); break;
+    case SYM_INVBIHARM: f(SymFn<T, SYM_INVBIHARM>{s}); break;
+    case SYM_GRADX: f(SymFn<T, SYM_GRADX>{s}); break;
+    case SYM_GRADY: f(SymFn<T, SYM_GRADY>{s}); break;
+    case SYM_GRADZ: f(SymFn<T, SYM_GRADZ>{s}); break;
+    case SYM_DERIV1: f(SymFn<T, SYM_DERIV1>{s}); break;
+    case SYM_DERIV2: f(SymFn<T, SYM_DERIV2>{s}); break;
+    case SYM_HEAT: f(SymFn<T, SYM_HEAT>{s}); break;
+    case SYM_HELMHOLTZ: f(SymFn<T, SYM_HELMHOLTZ>{s}); break;
+    case SYM_POISSON_FD: f(SymFn<T, SYM_POISSON_FD>{s}); break;
+    case SYM_POISSON_SPEC: f(SymFn<T, SYM_POISSON_SPEC>{s}); break;
+    default: f(SymFn<T, SYM_NONE>{s}); break;
   }
 }
 
@@ -165,12 +183,14 @@ template <typename T, int L, int EF = 0, int TLF = 0> struct ContigShape {
 };
 
 // ------------------------------------------------------------------ kernels
-// float tiles of up to 256 threads keep two CTAs per SM (while one CTA
-// computes, the other's loads are in flight); larger or double tiles would
-// spill under that register cap
+// float tiles of 512-point (and longer) lines with up to 256 threads are
+// compiled for two CTAs per SM: the 128-register budget this fixes measured
+// faster than the compiler's own choice there (one CTA's loads in flight
+// while the other computes).  Shorter lines keep the compiler's choice, which
+// leaves room for more CTAs; larger or double tiles would spill.
 template <typename T, int L, int EF, int TCF>
 constexpr int strided_min_blocks() {
-  return (sizeof(T) == 4 && StridedShape<T, L, EF, TCF>::threads <= 256) ? 2 : 1;
+  return (sizeof(T) == 4 && L >= 512 && StridedShape<T, L, EF, TCF>::threads <= 256) ? 2 : 1;
 }
 // One column tile of the strided pass (the body of k_strided; also run by the
 // persistent z+y kernels).  CG loads the input through L2 only.
@@ -263,7 +283,7 @@ __device__ __forceinline__ void strided_tile(const StridedArgs& a, long long til
     // (LineFFT::to_load_order) instead of a shared-memory round trip
     V v[LN::E];
     LN::compute(t, tw, ld, xw, xr, [] {}, v);
-    LN::for_outputs(t, v, [&](int p, V& x) { x = c_conj(sym_apply<T>(a.sym, scol, p, x)); });
+    with_symbol<T>(a.sym, [&](auto sf) { LN::for_outputs(t, v, [&](int p, V& x) { x = c_conj(sf(scol, p, x)); }); });
     LN::to_load_order(v);
     // the inverse's first exchange waits until every thread has read the
     // forward's last one
@@ -432,8 +452,9 @@ k_zc2r(const ContigArgs a) {
   zc2r_tile<T, M, EF, TLF>(a, blockIdx.x);
 }
 
-// real line r2c -> symbol(k) -> c2r, one pass (z-direction derivative);
-// ACC adds the accumulate input a.acc
+// real line r2c -> i k / N -> c2r, one pass (z-direction derivative: the
+// kernel applies SYM_DERIV1 whatever a.sym.kind says); ACC adds the
+// accumulate input a.acc
 template <typename T, int M, int EF = 0, int TLF = 0, bool ACC = false>
 __global__ void __launch_bounds__(ContigShape<T, M, EF, TLF>::threads)
 k_zsym(const ContigArgs a) {
@@ -454,18 +475,18 @@ k_zsym(const ContigArgs a) {
     if (2 * k > M) continue;
     if (k == 0) {
       V z0 = xr(0);
-      V x0 = sym_apply<T>(a.sym, none, 0, c_make<V>(z0.x + z0.y, T(0)));
-      V xn = sym_apply<T>(a.sym, none, M, c_make<V>(z0.x - z0.y, T(0)));
+      V x0 = sym_apply_k<T, SYM_DERIV1>(a.sym, none, 0, c_make<V>(z0.x + z0.y, T(0)));
+      V xn = sym_apply_k<T, SYM_DERIV1>(a.sym, none, M, c_make<V>(z0.x - z0.y, T(0)));
       // imaginary parts of DC and Nyquist are dropped by the real inverse
       xw(0, c_make<V>(x0.x + xn.x, -(x0.x - xn.x)));   // conj(Z'[0])
     } else {
       V zk = xr(k), zm = xr(M - k);
       V wk = __ldg(twp + k), wm = __ldg(twp + (M - k));
-      V xk = sym_apply<T>(a.sym, none, k, r2c_split(zk, zm, wk));
+      V xk = sym_apply_k<T, SYM_DERIV1>(a.sym, none, k, r2c_split(zk, zm, wk));
       if (2 * k == M) {
         xw(k, c_conj(c2r_merge(xk, xk, c_conj(wk))));
       } else {
-        V xm = sym_apply<T>(a.sym, none, M - k, r2c_split(zm, zk, wm));
+        V xm = sym_apply_k<T, SYM_DERIV1>(a.sym, none, M - k, r2c_split(zm, zk, wm));
         xw(k, c_conj(c2r_merge(xk, xm, c_conj(wk))));
         xw(M - k, c_conj(c2r_merge(xm, xk, c_conj(wm))));
       }
