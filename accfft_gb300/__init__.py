@@ -68,6 +68,7 @@ def lib() -> ctypes.CDLL:
         "accfft_c_version": ([], i),
         "accfft_c_length_supported": ([i], i),
         "accfft_c_kernel_launches": ([], ctypes.c_ulonglong),
+        "accfft_c_set_pdl": ([ctypes.c_int], ctypes.c_int),
         "accfft_c_dfft_get_local_size": ([i, i, i, ip, ip, i], ll),
         "accfft_c_local_size_dft_r2c": ([ip, ip, ip, ip, ip, i], ll),
         "accfft_c_local_size_dft_c2c": ([ip, ip, ip, ip, ip, i], ll),
@@ -122,6 +123,14 @@ def last_error() -> str:
 
 def kernel_launches() -> int:
     return int(lib().accfft_c_kernel_launches())
+
+
+def set_pdl(mode: int | None = None) -> int:
+    """Programmatic dependent launch of the pass kernels (each pass waits in
+    hardware for the one before it): 0 off, 1 the next pass is released as
+    this one's CTAs finish (the default), 2 as they start.  ``None`` only
+    queries.  Returns the previous mode."""
+    return int(lib().accfft_c_set_pdl(-1 if mode is None else int(mode)))
 
 
 def _check(rc: int):

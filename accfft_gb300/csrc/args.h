@@ -55,6 +55,7 @@ struct StridedArgs {
   const void* in_nyq;
   void* out_nyq;
   long long nyq_slab, nyq_line;
+  int early_trigger;        // set by the launcher: release the next pass at CTA start
 };
 
 struct ContigArgs {
@@ -74,6 +75,7 @@ struct ContigArgs {
   void* nyq_out;
   const void* nyq_in;
   SymArgs sym;
+  int early_trigger;        // set by the launcher: release the next pass at CTA start
 };
 
 struct SlabArgs {

@@ -1,5 +1,6 @@
 // Length registry and dispatch over the per-translation-unit launchers.
 #include <atomic>
+#include <cstdlib>
 
 #include "launch.h"
 
@@ -7,10 +8,23 @@ namespace afg {
 
 namespace {
 std::atomic<unsigned long long> g_launches{0};
+// -1: not yet read from the environment
+std::atomic<int> g_pdl{-1};
 }
 
 void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 unsigned long long launch_count() { return g_launches.load(std::memory_order_relaxed); }
+
+int pdl_mode() {
+  int v = g_pdl.load(std::memory_order_relaxed);
+  if (v < 0) {
+    const char* e = getenv("ACCFFT_GB300_PDL");
+    v = (e && e[0] >= '0' && e[0] <= '2' && e[1] == 0) ? e[0] - '0' : 1;
+    g_pdl.store(v, std::memory_order_relaxed);
+  }
+  return v;
+}
+void set_pdl(int mode) { g_pdl.store(mode < 0 ? 0 : (mode > 2 ? 2 : mode), std::memory_order_relaxed); }
 
 bool length_supported(int L) {
   switch (L) {

@@ -59,8 +59,9 @@ static void run_strided(const StridedArgs& a, cudaStream_t s) {
   static bool done = false;
   prepare(k, SH::smem, done);
   unsigned grid = unsigned((a.ncols + SH::TC - 1) / SH::TC);
-  k<<<grid, SH::threads, SH::smem, s>>>(a);
-  count_launch();
+  StridedArgs b = a;
+  b.early_trigger = pdl_mode() == 2;
+  launch_pass(k, grid, SH::threads, SH::smem, s, b);
 }
 bool AFG_NAME(int L, int mode, const StridedArgs& a, cudaStream_t s) {
   switch (L) {
@@ -107,8 +108,9 @@ static void run_contig(const ContigArgs& a, cudaStream_t s) {
   static bool done = false;
   prepare(k, SH::smem, done);
   unsigned grid = unsigned((a.nlines + SH::TL - 1) / SH::TL);
-  k<<<grid, SH::threads, SH::smem, s>>>(a);
-  count_launch();
+  ContigArgs b = a;
+  b.early_trigger = pdl_mode() == 2;
+  launch_pass(k, grid, SH::threads, SH::smem, s, b);
 }
 bool AFG_NAME(int L, const ContigArgs& a, cudaStream_t s) {
   switch (L) {

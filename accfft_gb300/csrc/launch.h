@@ -58,4 +58,30 @@ bool launch_zy_persistent(bool dbl, bool forward, int M, int L, const ContigArgs
 unsigned long long launch_count();
 void count_launch();
 
+// Programmatic dependent launch of the pass kernels: 0 off, 1 the next pass
+// is released at the end of each CTA, 2 at its start (PassScope).  Read from
+// ACCFFT_GB300_PDL on first use; set_pdl overrides it for the process.
+int pdl_mode();
+void set_pdl(int mode);
+
+// Launch a pass kernel (one that opens a PassScope) on stream s, with the
+// programmatic-serialisation attribute when PDL is on, and count it.
+template <typename... Params, typename... Args>
+inline cudaError_t launch_pass(void (*kernel)(Params...), unsigned grid, unsigned threads, size_t smem,
+                               cudaStream_t s, Args&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid, 1, 1);
+  cfg.blockDim = dim3(threads, 1, 1);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = pdl_mode() > 0 ? 1 : 0;
+  const cudaError_t e = cudaLaunchKernelEx(&cfg, kernel, static_cast<Args&&>(args)...);
+  count_launch();
+  return e;
+}
+
 }  // namespace afg

@@ -317,9 +317,29 @@ __device__ __forceinline__ void strided_tile(const StridedArgs& a, long long til
   }
 }
 
+// Programmatic dependent launch.  Every pass kernel opens a PassScope before
+// its first global-memory access: griddepcontrol.wait returns once the grid
+// ahead of it in the stream has finished and its writes are visible (at once
+// when the kernel was launched without the programmatic-serialisation
+// attribute).  launch_dependents releases the next pass's launch; it takes
+// effect when every CTA of this grid has executed it or exited.  At the end
+// of the CTA (the default) that hides only the next launch's latency; at CTA
+// start (early) the next pass's CTAs are placed on the SMs this grid's last
+// wave leaves idle and wait there.  Either way the next pass is launched only
+// after every CTA of this grid is resident, so its waiting CTAs never take a
+// slot one of ours still needs, and it reads nothing before the wait.
+struct PassScope {
+  __device__ __forceinline__ explicit PassScope(int early) {
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    if (early) asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+  }
+  __device__ __forceinline__ ~PassScope() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+};
+
 template <typename T, int L, int MODE, int EF = 0, int TCF = 0>
 __global__ void __launch_bounds__(StridedShape<T, L, EF, TCF>::threads, (strided_min_blocks<T, L, EF, TCF>()))
 k_strided(const StridedArgs a) {
+  PassScope scope(a.early_trigger);
   strided_tile<T, L, MODE, EF, TCF>(a, blockIdx.x);
 }
 
@@ -343,6 +363,7 @@ k_strided(const StridedArgs a) {
 template <typename T, int L, int EF = 0, int TLF = 0>
 __global__ void __launch_bounds__(ContigShape<T, L, EF, TLF>::threads)
 k_zc2c(const ContigArgs a) {
+  PassScope scope(a.early_trigger);
   const long long tile = blockIdx.x;
   AFG_CONTIG_PROLOGUE(L)
   const V* in = static_cast<const V*>(a.in) + ls * a.in_dist;
@@ -401,6 +422,7 @@ __device__ __forceinline__ void zr2c_tile(const ContigArgs& a, long long tile) {
 template <typename T, int M, int EF = 0, int TLF = 0>
 __global__ void __launch_bounds__(ContigShape<T, M, EF, TLF>::threads)
 k_zr2c(const ContigArgs a) {
+  PassScope scope(a.early_trigger);
   zr2c_tile<T, M, EF, TLF>(a, blockIdx.x);
 }
 
@@ -449,6 +471,7 @@ __device__ __forceinline__ void zc2r_tile(const ContigArgs& a, long long tile) {
 template <typename T, int M, int EF = 0, int TLF = 0>
 __global__ void __launch_bounds__(ContigShape<T, M, EF, TLF>::threads)
 k_zc2r(const ContigArgs a) {
+  PassScope scope(a.early_trigger);
   zc2r_tile<T, M, EF, TLF>(a, blockIdx.x);
 }
 
@@ -458,6 +481,7 @@ k_zc2r(const ContigArgs a) {
 template <typename T, int M, int EF = 0, int TLF = 0, bool ACC = false>
 __global__ void __launch_bounds__(ContigShape<T, M, EF, TLF>::threads)
 k_zsym(const ContigArgs a) {
+  PassScope scope(a.early_trigger);
   const long long tile = blockIdx.x;
   AFG_CONTIG_PROLOGUE(M)
   const V* in = reinterpret_cast<const V*>(static_cast<const T*>(a.in) + ls * a.in_dist);

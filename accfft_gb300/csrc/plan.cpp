@@ -1097,6 +1097,11 @@ int accfft_c_last_error_code(void) { return g_err_code; }
 int accfft_c_version(void) { return 1; }
 int accfft_c_length_supported(int len) { return length_supported(len) ? 1 : 0; }
 unsigned long long accfft_c_kernel_launches(void) { return launch_count(); }
+int accfft_c_set_pdl(int mode) {
+  const int was = pdl_mode();
+  if (mode >= 0) set_pdl(mode);
+  return was;
+}
 
 long long accfft_c_dfft_get_local_size(int N0, int N1, int tuple, int isize[3], int istart[3], int real_bytes) {
   return local_size(N0, N1, tuple, isize, istart, real_bytes);

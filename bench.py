@@ -4,10 +4,13 @@
 
 A step is one r2c + c2r pair of the 512^3 float32 field through the C ABI
 (accfft_c_execute_r2c_gpuf then accfft_c_execute_c2r_gpuf, device arrays):
-z r2c, y, x passes then x, y, z c2r passes.  The plan's per-kernel profiling
-(accfft_c_set_profiling) brackets every pass with CUDA events on the plan's
-stream, which gives each kernel's mean launch time for the roofline.  Inputs
-(537 MB) exceed the 129 MB L2, so no flush is needed between steps.
+z r2c, y, x passes then x, y, z c2r passes.  Two timed regions of K steps
+each: the first has nothing between the launches (each pass is launched
+while the one before it drains: programmatic dependent launch) and gives the
+value; in the second the plan's per-kernel profiling (accfft_c_set_profiling)
+brackets every pass with CUDA events on the plan's stream, which gives each
+kernel's mean launch time for the roofline.  Inputs (537 MB) exceed the
+129 MB L2, so no flush is needed between steps.
 
 value   pairs/s with the field resident in HBM (max time over ranks)
 e2e     pairs/s through accfft_c_execute_r2c_gpuf / _c2r_gpuf with the field
@@ -414,30 +417,39 @@ def ours(args):
     err = (back / (N0 * N1 * N2) - u).norm().item() / u.norm().item()
     assert err < (1e-5 if dt == "float32" else 1e-12), err
 
-    # the timed region: full r2c + c2r calls; the plan brackets each of its
-    # kernels with CUDA events on the plan's stream
-    plan.set_profiling(True)
-    plan.profile()
+    # timed region 1 (value): K full r2c + c2r calls, nothing between the
+    # kernels, so each pass's launch overlaps the end of the pass before it
+    # (programmatic dependent launch)
+    def timed(profiled):
+        plan.set_profiling(profiled)
+        plan.profile()
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        t0.record(stream)
+        with torch.cuda.stream(stream):
+            for k in range(args.steps):
+                step()
+        t1.record(stream)
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        prof = plan.profile()
+        plan.set_profiling(False)
+        return max_over_ranks(t0.elapsed_time(t1), world), prof
+
     launches0 = ag.kernel_launches()
     clk = Clocks(torch.cuda.current_device()) if rank == 0 else None
-    if world > 1:
-        torch.distributed.barrier()
-    torch.cuda.synchronize()
-    t0 = torch.cuda.Event(enable_timing=True)
-    t1 = torch.cuda.Event(enable_timing=True)
-    t0.record(stream)
-    with torch.cuda.stream(stream):
-        for k in range(args.steps):
-            step()
-    t1.record(stream)
-    torch.cuda.synchronize()
-    if world > 1:
-        torch.distributed.barrier()
-    clocks = clk.stop() if clk else None
+    total_ms, _ = timed(False)
     launches = ag.kernel_launches() - launches0
-    prof = plan.profile()
-    plan.set_profiling(False)
-    total_ms = max_over_ranks(t0.elapsed_time(t1), world)
+    # timed region 2 (roofline): the same K steps with the plan bracketing
+    # each of its kernels with CUDA events on the plan's stream; the events
+    # between launches cost about 40 us per pair and stop the launch overlap,
+    # so this region gives per-kernel durations, not the value
+    prof_total_ms, prof = timed(True)
+    clocks = clk.stop() if clk else None
     ms_step = total_ms / args.steps
     value = replicas_value(args.steps, world, total_ms)
 
@@ -462,6 +474,8 @@ def ours(args):
         "config": {"workload": f"{label} {dt} r2c+c2r round trip", "grid": list(n),
                    "flush": "inputs_larger_than_l2", "parallelism": f"replicas{world}"},
         "gpu_launches": int(launches),
+        "pdl_mode": ag.set_pdl(None),
+        "profiled_ms_per_step": prof_total_ms / args.steps,
         "roofline": {"bound": "hbm", "kernel": KERNEL_OF.get(dom, dom), "pass": dom, "achieved": achieved,
                      "peak": peak, "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": TRAFFIC.get((n, dt), {}).get(dom), "bytes_per_launch": dom_bytes,
@@ -809,6 +823,10 @@ def operators_workload(args):
             "value": res["laplace"]["ms"], "unit": "ms (laplace)", "higher_is_better": False,
             "dtype": "f32" if dt == "float32" else "f64", "peak_GBps": peak, "peak_kind": peak_kind,
             "calls": res, "steps": K,
+            "error_note": ("rel_l2_vs_exact of the symbol operators is the transform's rounding noise times "
+                           "the symbol: |k|^2 (laplace, up to 2e5 at 512^3) and |k|^4 (biharmonic, up to 3.8e10) "
+                           "amplify the round trip's ~1e-7 noise in every mode against an exact field that "
+                           "lives in two low modes; in float32 biharmonic that is O(1) for any FFT"),
             "data": "analytic u = sin x cos 2y sin 3z + 0.5 cos 5x (exact derivatives); c2c: unit-modulus random phases"}
     print(json.dumps(line), flush=True)
 

@@ -68,6 +68,14 @@ int accfft_c_version(void);
 int accfft_c_length_supported(int len);
 /* kernels launched by this process through the library (for audits) */
 unsigned long long accfft_c_kernel_launches(void);
+/* programmatic dependent launch of the pass kernels (each pass waits in
+ * hardware for the pass before it): 0 off; 1 the next pass is released as
+ * this one's CTAs finish (hides the launch latency; the default); 2 it is
+ * released as they start, so its CTAs wait on the SMs this pass's last wave
+ * leaves idle.  ACCFFT_GB300_PDL=0|1|2 in the environment sets the start
+ * value; mode >= 0 sets it for the process, -1 only queries; returns the
+ * previous mode. */
+int accfft_c_set_pdl(int mode);
 
 /* --- local sizes ------------------------------------------------------
  * Replaces dfft_get_local_size_t (src/accfft_common.cpp:49-91),

@@ -96,3 +96,18 @@ def test_null_plan_is_an_error(native):
     assert rc == native.EINVAL
     assert "NULL plan" in native.last_error()
     assert L.accfft_c_laplace(None, None, None, None) == native.EINVAL
+
+
+def test_pdl_switch_queries_and_restores(native):
+    """The launch-overlap switch is process state with query (-1) semantics;
+    no GPU is touched."""
+    prev = native.set_pdl(None)
+    assert prev in (0, 1, 2)
+    try:
+        assert native.set_pdl(0) == prev
+        assert native.set_pdl(None) == 0
+        assert native.set_pdl(2) == 0
+        assert native.set_pdl(9) == 2       # clamped
+        assert native.set_pdl(None) == 2
+    finally:
+        native.set_pdl(prev)

@@ -354,3 +354,62 @@ def test_persistent_zy_schedule(cuda, native, monkeypatch, n):
     plan.c2r(b, rb)
     assert torch.equal(ra, rb)
     assert torch.allclose(rb / u.numel(), u, atol=1e-5)
+
+
+def test_pdl_on_off_bit_identical(cuda, native):
+    """Programmatic dependent launch changes only when a pass's CTAs are
+    scheduled, never what they compute: transforms and fused operators give
+    the same bits with it off and in both release modes, and so does a
+    CUDA-graph capture of a round trip made with it on (the graph keeps the
+    programmatic edges)."""
+    torch = cuda
+    n = (64, 96, 128)
+    h_shape = (n[0], n[1], n[2] // 2 + 1, 2)
+    u = torch.randn(n, device="cuda")
+    prev = native.set_pdl(None)
+    out = {}
+    try:
+        for mode in (0, 1, 2):
+            native.set_pdl(mode)
+            plan = native.PlanR2C(n, "float32")
+            h = torch.empty(h_shape, device="cuda")
+            b, lap = torch.empty_like(u), torch.empty_like(u)
+            gx, gy, gz = (torch.empty_like(u) for _ in range(3))
+            div = torch.empty_like(u)
+            plan.r2c(u, h)
+            plan.c2r(h.clone(), b)
+            plan.laplace(lap, u)
+            plan.grad(gx, gy, gz, u)
+            plan.divergence(div, gx, gy, gz)
+            torch.cuda.synchronize()
+            out[mode] = [h, b, lap, gx, gy, gz, div]
+            plan.destroy()
+        for mode in (1, 2):
+            for x, y in zip(out[0], out[mode]):
+                assert torch.equal(x, y)
+
+        native.set_pdl(2)
+        plan = native.PlanR2C(n, "float32")
+        s = torch.cuda.Stream()
+        plan.set_stream(s)
+        h, b = torch.empty(h_shape, device="cuda"), torch.empty_like(u)
+        torch.cuda.synchronize()
+        with torch.cuda.stream(s):
+            plan.r2c(u, h)
+            plan.c2r(h, b)
+        torch.cuda.synchronize()
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, stream=s, capture_error_mode="relaxed"):
+            plan.r2c(u, h)
+            plan.c2r(h, b)
+        b.zero_()
+        h.zero_()
+        torch.cuda.synchronize()
+        for _ in range(3):
+            g.replay()
+        torch.cuda.synchronize()
+        assert torch.equal(h, out[0][0])
+        assert torch.equal(b, out[0][1])
+        plan.destroy()
+    finally:
+        native.set_pdl(prev)
