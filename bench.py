@@ -320,6 +320,35 @@ def precision_variants(ag, torch, n, u, stream, reps=10):
     return out
 
 
+def link_probe(torch, hu, hb, reps=4):
+    """The host link's rate on this machine, both directions at once (the e2e
+    step's traffic pattern): `reps` plain pinned copies of the field each way
+    on two streams, each direction timed from a common start to its last
+    copy.  The e2e floor per pair is the slower direction's time for one
+    field."""
+    d_in, d_out = torch.empty_like(hu, device="cuda"), torch.empty_like(hu, device="cuda")
+    s1, s2 = torch.cuda.Stream(), torch.cuda.Stream()
+    nbytes = hu.numel() * hu.element_size()
+    rates = None
+    for _ in range(2):   # the first round warms the copy path
+        start = torch.cuda.Event(enable_timing=True)
+        start.record()
+        ends = []
+        for s, (dst, src) in ((s1, (d_in, hu)), (s2, (hb, d_out))):
+            s.wait_event(start)
+            with torch.cuda.stream(s):
+                for _ in range(reps):
+                    dst.copy_(src, non_blocking=True)
+            e = torch.cuda.Event(enable_timing=True)
+            e.record(s)
+            ends.append(e)
+        torch.cuda.synchronize()
+        rates = [reps * nbytes / (start.elapsed_time(e) / 1000.0) / 1e9 for e in ends]
+    del d_in, d_out
+    floor_ms = max(nbytes / (r * 1e9) * 1000.0 for r in rates)
+    return {"h2d_GBps": rates[0], "d2h_GBps": rates[1], "both_directions": True, "floor_ms_per_pair": floor_ms}
+
+
 def e2e_pairs_per_s(args, ag, torch, n, dt, u, stream, world, inflight=3):
     """pairs/s through the public r2c / c2r calls with the real field in pinned
     host memory: every step the r2c reads the field from the host and the c2r
@@ -374,8 +403,10 @@ def e2e_pairs_per_s(args, ag, torch, n, dt, u, stream, world, inflight=3):
     esz = hu.element_size()
     for _, plan, *_ in lanes:
         plan.destroy()
+    link = link_probe(torch, hu, lanes[0][3])
+    link["frac"] = link["floor_ms_per_pair"] / e2e_ms
     return {"value": world * 1000.0 / e2e_ms, "unit": "pairs/s", "h2d_bytes_per_step": int(hu.numel() * esz),
-            "d2h_bytes_per_step": int(hu.numel() * esz), "ms_per_step": e2e_ms,
+            "d2h_bytes_per_step": int(hu.numel() * esz), "ms_per_step": e2e_ms, "link": link,
             "path": f"pinned host field copied in 16 slab batches each way through a device staging ring; "
                     f"{inflight} pairs in flight on {inflight} streams"}
 
