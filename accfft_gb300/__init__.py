@@ -33,6 +33,7 @@ ACCFFT_MEASURE = 2
 # float r2c plans with radix-16 stages on the tensor cores (include/accfft_gb300.h)
 TC_TF32 = 0x100
 TC_BF16 = 0x200
+F64_DF = 0x400       # double plan computing in double-float on the FP32 pipes
 
 OK, EINVAL, EUNSUPPORTED, ECUDA, ENOTBAKED, EOVERFLOW = range(6)
 

@@ -81,8 +81,10 @@ def build(verbose: bool = False, jobs: int | None = None) -> str:
     hdrs = _headers()
     work = []
     ksrc = os.path.join(CSRC, "kernels.cu")
-    for prec in (0, 1):
+    for prec in (0, 1, 2):
         for kind in range(KINDS):
+            if prec == 2 and kind == 4:      # double-float: no symbol kernels
+                continue
             for grp in range(GROUPS):
                 obj = os.path.join(OBJ, f"kernels_p{prec}_k{kind}_g{grp}.o")
                 cmd = [nvcc, *NVCC_FLAGS, f"-DAFG_PREC={prec}", f"-DAFG_KIND={kind}", f"-DAFG_GROUP={grp}",

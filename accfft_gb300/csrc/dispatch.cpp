@@ -38,19 +38,27 @@ bool length_supported(int L) {
   }
 }
 
-bool launch_strided(bool dbl, int L, int mode, const StridedArgs& a, cudaStream_t s) {
-  return dbl ? (launch_strided_f64_g0(L, mode, a, s) || launch_strided_f64_g1(L, mode, a, s))
-             : (launch_strided_f32_g0(L, mode, a, s) || launch_strided_f32_g1(L, mode, a, s));
-}
-#define AFG_DISPATCH(K)                                                              \
-  bool launch_##K(bool dbl, int L, const ContigArgs& a, cudaStream_t s) {           \
-    return dbl ? (launch_##K##_f64_g0(L, a, s) || launch_##K##_f64_g1(L, a, s))     \
-               : (launch_##K##_f32_g0(L, a, s) || launch_##K##_f32_g1(L, a, s));    \
+bool launch_strided(int prec, int L, int mode, const StridedArgs& a, cudaStream_t s) {
+  switch (prec) {
+    case PREC_F32: return launch_strided_f32_g0(L, mode, a, s) || launch_strided_f32_g1(L, mode, a, s);
+    case PREC_F64: return launch_strided_f64_g0(L, mode, a, s) || launch_strided_f64_g1(L, mode, a, s);
+    case PREC_DF: return launch_strided_fdf_g0(L, mode, a, s) || launch_strided_fdf_g1(L, mode, a, s);
+    default: return false;
   }
-AFG_DISPATCH(zc2c)
-AFG_DISPATCH(zr2c)
-AFG_DISPATCH(zc2r)
-AFG_DISPATCH(zsym)
+}
+#define AFG_DISPATCH(K, DF)                                                                  \
+  bool launch_##K(int prec, int L, const ContigArgs& a, cudaStream_t s) {                   \
+    switch (prec) {                                                                          \
+      case PREC_F32: return launch_##K##_f32_g0(L, a, s) || launch_##K##_f32_g1(L, a, s);   \
+      case PREC_F64: return launch_##K##_f64_g0(L, a, s) || launch_##K##_f64_g1(L, a, s);   \
+      case PREC_DF: return DF;                                                               \
+      default: return false;                                                                 \
+    }                                                                                        \
+  }
+AFG_DISPATCH(zc2c, launch_zc2c_fdf_g0(L, a, s) || launch_zc2c_fdf_g1(L, a, s))
+AFG_DISPATCH(zr2c, launch_zr2c_fdf_g0(L, a, s) || launch_zr2c_fdf_g1(L, a, s))
+AFG_DISPATCH(zc2r, launch_zc2r_fdf_g0(L, a, s) || launch_zc2r_fdf_g1(L, a, s))
+AFG_DISPATCH(zsym, false)
 #undef AFG_DISPATCH
 
 }  // namespace afg

@@ -21,14 +21,38 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <type_traits>
+#include "df64.cuh"
 #include "line_plan.h"
 
 namespace afg {
 
 // ---------------------------------------------------------------- complex
+// CT<T>::V is the complex type the arithmetic runs in (registers, shared
+// memory, twiddle tables); Mem<T> the real and complex types of the arrays in
+// global memory.  They differ only for double-float (IEEE double arrays).
 template <typename T> struct CT;
 template <> struct CT<float>  { typedef float2  V; };
 template <> struct CT<double> { typedef double2 V; };
+template <> struct CT<df>     { typedef dfc     V; };
+template <typename T> struct Mem { typedef T R; typedef typename CT<T>::V C; };
+template <> struct Mem<df> { typedef double R; typedef double2 C; };
+
+// array element -> arithmetic type and back (identity but for double-float)
+template <typename T> __device__ __forceinline__ typename CT<T>::V to_reg(typename Mem<T>::C m) { return m; }
+template <> __device__ __forceinline__ dfc to_reg<df>(double2 m) {
+  return dfc{df_from_double(m.x), df_from_double(m.y)};
+}
+template <typename T> __device__ __forceinline__ typename Mem<T>::C to_mem(typename CT<T>::V v) { return v; }
+template <> __device__ __forceinline__ double2 to_mem<df>(dfc v) {
+  return make_double2(df_to_double(v.x), df_to_double(v.y));
+}
+// twiddle-table entry through the read-only path
+__device__ __forceinline__ float2 ld_tw(const float2* p) { return __ldg(p); }
+__device__ __forceinline__ double2 ld_tw(const double2* p) { return __ldg(p); }
+__device__ __forceinline__ dfc ld_tw(const dfc* p) {
+  const float4 f = __ldg(reinterpret_cast<const float4*>(p));
+  return dfc{df_make(f.x, f.y), df_make(f.z, f.w)};
+}
 
 template <typename V> __device__ __forceinline__ V c_add(V a, V b) { V r; r.x = a.x + b.x; r.y = a.y + b.y; return r; }
 template <typename V> __device__ __forceinline__ V c_sub(V a, V b) { V r; r.x = a.x - b.x; r.y = a.y - b.y; return r; }
@@ -249,7 +273,7 @@ template <int R, int S> struct Dft {
 template <typename T, int L, int EF = 0>
 struct LineFFT {
   typedef typename CT<T>::V V;
-  static constexpr LinePlan pl = plan_select(L, std::is_same<T, double>::value, EF);
+  static constexpr LinePlan pl = plan_select(L, std::is_same<T, df>::value ? 2 : (sizeof(T) == 8 ? 1 : 0), EF);
   static constexpr int E = pl.E;
   static constexpr int P = pl.P;
   static constexpr int NS = pl.ns;
@@ -307,7 +331,7 @@ struct LineFFT {
           const int j = t + b * P;
           const int k = j % Ns;
 #pragma unroll
-          for (int r = 1; r < R; ++r) v[b * R + r] = c_mul(v[b * R + r], __ldg(tw + two + (r - 1) * Ns + k));
+          for (int r = 1; r < R; ++r) v[b * R + r] = c_mul(v[b * R + r], ld_tw(tw + two + (r - 1) * Ns + k));
           Dft<R, 1>::run(v + b * R);
         }
       });

@@ -1,7 +1,8 @@
 // One translation unit per (precision, kernel kind, length group): the build
-// compiles this file with -DAFG_PREC=<0|1> -DAFG_KIND=<0..4> -DAFG_GROUP=<0|1>
+// compiles this file with -DAFG_PREC=<0..2> -DAFG_KIND=<0..4> -DAFG_GROUP=<0|1>
 // so the template instantiations spread over parallel nvcc processes.
-//   AFG_PREC 0 = float, 1 = double
+//   AFG_PREC 0 = float, 1 = double, 2 = double-float arithmetic on double
+//            arrays (plain transforms only: kinds 0..3, strided mode 0)
 //   AFG_KIND 0 = strided (MODE 0..4), 1 = zc2c, 2 = zr2c, 3 = zc2r, 4 = zsym (with and without accumulate)
 #include "passes.cuh"
 #include "launch.h"
@@ -13,9 +14,15 @@
 #if AFG_PREC == 0
 typedef float Real;
 #define AFG_P f32
-#else
+#elif AFG_PREC == 1
 typedef double Real;
 #define AFG_P f64
+#else
+typedef afg::df Real;
+#define AFG_P fdf
+#if AFG_KIND == 4
+#error "double-float plans have no symbol kernels"
+#endif
 #endif
 #if AFG_GROUP == 0
 #define AFG_G g0
@@ -64,6 +71,18 @@ static void run_strided(const StridedArgs& a, cudaStream_t s) {
   launch_pass(k, grid, SH::threads, SH::smem, s, b);
 }
 bool AFG_NAME(int L, int mode, const StridedArgs& a, cudaStream_t s) {
+#if AFG_PREC == 2
+  if (mode != 0) return false;
+  switch (L) {
+#define AFG_CASE(n)             \
+  case n:                       \
+    run_strided<n, 0>(a, s);    \
+    return true;
+    AFG_LIST(AFG_CASE)
+#undef AFG_CASE
+    default: return false;
+  }
+#else
   switch (L) {
 #define AFG_CASE(n)                        \
   case n:                                  \
@@ -79,6 +98,7 @@ bool AFG_NAME(int L, int mode, const StridedArgs& a, cudaStream_t s) {
 #undef AFG_CASE
     default: return false;
   }
+#endif
 }
 #else
 // float z c2r tiles of 256-point (and longer) half lines hold half the

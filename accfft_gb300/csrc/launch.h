@@ -29,12 +29,18 @@ AFG_DECL_LAUNCHERS(f32, g0)
 AFG_DECL_LAUNCHERS(f32, g1)
 AFG_DECL_LAUNCHERS(f64, g0)
 AFG_DECL_LAUNCHERS(f64, g1)
+AFG_DECL_LAUNCHERS(fdf, g0)   // double-float: no zsym, strided mode 0 only
+AFG_DECL_LAUNCHERS(fdf, g1)
 
-bool launch_strided(bool dbl, int L, int mode, const StridedArgs& a, cudaStream_t s);
-bool launch_zc2c(bool dbl, int L, const ContigArgs& a, cudaStream_t s);
-bool launch_zr2c(bool dbl, int M, const ContigArgs& a, cudaStream_t s);
-bool launch_zc2r(bool dbl, int M, const ContigArgs& a, cudaStream_t s);
-bool launch_zsym(bool dbl, int M, const ContigArgs& a, cudaStream_t s);
+// arithmetic of a plan's kernels (the arrays are float for PREC_F32, IEEE
+// double for the other two)
+enum Prec { PREC_F32 = 0, PREC_F64 = 1, PREC_DF = 2 };
+
+bool launch_strided(int prec, int L, int mode, const StridedArgs& a, cudaStream_t s);
+bool launch_zc2c(int prec, int L, const ContigArgs& a, cudaStream_t s);
+bool launch_zr2c(int prec, int M, const ContigArgs& a, cudaStream_t s);
+bool launch_zc2r(int prec, int M, const ContigArgs& a, cudaStream_t s);
+bool launch_zsym(int prec, int M, const ContigArgs& a, cudaStream_t s);
 
 // fused z+y slab passes (thread-block clusters); false when the grid has no
 // slab kernel or its cluster cannot be scheduled on this device

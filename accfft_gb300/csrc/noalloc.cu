@@ -177,17 +177,17 @@ extern "C" int accfft_c_laplace_gpuf_noalloc(const int n[3], float* LA, const fl
   x.sym.h2 = (int)H2;
   x.sym.scale = 1.0 / ((double)N0 * N1 * N2);
 
-  bool ok = afg::launch_zr2c(false, M, z, s);
-  ok = ok && afg::launch_strided(false, N1, 0, y, s);
-  ok = ok && afg::launch_strided(false, N0, 1, x, s);
+  bool ok = afg::launch_zr2c(afg::PREC_F32, M, z, s);
+  ok = ok && afg::launch_strided(afg::PREC_F32, N1, 0, y, s);
+  ok = ok && afg::launch_strided(afg::PREC_F32, N0, 1, x, s);
   y.inverse = 1;
-  ok = ok && afg::launch_strided(false, N1, 0, y, s);
+  ok = ok && afg::launch_strided(afg::PREC_F32, N1, 0, y, s);
   afg::ContigArgs zi = z;
   zi.in = spec;
   zi.out = LA;
   zi.in_dist = H2;
   zi.out_dist = N2;
-  ok = ok && afg::launch_zc2r(false, M, zi, s);
+  ok = ok && afg::launch_zc2r(afg::PREC_F32, M, zi, s);
   if (!ok) return err(ACCFFT_C_EUNSUPPORTED, "laplace_gpuf_noalloc: kernel dispatch failed");
   e = cudaGetLastError();
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);

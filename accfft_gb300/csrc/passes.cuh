@@ -188,9 +188,16 @@ template <typename T, int L, int EF = 0, int TLF = 0> struct ContigShape {
 // faster than the compiler's own choice there (one CTA's loads in flight
 // while the other computes).  Shorter lines keep the compiler's choice, which
 // leaves room for more CTAs; larger or double tiles would spill.
+// Double-float tiles with E <= 8 aim at 64 registers a thread (two 512-thread
+// CTAs per SM for 512-point lines: measured 1.34 ms against 1.72 ms for the
+// compiler's 92 registers and one CTA).
 template <typename T, int L, int EF, int TCF>
 constexpr int strided_min_blocks() {
-  return (sizeof(T) == 4 && L >= 512 && StridedShape<T, L, EF, TCF>::threads <= 256) ? 2 : 1;
+  return std::is_same<T, df>::value
+             ? ((LineFFT<T, L, EF>::E <= 8 && StridedShape<T, L, EF, TCF>::threads >= 64)
+                    ? 1024 / StridedShape<T, L, EF, TCF>::threads
+                    : 1)
+             : ((sizeof(T) == 4 && L >= 512 && StridedShape<T, L, EF, TCF>::threads <= 256) ? 2 : 1);
 }
 // One column tile of the strided pass (the body of k_strided; also run by the
 // persistent z+y kernels).  CG loads the input through L2 only.
@@ -198,6 +205,7 @@ template <typename T, int L, int MODE, int EF = 0, int TCF = 0, bool CG = false>
 __device__ __forceinline__ void strided_tile(const StridedArgs& a, long long tile) {
   typedef LineFFT<T, L, EF> LN;
   typedef typename CT<T>::V V;
+  typedef typename Mem<T>::C MC;   // array element (IEEE double for double-float)
   constexpr int TC = StridedShape<T, L, EF, TCF>::TC;
   extern __shared__ __align__(16) unsigned char smraw[];
   V* sm = reinterpret_cast<V*>(smraw);
@@ -208,13 +216,13 @@ __device__ __forceinline__ void strided_tile(const StridedArgs& a, long long til
   const long long gs = valid ? g : 0;          // idle lanes read column 0, store nothing
   long long slab = gs / a.cps;
   long long cc = gs - slab * a.cps;
-  const V* in = static_cast<const V*>(a.in) + slab * a.in_slab + cc;
-  V* out = static_cast<V*>(a.out) + slab * a.out_slab + cc;
+  const MC* in = static_cast<const MC*>(a.in) + slab * a.in_slab + cc;
+  MC* out = static_cast<MC*>(a.out) + slab * a.out_slab + cc;
   long long il = a.in_line, ol = a.out_line;
   if (a.ncols_main > 0 && gs >= a.ncols_main) {   // a Nyquist column of the split layout
     const long long j = gs - a.ncols_main;
-    in = static_cast<const V*>(a.in_nyq) + j * a.nyq_slab;
-    out = static_cast<V*>(a.out_nyq) + j * a.nyq_slab;
+    in = static_cast<const MC*>(a.in_nyq) + j * a.nyq_slab;
+    out = static_cast<MC*>(a.out_nyq) + j * a.nyq_slab;
     il = ol = a.nyq_line;
     slab = j;
     cc = -1;
@@ -226,19 +234,19 @@ __device__ __forceinline__ void strided_tile(const StridedArgs& a, long long til
     const T sg = a.inverse ? T(-1) : T(1);
     auto ld = [&](int p) {
       V x;
-      if constexpr (CG) x = __ldcg(in + p * il);
-      else x = in[p * il];
+      if constexpr (CG) x = to_reg<T>(__ldcg(in + p * il));
+      else x = to_reg<T>(in[p * il]);
       x.y *= sg;
       return x;
     };
-    auto st = [&](int p, V x) { x.y *= sg; if (valid) out[p * ol] = x; };
+    auto st = [&](int p, V x) { x.y *= sg; if (valid) out[p * ol] = to_mem<T>(x); };
     LN::template run<false, false>(t, tw, ld, st, xw, xr);
   } else if constexpr (MODE == 2) {
     // real transform along the line of column pairs (2cc, 2cc+1) packed as
     // u = a + i*b: A[k] = (U[k] + conj U[L-k])/2, B[k] = (U[k] - conj U[L-k])/(2i),
     // written to the half spectrum at complex columns 2cc and 2cc+1
-    V* o2 = static_cast<V*>(a.out) + slab * a.out_slab + 2 * cc;
-    auto ld = [&](int p) { return in[p * il]; };
+    MC* o2 = static_cast<MC*>(a.out) + slab * a.out_slab + 2 * cc;
+    auto ld = [&](int p) { return to_reg<T>(in[p * il]); };
     LN::template run<true, false>(t, tw, ld, xw, xw, xr);
     __syncthreads();
 #pragma unroll
@@ -249,8 +257,8 @@ __device__ __forceinline__ void strided_tile(const StridedArgs& a, long long til
         V A = c_make<V>(T(0.5) * (uk.x + um.x), T(0.5) * (uk.y - um.y));
         V B = c_make<V>(T(0.5) * (uk.y + um.y), T(-0.5) * (uk.x - um.x));
         if (valid) {
-          o2[k * ol] = A;
-          o2[k * ol + 1] = B;
+          o2[k * ol] = to_mem<T>(A);
+          o2[k * ol + 1] = to_mem<T>(B);
         }
       }
     }
@@ -258,12 +266,12 @@ __device__ __forceinline__ void strided_tile(const StridedArgs& a, long long til
     // inverse of MODE 2: U[k] = A[k] + i B[k], U[L-k] = conj A[k] + i conj B[k]
     // (imaginary parts of A, B at k = 0 and k = L/2 dropped), inverse complex
     // FFT, the real pair (a, b) stored at columns (2cc, 2cc+1)
-    const V* i2 = static_cast<const V*>(a.in) + slab * a.in_slab + 2 * cc;
+    const MC* i2 = static_cast<const MC*>(a.in) + slab * a.in_slab + 2 * cc;
 #pragma unroll
     for (int r = 0; r < LN::E; ++r) {
       const int k = t + r * LN::P;
       if (2 * k <= L) {
-        V A = i2[k * il], B = i2[k * il + 1];
+        V A = to_reg<T>(i2[k * il]), B = to_reg<T>(i2[k * il + 1]);
         if (k == 0 || 2 * k == L) { A.y = T(0); B.y = T(0); }
         // conjugated for the forward-engine inverse
         xw(k, c_make<V>(A.x - B.y, -(A.y + B.x)));
@@ -271,13 +279,13 @@ __device__ __forceinline__ void strided_tile(const StridedArgs& a, long long til
       }
     }
     __syncthreads();
-    auto st = [&](int p, V x) { x.y = -x.y; if (valid) out[p * ol] = x; };
+    auto st = [&](int p, V x) { x.y = -x.y; if (valid) out[p * ol] = to_mem<T>(x); };
     LN::template run<false, true>(t, tw, xr, st, xw, xr);
   } else {
     // the symbol sees the column as (y, kz); Nyquist column j of the split
     // layout is (j, N2/2)
     const SymCol scol = cc >= 0 ? sym_column(a.sym, gs) : sym_column_nyq(a.sym, slab);
-    auto ld = [&](int p) { return in[p * il]; };
+    auto ld = [&](int p) { return to_reg<T>(in[p * il]); };
     // forward transform; the symbol is applied in registers and the result
     // conjugated for the inverse run, which starts from the same registers
     // (LineFFT::to_load_order) instead of a shared-memory round trip
@@ -291,13 +299,13 @@ __device__ __forceinline__ void strided_tile(const StridedArgs& a, long long til
     if constexpr (MODE == 1) {
       LN::emit(t, v, [&](int p, V x) {
         x.y = -x.y;
-        if (valid) out[p * ol] = x;
+        if (valid) out[p * ol] = to_mem<T>(x);
       });
     } else {
       // the accumulate input has the output's layout (main columns only);
       // the result is staged in shared memory so that all of this thread's
       // accumulate loads are in flight together
-      const V* acc = static_cast<const V*>(a.acc) + (out - static_cast<V*>(a.out));
+      const MC* acc = static_cast<const MC*>(a.acc) + (out - static_cast<MC*>(a.out));
       if constexpr (LN::NS >= 2) __syncthreads();   // last exchange read before the staging writes
       LN::emit(t, v, [&](int p, V x) { sm[p * TC + c] = c_conj(x); });
       __syncthreads();
@@ -307,11 +315,11 @@ __device__ __forceinline__ void strided_tile(const StridedArgs& a, long long til
         V av[CH];
 #pragma unroll
         for (int j = 0; j < CH; ++j)
-          if (r0 + j < LN::E) av[j] = acc[(t + (r0 + j) * LN::P) * ol];
+          if (r0 + j < LN::E) av[j] = to_reg<T>(acc[(t + (r0 + j) * LN::P) * ol]);
 #pragma unroll
         for (int j = 0; j < CH; ++j)
           if (valid && r0 + j < LN::E)
-            out[(t + (r0 + j) * LN::P) * ol] = c_add(sm[(t + (r0 + j) * LN::P) * TC + c], av[j]);
+            out[(t + (r0 + j) * LN::P) * ol] = to_mem<T>(c_add(sm[(t + (r0 + j) * LN::P) * TC + c], av[j]));
       }
     }
   }
@@ -349,6 +357,8 @@ k_strided(const StridedArgs a) {
   typedef LineFFT<T, L_, EF> LN;                                               \
   typedef ContigShape<T, L_, EF, TLF> SH;                                      \
   typedef typename CT<T>::V V;                                                 \
+  typedef typename Mem<T>::C MC;                                               \
+  typedef typename Mem<T>::R MR;                                               \
   constexpr int P = LN::P, TL = SH::TL;                                        \
   extern __shared__ __align__(16) unsigned char smraw[];                       \
   V* sm = reinterpret_cast<V*>(smraw);                                         \
@@ -366,11 +376,11 @@ k_zc2c(const ContigArgs a) {
   PassScope scope(a.early_trigger);
   const long long tile = blockIdx.x;
   AFG_CONTIG_PROLOGUE(L)
-  const V* in = static_cast<const V*>(a.in) + ls * a.in_dist;
-  V* out = static_cast<V*>(a.out) + ls * a.out_dist;
+  const MC* in = static_cast<const MC*>(a.in) + ls * a.in_dist;
+  MC* out = static_cast<MC*>(a.out) + ls * a.out_dist;
   const T sg = a.inverse ? T(-1) : T(1);
-  auto ld = [&](int p) { V x = in[p]; x.y *= sg; return x; };
-  auto st = [&](int p, V x) { x.y *= sg; if (valid) out[p] = x; };
+  auto ld = [&](int p) { V x = to_reg<T>(in[p]); x.y *= sg; return x; };
+  auto st = [&](int p, V x) { x.y *= sg; if (valid) out[p] = to_mem<T>(x); };
   LN::template run<false, false>(t, static_cast<const V*>(a.tw), ld, st, xw, xr);
 }
 
@@ -394,9 +404,9 @@ __device__ __forceinline__ V c2r_merge(V xk, V xm, V wc) {
 template <typename T, int M, int EF = 0, int TLF = 0>
 __device__ __forceinline__ void zr2c_tile(const ContigArgs& a, long long tile) {
   AFG_CONTIG_PROLOGUE(M)
-  const V* in = reinterpret_cast<const V*>(static_cast<const T*>(a.in) + ls * a.in_dist);
-  V* out = static_cast<V*>(a.out) + ls * a.out_dist;
-  auto ld = [&](int p) { return in[p]; };
+  const MC* in = reinterpret_cast<const MC*>(static_cast<const MR*>(a.in) + ls * a.in_dist);
+  MC* out = static_cast<MC*>(a.out) + ls * a.out_dist;
+  auto ld = [&](int p) { return to_reg<T>(in[p]); };
   LN::template run<true, false>(t, static_cast<const V*>(a.tw), ld, xw, xw, xr);
   __syncthreads();
   const V* twp = static_cast<const V*>(a.tw_post);
@@ -405,16 +415,16 @@ __device__ __forceinline__ void zr2c_tile(const ContigArgs& a, long long tile) {
 #pragma unroll
   for (int r = 0; r < LN::E; ++r) {
     const int k = t + r * P;
-    V x = r2c_split(xr(k), xr(k == 0 ? 0 : M - k), __ldg(twp + k));
+    V x = r2c_split(xr(k), xr(k == 0 ? 0 : M - k), ld_tw(twp + k));
     if (k != 0) x = c_scale(x, wint);
-    if (valid) out[k] = x;
+    if (valid) out[k] = to_mem<T>(x);
   }
   if (t == 0) {
     V z0 = xr(0);
     V xn = c_make<V>(z0.x - z0.y, T(0));
     if (valid) {
-      if (a.nyq_out) static_cast<V*>(a.nyq_out)[ls] = xn;
-      else out[M] = xn;
+      if (a.nyq_out) static_cast<MC*>(a.nyq_out)[ls] = to_mem<T>(xn);
+      else out[M] = to_mem<T>(xn);
     }
   }
 }
@@ -430,8 +440,8 @@ k_zr2c(const ContigArgs a) {
 template <typename T, int M, int EF = 0, int TLF = 0, bool CG = false>
 __device__ __forceinline__ void zc2r_tile(const ContigArgs& a, long long tile) {
   AFG_CONTIG_PROLOGUE(M)
-  const V* in = static_cast<const V*>(a.in) + ls * a.in_dist;
-  V* out = reinterpret_cast<V*>(static_cast<T*>(a.out) + ls * a.out_dist);
+  const MC* in = static_cast<const MC*>(a.in) + ls * a.in_dist;
+  MC* out = reinterpret_cast<MC*>(static_cast<MR*>(a.out) + ls * a.out_dist);
   {
     // stage the M+1 input entries: E independent loads per thread, then the
     // Nyquist entry by thread 0
@@ -439,12 +449,12 @@ __device__ __forceinline__ void zc2r_tile(const ContigArgs& a, long long tile) {
     V nyq;
     if constexpr (CG) {
 #pragma unroll
-      for (int r = 0; r < LN::E; ++r) v[r] = __ldcg(in + t + r * P);
-      nyq = __ldcg(in + (t == 0 ? M : 0));
+      for (int r = 0; r < LN::E; ++r) v[r] = to_reg<T>(__ldcg(in + t + r * P));
+      nyq = to_reg<T>(__ldcg(in + (t == 0 ? M : 0)));
     } else {
 #pragma unroll
-      for (int r = 0; r < LN::E; ++r) v[r] = in[t + r * P];
-      nyq = a.nyq_in ? static_cast<const V*>(a.nyq_in)[ls] : in[t == 0 ? M : 0];
+      for (int r = 0; r < LN::E; ++r) v[r] = to_reg<T>(in[t + r * P]);
+      nyq = to_reg<T>(a.nyq_in ? static_cast<const MC*>(a.nyq_in)[ls] : in[t == 0 ? M : 0]);
     }
 #pragma unroll
     for (int r = 0; r < LN::E; ++r) xw(t + r * P, v[r]);
@@ -462,9 +472,9 @@ __device__ __forceinline__ void zc2r_tile(const ContigArgs& a, long long tile) {
       xk = c_scale(xk, wint);
       xm = c_scale(xm, wint);
     }
-    return c_conj(c2r_merge(xk, xm, c_conj(__ldg(twp + p))));
+    return c_conj(c2r_merge(xk, xm, c_conj(ld_tw(twp + p))));
   };
-  auto st = [&](int p, V x) { x.y = -x.y; if (valid) out[p] = x; };
+  auto st = [&](int p, V x) { x.y = -x.y; if (valid) out[p] = to_mem<T>(x); };
   LN::template run<false, true>(t, static_cast<const V*>(a.tw), ld, st, xw, xr);
 }
 
@@ -484,11 +494,11 @@ k_zsym(const ContigArgs a) {
   PassScope scope(a.early_trigger);
   const long long tile = blockIdx.x;
   AFG_CONTIG_PROLOGUE(M)
-  const V* in = reinterpret_cast<const V*>(static_cast<const T*>(a.in) + ls * a.in_dist);
-  V* out = reinterpret_cast<V*>(static_cast<T*>(a.out) + ls * a.out_dist);
-  const V* acc = ACC ? reinterpret_cast<const V*>(static_cast<const T*>(a.acc) + ls * a.out_dist) : nullptr;
+  const MC* in = reinterpret_cast<const MC*>(static_cast<const MR*>(a.in) + ls * a.in_dist);
+  MC* out = reinterpret_cast<MC*>(static_cast<MR*>(a.out) + ls * a.out_dist);
+  const MC* acc = ACC ? reinterpret_cast<const MC*>(static_cast<const MR*>(a.acc) + ls * a.out_dist) : nullptr;
   const V* tw = static_cast<const V*>(a.tw);
-  auto ld = [&](int p) { return in[p]; };
+  auto ld = [&](int p) { return to_reg<T>(in[p]); };
   LN::template run<true, false>(t, tw, ld, xw, xw, xr);
   __syncthreads();
   const V* twp = static_cast<const V*>(a.tw_post);
@@ -505,7 +515,7 @@ k_zsym(const ContigArgs a) {
       xw(0, c_make<V>(x0.x + xn.x, -(x0.x - xn.x)));   // conj(Z'[0])
     } else {
       V zk = xr(k), zm = xr(M - k);
-      V wk = __ldg(twp + k), wm = __ldg(twp + (M - k));
+      V wk = ld_tw(twp + k), wm = ld_tw(twp + (M - k));
       V xk = sym_apply_k<T, SYM_DERIV1>(a.sym, none, k, r2c_split(zk, zm, wk));
       if (2 * k == M) {
         xw(k, c_conj(c2r_merge(xk, xk, c_conj(wk))));
@@ -520,7 +530,7 @@ k_zsym(const ContigArgs a) {
   if constexpr (!ACC) {
     auto gst = [&](int p, V x) {
       x.y = -x.y;
-      if (valid) out[p] = x;
+      if (valid) out[p] = to_mem<T>(x);
     };
     LN::template run<false, true>(t, tw, xr, gst, xw, xr);
     return;
@@ -537,10 +547,10 @@ k_zsym(const ContigArgs a) {
     V av[CH];
 #pragma unroll
     for (int j = 0; j < CH; ++j)
-      if (r0 + j < LN::E) av[j] = acc[t + (r0 + j) * P];
+      if (r0 + j < LN::E) av[j] = to_reg<T>(acc[t + (r0 + j) * P]);
 #pragma unroll
     for (int j = 0; j < CH; ++j)
-      if (valid && r0 + j < LN::E) out[t + (r0 + j) * P] = c_add(xr(t + (r0 + j) * P), av[j]);
+      if (valid && r0 + j < LN::E) out[t + (r0 + j) * P] = to_mem<T>(c_add(xr(t + (r0 + j) * P), av[j]));
   }
 }
 

@@ -70,8 +70,9 @@ void twiddle(long long m, long long d, long double* c, long double* s) {
 }
 
 // stage twiddles of a line length (layout fixed by plan_tw_offset)
-std::vector<long double> stage_table(int L, bool dbl, int first_radix = 0) {
-  LinePlan pl = plan_select(L, dbl, first_radix);
+// cls: 0 float, 1 double, 2 double-float (line_plan.h plan_select)
+std::vector<long double> stage_table(int L, int cls, int first_radix = 0) {
+  LinePlan pl = plan_select(L, cls, first_radix);
   int n = plan_tw_size(pl);
   std::vector<long double> t(2 * (size_t)(n > 0 ? n : 1), 0.0L);
   for (int s = 1; s < pl.ns; ++s) {
@@ -146,6 +147,8 @@ struct accfft_c_plan {
   // kernels set *tc_err when a completion wait timed out
   int tc = 0;
   int* tc_err = nullptr;
+  // double plan whose kernels compute in double-float (ACCFFT_C_F64_DF)
+  bool df = false;
   // per-kernel CUDA-event profiling (accfft_c_set_profiling)
   bool profile = false;
   std::vector<cudaEvent_t> pev;
@@ -153,6 +156,7 @@ struct accfft_c_plan {
   std::map<std::string, std::pair<long long, double>> pstats;
 
   long long esz() const { return dbl ? 8 : 4; }
+  int prec() const { return dbl ? (df ? PREC_DF : PREC_F64) : PREC_F32; }
   int M() const { return n[2] / 2; }
   long long H2() const { return n[2] / 2 + 1; }
   // row length (reals) of the plan's real arrays
@@ -237,9 +241,14 @@ accfft_c_plan* make_plan(int kind, bool dbl, const int* n, void* data, void* dat
       return nullptr;
     }
   }
+  if ((flags & ACCFFT_C_F64_DF) && !dbl) {
+    fail(ACCFFT_C_EUNSUPPORTED, "plan: ACCFFT_C_F64_DF is a flag of double plans");
+    return nullptr;
+  }
   auto* p = new accfft_c_plan;
   p->kind = kind;
   p->tc = tcf == ACCFFT_C_TC_TF32 ? 1 : tcf == ACCFFT_C_TC_BF16 ? 2 : 0;
+  p->df = (flags & ACCFFT_C_F64_DF) != 0;
   p->dbl = dbl;
   for (int i = 0; i < 3; ++i) p->n[i] = n[i];
   // in place when the plan-time pointers are equal (the reference's rule);
@@ -256,9 +265,10 @@ accfft_c_plan* make_plan(int kind, bool dbl, const int* n, void* data, void* dat
   std::vector<std::vector<long double>> tabs;
   // the tensor-core forms run every line as radix 16 first (16 x 16 x ...)
   const int er = p->tc ? 16 : 0;
-  tabs.push_back(stage_table(n[0], dbl, er));
-  tabs.push_back(stage_table(n[1], dbl, er));
-  tabs.push_back(stage_table(zlen, dbl, er));
+  const int cls = p->df ? 2 : (dbl ? 1 : 0);
+  tabs.push_back(stage_table(n[0], cls, er));
+  tabs.push_back(stage_table(n[1], cls, er));
+  tabs.push_back(stage_table(zlen, cls, er));
   if (kind == 1) tabs.push_back(post_table(n[2] / 2));
   // finite-difference Laplacian eigenvalues D(k) = 2 (cos(2 pi k / N) - 1) N^2
   // for |k| = 0..N/2 of each axis (x, then y, then z; the Poisson solver's
@@ -286,7 +296,14 @@ accfft_c_plan* make_plan(int kind, bool dbl, const int* n, void* data, void* dat
   for (size_t i = 0; i < tabs.size(); ++i) {
     auto& t = tabs[i];
     for (size_t j = 0; j < t.size(); ++j) {
-      if (dbl) {
+      if (p->df) {
+        // double-float entries: the float nearest the value, then the float
+        // nearest the rest
+        const float hi = (float)t[j];
+        const float lo = (float)(t[j] - (long double)hi);
+        memcpy(&host[off[i] + j * 8], &hi, 4);
+        memcpy(&host[off[i] + j * 8 + 4], &lo, 4);
+      } else if (dbl) {
         double v = (double)t[j];
         memcpy(&host[off[i] + j * 8], &v, 8);
       } else {
@@ -420,7 +437,7 @@ struct Exec {
     a.in_line = a.out_line = line;
     a.inverse = inverse;
     if (!timed(tw == p->tw_x ? (inverse ? "x_inv" : "x") : (inverse ? "y_inv" : "y"), p->stream, [&] {
-          return p->tc ? launch_strided_tc(p->tc, L, a, p->tc_err, p->stream) : launch_strided(p->dbl, L, 0, a, p->stream);
+          return p->tc ? launch_strided_tc(p->tc, L, a, p->tc_err, p->stream) : launch_strided(p->prec(), L, 0, a, p->stream);
         }))
       unsupported("strided pass", L);
   }
@@ -438,7 +455,7 @@ struct Exec {
     a.in_line = a.out_line = line;
     a.sym = sym;
     const int mode = acc ? 4 : 1;   // fused pass, with the accumulate input when given
-    if (!timed(label, p->stream, [&] { return launch_strided(p->dbl, L, mode, a, p->stream); }))
+    if (!timed(label, p->stream, [&] { return launch_strided(p->prec(), L, mode, a, p->stream); }))
       unsupported("symbol pass", L);
   }
   // y pass over an [N0][N1][h] complex array, x pass over [N0][N1*h]
@@ -462,7 +479,7 @@ struct Exec {
     a.out_dist = p->H2();
     if (!timed("z_r2c", p->stream, [&] {
           return p->tc ? launch_z_tc(p->tc, true, p->M(), a, p->tc_err, p->stream)
-                       : launch_zr2c(p->dbl, p->M(), a, p->stream);
+                       : launch_zr2c(p->prec(), p->M(), a, p->stream);
         }))
       unsupported("z r2c pass", p->M());
   }
@@ -479,7 +496,7 @@ struct Exec {
     a.out_dist = out_row;
     if (!timed("z_c2r", p->stream, [&] {
           return p->tc ? launch_z_tc(p->tc, false, p->M(), a, p->tc_err, p->stream)
-                       : launch_zc2r(p->dbl, p->M(), a, p->stream);
+                       : launch_zc2r(p->prec(), p->M(), a, p->stream);
         }))
       unsupported("z c2r pass", p->M());
   }
@@ -497,7 +514,7 @@ struct Exec {
     a.nlines = ns * N1;
     a.in_dist = in_row;
     a.out_dist = p->H2();
-    if (!timed("z_r2c", st, [&] { return launch_zr2c(p->dbl, p->M(), a, st); })) unsupported("z r2c pass", p->M());
+    if (!timed("z_r2c", st, [&] { return launch_zr2c(p->prec(), p->M(), a, st); })) unsupported("z r2c pass", p->M());
   }
   void zc2r_slabs(const void* in, void* out, long long out_row, long long s0, long long ns, cudaStream_t st) {
     if (!ok()) return;
@@ -511,7 +528,7 @@ struct Exec {
     a.nlines = ns * N1;
     a.in_dist = p->H2();
     a.out_dist = out_row;
-    if (!timed("z_c2r", st, [&] { return launch_zc2r(p->dbl, p->M(), a, st); })) unsupported("z c2r pass", p->M());
+    if (!timed("z_c2r", st, [&] { return launch_zc2r(p->prec(), p->M(), a, st); })) unsupported("z c2r pass", p->M());
   }
   void ypass_slabs(const void* in, void* out, int inverse, long long s0, long long ns, cudaStream_t st) {
     if (!ok()) return;
@@ -526,7 +543,7 @@ struct Exec {
     a.in_slab = a.out_slab = N1 * h;
     a.in_line = a.out_line = h;
     a.inverse = inverse;
-    if (!timed(inverse ? "y_inv" : "y", st, [&] { return launch_strided(p->dbl, p->n[1], 0, a, st); }))
+    if (!timed(inverse ? "y_inv" : "y", st, [&] { return launch_strided(p->prec(), p->n[1], 0, a, st); }))
       unsupported("strided pass", p->n[1]);
   }
   // z r2c then y forward (forward = true), or y backward then z c2r, over
@@ -707,7 +724,7 @@ struct Exec {
     a.nlines = (long long)p->n[0] * p->n[1];
     a.in_dist = a.out_dist = p->n[2];
     a.inverse = inverse;
-    if (!timed("z_c2c", p->stream, [&] { return launch_zc2c(p->dbl, p->n[2], a, p->stream); }))
+    if (!timed("z_c2c", p->stream, [&] { return launch_zc2c(p->prec(), p->n[2], a, p->stream); }))
       unsupported("z c2c pass", p->n[2]);
   }
   void zsym(const void* in, void* out, const void* acc, long long row, const SymArgs& sym) {
@@ -721,7 +738,7 @@ struct Exec {
     a.nlines = (long long)p->n[0] * p->n[1];
     a.in_dist = a.out_dist = row;
     a.sym = sym;
-    if (!timed("z_deriv", p->stream, [&] { return launch_zsym(p->dbl, p->M(), a, p->stream); }))
+    if (!timed("z_deriv", p->stream, [&] { return launch_zsym(p->prec(), p->M(), a, p->stream); }))
       unsupported("z symbol pass", p->M());
   }
   void slab(bool forward, const void* in, void* out) {
@@ -774,7 +791,7 @@ struct Exec {
     } else {
       a.in_slab = spec_slab; a.in_line = spec_line; a.out_slab = real_slab; a.out_line = real_line;
     }
-    if (!timed(axis == 0 ? "x_real" : "y_real", p->stream, [&] { return launch_strided(p->dbl, L, mode, a, p->stream); }))
+    if (!timed(axis == 0 ? "x_real" : "y_real", p->stream, [&] { return launch_strided(p->prec(), L, mode, a, p->stream); }))
       unsupported("single-axis pass", L);
   }
   // ---- passes through the aligned intermediate layout (p->split)
@@ -794,7 +811,7 @@ struct Exec {
     a.nlines = (long long)p->n[0] * p->n[1];
     a.in_dist = in_row;
     a.out_dist = p->M();
-    if (!timed("z_r2c", p->stream, [&] { return launch_zr2c(p->dbl, p->M(), a, p->stream); }))
+    if (!timed("z_r2c", p->stream, [&] { return launch_zr2c(p->prec(), p->M(), a, p->stream); }))
       unsupported("z r2c pass", p->M());
   }
   void zc2r_split(void* out, long long out_row) {
@@ -809,7 +826,7 @@ struct Exec {
     a.nlines = (long long)p->n[0] * p->n[1];
     a.in_dist = p->M();
     a.out_dist = out_row;
-    if (!timed("z_c2r", p->stream, [&] { return launch_zc2r(p->dbl, p->M(), a, p->stream); }))
+    if (!timed("z_c2r", p->stream, [&] { return launch_zc2r(p->prec(), p->M(), a, p->stream); }))
       unsupported("z c2r pass", p->M());
   }
   // y lines of the main part (aligned columns) and, as extra columns of the
@@ -829,7 +846,7 @@ struct Exec {
     a.nyq_slab = N1;
     a.nyq_line = 1;
     a.inverse = inverse;
-    if (!timed(inverse ? "y_inv" : "y", p->stream, [&] { return launch_strided(p->dbl, (int)N1, 0, a, p->stream); }))
+    if (!timed(inverse ? "y_inv" : "y", p->stream, [&] { return launch_strided(p->prec(), (int)N1, 0, a, p->stream); }))
       unsupported("strided pass", (int)N1);
   }
   // fused x pass of a 3-D operator on the split layout (in place, aligned;
@@ -850,7 +867,7 @@ struct Exec {
     a.nyq_line = N1;
     sym.h2 = (int)M;
     a.sym = sym;
-    if (!timed("x_sym", p->stream, [&] { return launch_strided(p->dbl, p->n[0], 1, a, p->stream); }))
+    if (!timed("x_sym", p->stream, [&] { return launch_strided(p->prec(), p->n[0], 1, a, p->stream); }))
       unsupported("symbol pass", p->n[0]);
   }
   int finish() {
@@ -919,6 +936,9 @@ int check_plan(accfft_c_plan* p, int kind, int dbl, const char* fn) {
     return fail(ACCFFT_C_EINVAL, "%s: precision mismatch (plan is %s)", fn, p->dbl ? "double" : "float");
   if (p->tc && strcmp(fn, "execute_r2c") && strcmp(fn, "execute_c2r") && strcmp(fn, "execute"))
     return fail(ACCFFT_C_EUNSUPPORTED, "%s: tensor-core plans run full r2c / c2r transforms only", fn);
+  if (p->df && strcmp(fn, "execute_r2c") && strcmp(fn, "execute_c2r") && strcmp(fn, "execute") &&
+      strcmp(fn, "execute_c2c"))
+    return fail(ACCFFT_C_EUNSUPPORTED, "%s: double-float plans run r2c, c2r and c2c transforms only", fn);
   return ACCFFT_C_OK;
 }
 

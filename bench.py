@@ -275,14 +275,16 @@ def reference_arm(args):
 
 def precision_variants(ag, torch, n, u, stream, reps=10):
     """The same pairs in the other precision forms: the radix-16 stages on the
-    tensor cores (3xTF32, split BF16) and the FP64 drop-in; pairs/s and the
+    tensor cores (3xTF32, split BF16), the FP64 drop-in, and double plans
+    computing in double-float on the FP32 pipes; pairs/s and the
     forward spectrum's rel-L2 against the FP64 drop-in's (which the tests pin
     to the oracle at 1e-12) on the same float32-rounded input."""
     N0, N1, N2 = n
     u64 = u.double()
     out = {}
     spec64 = None
-    for name, dt, flags in (("fp64_drop_in", "float64", 0), ("fp32_cuda_core", "float32", 0),
+    for name, dt, flags in (("fp64_drop_in", "float64", 0), ("fp64_double_float", "float64", ag.F64_DF),
+                            ("fp32_cuda_core", "float32", 0),
                             ("fp32_tensor_core_3xtf32", "float32", ag.TC_TF32),
                             ("fp32_tensor_core_split_bf16", "float32", ag.TC_BF16)):
         try:
@@ -299,7 +301,7 @@ def precision_variants(ag, torch, n, u, stream, reps=10):
                 plan.r2c(x, spec)
                 plan.c2r(spec, back)
         stream.synchronize()
-        k = 2 if dt == "float64" else reps
+        k = 2 if (dt == "float64" and not flags) else reps
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         a.record(stream)
         with torch.cuda.stream(stream):

@@ -54,6 +54,15 @@ extern "C" {
  * only; x and y lengths 128, 256, 512 or 1024, N2/2 128, 256 or 512. */
 #define ACCFFT_C_TC_TF32 0x100u
 #define ACCFFT_C_TC_BF16 0x200u
+/* Double plans whose kernels compute in double-float: every value a pair
+ * of floats (hi + lo, 48-bit significand) on the FP32 pipes, which on GB300
+ * issue about 70x the operations per cycle of the FP64 pipe.  Arrays stay
+ * IEEE double.  rel-L2 against an exact transform is about 1e-14 instead of
+ * 1e-16; magnitudes must stay within float's exponent range (results below
+ * 2^128, inputs above 2^-126 or flushed to zero).  Such plans run the r2c,
+ * c2r and c2c transforms (any xyz); the single-axis transforms and the
+ * operators stay with plain double plans. */
+#define ACCFFT_C_F64_DF 0x400u
 
 typedef struct accfft_c_plan accfft_c_plan; /* opaque */
 

@@ -111,3 +111,10 @@ def test_pdl_switch_queries_and_restores(native):
         assert native.set_pdl(None) == 2
     finally:
         native.set_pdl(prev)
+
+
+def test_double_float_flag_needs_a_double_plan(native):
+    with pytest.raises(native.AccfftError) as e:
+        native.PlanR2C((8, 8, 8), "float32", flags=native.F64_DF)
+    assert e.value.code == native.EUNSUPPORTED
+    assert "double plans" in str(e.value)

@@ -1,0 +1,113 @@
+"""Double plans computing in double-float (ACCFFT_C_F64_DF): parity with the
+FP64 oracle through the C ABI.
+
+Tolerance: rel-L2 1e-13 against the oracle in double (a 48-bit significand
+through the passes; measured about 1e-14), inside the 1e-12 bar of the
+double drop-in."""
+import numpy as np
+import pytest
+
+from conftest import rng
+from test_gpu_transforms import empty, from_dev, to_dev
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-13
+SHAPES = [(4, 6, 8), (8, 8, 8), (16, 12, 10), (5, 9, 4), (48, 96, 64), (64, 32, 128), (90, 100, 180),
+          (128, 128, 128), (160, 180, 200), (256, 256, 256), (200, 192, 96), (2, 1024, 512)]
+C2C_SHAPES = [(4, 6, 8), (9, 5, 6), (16, 12, 10), (48, 96, 64), (160, 180, 200), (256, 128, 64)]
+
+
+@pytest.mark.parametrize("n", SHAPES)
+def test_df_r2c_c2r(cuda, native, oracle, n):
+    torch = cuda
+    u = rng(30).standard_normal(n)
+    plan = native.PlanR2C(n, "float64", flags=native.F64_DF)
+    du = to_dev(torch, u, "float64")
+    dh = empty(torch, (n[0], n[1], n[2] // 2 + 1, 2), "float64")
+    plan.r2c(du, dh)
+    ref = oracle.r2c(u)
+    assert oracle.rel_l2(from_dev(dh, True), ref) < TOL
+    h = rng(31).standard_normal(ref.shape) + 1j * rng(32).standard_normal(ref.shape)
+    dh2 = to_dev(torch, h, "float64")
+    keep = dh2.clone()
+    db = empty(torch, n, "float64")
+    plan.c2r(dh2, db)
+    assert oracle.rel_l2(from_dev(db), oracle.c2r(h, n[2])) < TOL
+    assert torch.equal(dh2, keep)
+    plan.destroy()
+
+
+@pytest.mark.parametrize("n", C2C_SHAPES)
+def test_df_c2c(cuda, native, oracle, n):
+    torch = cuda
+    a = rng(33).standard_normal(n) + 1j * rng(34).standard_normal(n)
+    plan = native.PlanC2C(n, "float64", flags=native.F64_DF)
+    da = to_dev(torch, a, "float64")
+    out = empty(torch, n + (2,), "float64")
+    plan.c2c(-1, da, out)
+    assert oracle.rel_l2(from_dev(out, True), oracle.c2c(a, -1)) < TOL
+    back = empty(torch, n + (2,), "float64")
+    plan.c2c(1, out, back)
+    assert oracle.rel_l2(from_dev(back, True) / np.prod(n), a) < TOL
+    plan.destroy()
+
+
+@pytest.mark.parametrize("xyz", [1, 2, 3, 4, 5, 6])
+def test_df_partial_axes(cuda, native, oracle, xyz):
+    """xyz bitsets on a double-float plan, against the oracle (with z skipped
+    the remaining passes transform the input array in place, as the
+    reference does)."""
+    torch = cuda
+    n = (16, 12, 20)
+    h = (n[0], n[1], n[2] // 2 + 1)
+    plan = native.PlanR2C(n, "float64", flags=native.F64_DF)
+    if xyz & 4:
+        u = rng(40).standard_normal(n)
+        dh = empty(torch, h + (2,), "float64")
+        plan.r2c(to_dev(torch, u, "float64"), dh, xyz=xyz)
+        got, ref = from_dev(dh, True), oracle.r2c(u, xyz)
+    else:
+        c = rng(41).standard_normal(h) + 1j * rng(42).standard_normal(h)
+        dc = to_dev(torch, c, "float64")
+        plan.r2c(dc, empty(torch, h + (2,), "float64"), xyz=xyz)
+        got, ref = from_dev(dc, True), oracle.r2c(c, xyz)
+    assert oracle.rel_l2(got, ref) < TOL
+    plan.destroy()
+
+
+def test_df_plans_reject_operators_and_float(cuda, native):
+    torch = cuda
+    n = (16, 16, 16)
+    p = native.PlanR2C(n, "float64", flags=native.F64_DF)
+    u = torch.zeros(n, dtype=torch.float64, device="cuda")
+    with pytest.raises(native.AccfftError) as e:
+        p.laplace(torch.empty_like(u), u)
+    assert e.value.code == native.EUNSUPPORTED
+    p.destroy()
+    with pytest.raises(native.AccfftError) as e:
+        native.PlanR2C(n, "float32", flags=native.F64_DF)
+    assert e.value.code == native.EUNSUPPORTED
+
+
+def test_df_512_round_trip(cuda, native):
+    """512^3 in double-float against the plain double plan (the oracle's
+    accuracy at this size is pinned by the double plan's own tests)."""
+    torch = cuda
+    n = (512, 512, 512)
+    g = torch.Generator(device="cuda").manual_seed(36)
+    u = torch.randn(n, dtype=torch.float64, device="cuda", generator=g)
+    h = (n[0], n[1], n[2] // 2 + 1, 2)
+    pd = native.PlanR2C(n, "float64")
+    spec = torch.empty(h, dtype=torch.float64, device="cuda")
+    pd.r2c(u, spec)
+    pf = native.PlanR2C(n, "float64", flags=native.F64_DF)
+    s2 = torch.empty(h, dtype=torch.float64, device="cuda")
+    pf.r2c(u, s2)
+    assert ((s2 - spec).norm() / spec.norm()).item() < TOL
+    del spec
+    back = torch.empty_like(u)
+    pf.c2r(s2, back)
+    assert ((back / u.numel() - u).norm() / u.norm()).item() < TOL
+    pd.destroy()
+    pf.destroy()
