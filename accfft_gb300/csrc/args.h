@@ -56,6 +56,9 @@ struct StridedArgs {
   void* out_nyq;
   long long nyq_slab, nyq_line;
   int early_trigger;        // set by the launcher: release the next pass at CTA start
+  // double-float plans: the largest biased exponent of the transform's input
+  // (the passes scale by an exact power of two around their arithmetic)
+  const int* dfx;
 };
 
 struct ContigArgs {
@@ -76,6 +79,7 @@ struct ContigArgs {
   const void* nyq_in;
   SymArgs sym;
   int early_trigger;        // set by the launcher: release the next pass at CTA start
+  const int* dfx;           // as StridedArgs::dfx
 };
 
 struct SlabArgs {

@@ -65,29 +65,36 @@ __device__ __forceinline__ df& operator*=(df& a, df b) { return a = a * b; }
 __device__ __forceinline__ bool operator==(df a, df b) { return a.hi == b.hi && a.lo == b.lo; }
 
 // ------------------------------------------------------- IEEE double <-> df
+// Both directions scale by an exact power of two: d * 2^k in, v * 2^-k out.
+// A transform picks k so that its input's largest magnitude lands in
+// [1, 2) (df_shift), which keeps every value of the transform inside float's
+// exponent range whatever the data's scale.
+//
 // hi = the double's sign, exponent and top 23 significand bits (truncated),
-// lo = the remaining 29 bits (rounded to 24); values below 2^-126 flush to
-// zero, and lo is dropped below 2^-74 (its weight would be subnormal).
-__device__ __forceinline__ df df_from_double(double d) {
+// lo = the remaining 29 bits (rounded to 24); after scaling, values below
+// 2^-126 flush to zero and lo is dropped below 2^-74 (|value| relative to the
+// input's largest is then below 2^-75: far under the transform's rounding).
+__device__ __forceinline__ df df_from_double(double d, int k) {
   const unsigned long long u = (unsigned long long)__double_as_longlong(d);
   const unsigned hw = unsigned(u >> 32), lw = unsigned(u);
   const unsigned sign = hw & 0x80000000u;
   const int e = int((hw >> 20) & 0x7FFu);
-  const int ef = e - 896;                        // float biased exponent of hi
-  if (ef <= 0) return df_make(__uint_as_float(sign), __uint_as_float(sign));
-  if (ef >= 255) {                               // beyond float range, inf or nan
+  const int ef = e - 896 + k;                    // float biased exponent of hi
+  if (e == 0 || ef <= 0) return df_make(__uint_as_float(sign), __uint_as_float(sign));
+  if (e == 0x7FF || ef >= 255) {                 // inf or nan, or beyond float range
     const bool nan = e == 0x7FF && ((hw & 0xFFFFFu) | lw) != 0;
     return df_make(__uint_as_float(sign | 0x7F800000u | (nan ? 0x400000u : 0u)), 0.0f);
   }
   const float hi = __uint_as_float(sign | (unsigned(ef) << 23) | ((hw & 0xFFFFFu) << 3) | (lw >> 29));
-  const int el = e - 948;                        // float biased exponent of 2^(e - 1075)
+  const int el = e - 948 + k;                    // float biased exponent of 2^(e - 1075 + k)
   float lo = 0.0f;
   if (el > 0) lo = __fmul_rn(__uint2float_rn(lw & 0x1FFFFFFFu), __uint_as_float(unsigned(el) << 23));
   return df_make(hi, sign ? -lo : lo);
 }
 
-// the double nearest hi + lo (ties and the bits below 2^-53 |hi| truncated)
-__device__ __forceinline__ double df_to_double(df v) {
+// the double nearest (hi + lo) * 2^-k (ties and the bits below 2^-53 |hi|
+// truncated; results below the double normal range flush to zero)
+__device__ __forceinline__ double df_to_double(df v, int k) {
   // renormalise so that |lo| <= ulp(hi) / 2 with hi = fl(hi + lo)
   v = df_quick(v.hi, v.lo);
   const unsigned hb = __float_as_uint(v.hi);
@@ -109,7 +116,7 @@ __device__ __forceinline__ double df_to_double(df v) {
     m += lv;
   }
   // |lo| <= ulp(hi)/2 keeps m within [2^52 - 2^28, 2^53 + 2^28]: renormalise one bit
-  int ex = int(eh) - 127 + 1023;
+  int ex = int(eh) - 127 + 1023 - k;
   if (m >= (1ll << 53)) {
     m >>= 1;
     ++ex;
@@ -117,9 +124,15 @@ __device__ __forceinline__ double df_to_double(df v) {
     m <<= 1;
     --ex;
   }
-  const unsigned long long bits = ((unsigned long long)(hb & 0x80000000u) << 32) |
-                                  ((unsigned long long)ex << 52) | ((unsigned long long)m & 0xFFFFFFFFFFFFFull);
+  const unsigned long long s = (unsigned long long)(hb & 0x80000000u) << 32;
+  if (ex <= 0) return __longlong_as_double((long long)s);
+  if (ex >= 0x7FF) return __longlong_as_double((long long)(s | 0x7FF0000000000000ull));
+  const unsigned long long bits = s | ((unsigned long long)ex << 52) | ((unsigned long long)m & 0xFFFFFFFFFFFFFull);
   return __longlong_as_double((long long)bits);
 }
+
+// the scale exponent k of a transform whose input's largest biased double
+// exponent is m (0: all zero or subnormal; 0x7FF: an inf or nan)
+__device__ __forceinline__ int df_shift_of(int m) { return (m <= 0 || m >= 0x7FF) ? 0 : 1023 - m; }
 
 }  // namespace afg

@@ -37,15 +37,19 @@ template <> struct CT<df>     { typedef dfc     V; };
 template <typename T> struct Mem { typedef T R; typedef typename CT<T>::V C; };
 template <> struct Mem<df> { typedef double R; typedef double2 C; };
 
-// array element -> arithmetic type and back (identity but for double-float)
-template <typename T> __device__ __forceinline__ typename CT<T>::V to_reg(typename Mem<T>::C m) { return m; }
-template <> __device__ __forceinline__ dfc to_reg<df>(double2 m) {
-  return dfc{df_from_double(m.x), df_from_double(m.y)};
+// array element -> arithmetic type and back (identity but for double-float,
+// which scales by 2^sh on the way in and 2^-sh on the way out)
+template <typename T> __device__ __forceinline__ typename CT<T>::V to_reg(int, typename Mem<T>::C m) { return m; }
+template <> __device__ __forceinline__ dfc to_reg<df>(int sh, double2 m) {
+  return dfc{df_from_double(m.x, sh), df_from_double(m.y, sh)};
 }
-template <typename T> __device__ __forceinline__ typename Mem<T>::C to_mem(typename CT<T>::V v) { return v; }
-template <> __device__ __forceinline__ double2 to_mem<df>(dfc v) {
-  return make_double2(df_to_double(v.x), df_to_double(v.y));
+template <typename T> __device__ __forceinline__ typename Mem<T>::C to_mem(int, typename CT<T>::V v) { return v; }
+template <> __device__ __forceinline__ double2 to_mem<df>(int sh, dfc v) {
+  return make_double2(df_to_double(v.x, sh), df_to_double(v.y, sh));
 }
+// a pass's scale exponent (double-float: from the transform's input exponent)
+template <typename T> __device__ __forceinline__ int pass_shift(const int*) { return 0; }
+template <> __device__ __forceinline__ int pass_shift<df>(const int* dfx) { return df_shift_of(__ldg(dfx)); }
 // twiddle-table entry through the read-only path
 __device__ __forceinline__ float2 ld_tw(const float2* p) { return __ldg(p); }
 __device__ __forceinline__ double2 ld_tw(const double2* p) { return __ldg(p); }

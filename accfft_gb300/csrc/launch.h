@@ -60,6 +60,10 @@ bool zy_persistent_available(bool dbl, int M, int L);
 bool launch_zy_persistent(bool dbl, bool forward, int M, int L, const ContigArgs& z, const StridedArgs& y,
                           unsigned* ctl, int n0, int lead, cudaStream_t s);
 
+// double-float plans: the largest biased exponent of `rows` rows of `len`
+// doubles, `stride` apart, into *out (zeroed first), on stream s
+bool launch_df_scan(const void* x, long long rows, long long len, long long stride, int* out, cudaStream_t s);
+
 // number of kernel launches issued by this process through the launchers
 unsigned long long launch_count();
 void count_launch();

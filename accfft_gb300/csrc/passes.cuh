@@ -207,6 +207,7 @@ __device__ __forceinline__ void strided_tile(const StridedArgs& a, long long til
   typedef typename CT<T>::V V;
   typedef typename Mem<T>::C MC;   // array element (IEEE double for double-float)
   constexpr int TC = StridedShape<T, L, EF, TCF>::TC;
+  const int sh = pass_shift<T>(a.dfx);
   extern __shared__ __align__(16) unsigned char smraw[];
   V* sm = reinterpret_cast<V*>(smraw);
   const int c = threadIdx.x % TC;
@@ -234,19 +235,19 @@ __device__ __forceinline__ void strided_tile(const StridedArgs& a, long long til
     const T sg = a.inverse ? T(-1) : T(1);
     auto ld = [&](int p) {
       V x;
-      if constexpr (CG) x = to_reg<T>(__ldcg(in + p * il));
-      else x = to_reg<T>(in[p * il]);
+      if constexpr (CG) x = to_reg<T>(sh, __ldcg(in + p * il));
+      else x = to_reg<T>(sh, in[p * il]);
       x.y *= sg;
       return x;
     };
-    auto st = [&](int p, V x) { x.y *= sg; if (valid) out[p * ol] = to_mem<T>(x); };
+    auto st = [&](int p, V x) { x.y *= sg; if (valid) out[p * ol] = to_mem<T>(sh, x); };
     LN::template run<false, false>(t, tw, ld, st, xw, xr);
   } else if constexpr (MODE == 2) {
     // real transform along the line of column pairs (2cc, 2cc+1) packed as
     // u = a + i*b: A[k] = (U[k] + conj U[L-k])/2, B[k] = (U[k] - conj U[L-k])/(2i),
     // written to the half spectrum at complex columns 2cc and 2cc+1
     MC* o2 = static_cast<MC*>(a.out) + slab * a.out_slab + 2 * cc;
-    auto ld = [&](int p) { return to_reg<T>(in[p * il]); };
+    auto ld = [&](int p) { return to_reg<T>(sh, in[p * il]); };
     LN::template run<true, false>(t, tw, ld, xw, xw, xr);
     __syncthreads();
 #pragma unroll
@@ -257,8 +258,8 @@ __device__ __forceinline__ void strided_tile(const StridedArgs& a, long long til
         V A = c_make<V>(T(0.5) * (uk.x + um.x), T(0.5) * (uk.y - um.y));
         V B = c_make<V>(T(0.5) * (uk.y + um.y), T(-0.5) * (uk.x - um.x));
         if (valid) {
-          o2[k * ol] = to_mem<T>(A);
-          o2[k * ol + 1] = to_mem<T>(B);
+          o2[k * ol] = to_mem<T>(sh, A);
+          o2[k * ol + 1] = to_mem<T>(sh, B);
         }
       }
     }
@@ -271,7 +272,7 @@ __device__ __forceinline__ void strided_tile(const StridedArgs& a, long long til
     for (int r = 0; r < LN::E; ++r) {
       const int k = t + r * LN::P;
       if (2 * k <= L) {
-        V A = to_reg<T>(i2[k * il]), B = to_reg<T>(i2[k * il + 1]);
+        V A = to_reg<T>(sh, i2[k * il]), B = to_reg<T>(sh, i2[k * il + 1]);
         if (k == 0 || 2 * k == L) { A.y = T(0); B.y = T(0); }
         // conjugated for the forward-engine inverse
         xw(k, c_make<V>(A.x - B.y, -(A.y + B.x)));
@@ -279,13 +280,13 @@ __device__ __forceinline__ void strided_tile(const StridedArgs& a, long long til
       }
     }
     __syncthreads();
-    auto st = [&](int p, V x) { x.y = -x.y; if (valid) out[p * ol] = to_mem<T>(x); };
+    auto st = [&](int p, V x) { x.y = -x.y; if (valid) out[p * ol] = to_mem<T>(sh, x); };
     LN::template run<false, true>(t, tw, xr, st, xw, xr);
   } else {
     // the symbol sees the column as (y, kz); Nyquist column j of the split
     // layout is (j, N2/2)
     const SymCol scol = cc >= 0 ? sym_column(a.sym, gs) : sym_column_nyq(a.sym, slab);
-    auto ld = [&](int p) { return to_reg<T>(in[p * il]); };
+    auto ld = [&](int p) { return to_reg<T>(sh, in[p * il]); };
     // forward transform; the symbol is applied in registers and the result
     // conjugated for the inverse run, which starts from the same registers
     // (LineFFT::to_load_order) instead of a shared-memory round trip
@@ -299,7 +300,7 @@ __device__ __forceinline__ void strided_tile(const StridedArgs& a, long long til
     if constexpr (MODE == 1) {
       LN::emit(t, v, [&](int p, V x) {
         x.y = -x.y;
-        if (valid) out[p * ol] = to_mem<T>(x);
+        if (valid) out[p * ol] = to_mem<T>(sh, x);
       });
     } else {
       // the accumulate input has the output's layout (main columns only);
@@ -315,11 +316,11 @@ __device__ __forceinline__ void strided_tile(const StridedArgs& a, long long til
         V av[CH];
 #pragma unroll
         for (int j = 0; j < CH; ++j)
-          if (r0 + j < LN::E) av[j] = to_reg<T>(acc[(t + (r0 + j) * LN::P) * ol]);
+          if (r0 + j < LN::E) av[j] = to_reg<T>(sh, acc[(t + (r0 + j) * LN::P) * ol]);
 #pragma unroll
         for (int j = 0; j < CH; ++j)
           if (valid && r0 + j < LN::E)
-            out[(t + (r0 + j) * LN::P) * ol] = to_mem<T>(c_add(sm[(t + (r0 + j) * LN::P) * TC + c], av[j]));
+            out[(t + (r0 + j) * LN::P) * ol] = to_mem<T>(sh, c_add(sm[(t + (r0 + j) * LN::P) * TC + c], av[j]));
       }
     }
   }
@@ -359,6 +360,7 @@ k_strided(const StridedArgs a) {
   typedef typename CT<T>::V V;                                                 \
   typedef typename Mem<T>::C MC;                                               \
   typedef typename Mem<T>::R MR;                                               \
+  const int sh = pass_shift<T>(a.dfx);                                         \
   constexpr int P = LN::P, TL = SH::TL;                                        \
   extern __shared__ __align__(16) unsigned char smraw[];                       \
   V* sm = reinterpret_cast<V*>(smraw);                                         \
@@ -379,8 +381,8 @@ k_zc2c(const ContigArgs a) {
   const MC* in = static_cast<const MC*>(a.in) + ls * a.in_dist;
   MC* out = static_cast<MC*>(a.out) + ls * a.out_dist;
   const T sg = a.inverse ? T(-1) : T(1);
-  auto ld = [&](int p) { V x = to_reg<T>(in[p]); x.y *= sg; return x; };
-  auto st = [&](int p, V x) { x.y *= sg; if (valid) out[p] = to_mem<T>(x); };
+  auto ld = [&](int p) { V x = to_reg<T>(sh, in[p]); x.y *= sg; return x; };
+  auto st = [&](int p, V x) { x.y *= sg; if (valid) out[p] = to_mem<T>(sh, x); };
   LN::template run<false, false>(t, static_cast<const V*>(a.tw), ld, st, xw, xr);
 }
 
@@ -406,7 +408,7 @@ __device__ __forceinline__ void zr2c_tile(const ContigArgs& a, long long tile) {
   AFG_CONTIG_PROLOGUE(M)
   const MC* in = reinterpret_cast<const MC*>(static_cast<const MR*>(a.in) + ls * a.in_dist);
   MC* out = static_cast<MC*>(a.out) + ls * a.out_dist;
-  auto ld = [&](int p) { return to_reg<T>(in[p]); };
+  auto ld = [&](int p) { return to_reg<T>(sh, in[p]); };
   LN::template run<true, false>(t, static_cast<const V*>(a.tw), ld, xw, xw, xr);
   __syncthreads();
   const V* twp = static_cast<const V*>(a.tw_post);
@@ -417,14 +419,14 @@ __device__ __forceinline__ void zr2c_tile(const ContigArgs& a, long long tile) {
     const int k = t + r * P;
     V x = r2c_split(xr(k), xr(k == 0 ? 0 : M - k), ld_tw(twp + k));
     if (k != 0) x = c_scale(x, wint);
-    if (valid) out[k] = to_mem<T>(x);
+    if (valid) out[k] = to_mem<T>(sh, x);
   }
   if (t == 0) {
     V z0 = xr(0);
     V xn = c_make<V>(z0.x - z0.y, T(0));
     if (valid) {
-      if (a.nyq_out) static_cast<MC*>(a.nyq_out)[ls] = to_mem<T>(xn);
-      else out[M] = to_mem<T>(xn);
+      if (a.nyq_out) static_cast<MC*>(a.nyq_out)[ls] = to_mem<T>(sh, xn);
+      else out[M] = to_mem<T>(sh, xn);
     }
   }
 }
@@ -449,12 +451,12 @@ __device__ __forceinline__ void zc2r_tile(const ContigArgs& a, long long tile) {
     V nyq;
     if constexpr (CG) {
 #pragma unroll
-      for (int r = 0; r < LN::E; ++r) v[r] = to_reg<T>(__ldcg(in + t + r * P));
-      nyq = to_reg<T>(__ldcg(in + (t == 0 ? M : 0)));
+      for (int r = 0; r < LN::E; ++r) v[r] = to_reg<T>(sh, __ldcg(in + t + r * P));
+      nyq = to_reg<T>(sh, __ldcg(in + (t == 0 ? M : 0)));
     } else {
 #pragma unroll
-      for (int r = 0; r < LN::E; ++r) v[r] = to_reg<T>(in[t + r * P]);
-      nyq = to_reg<T>(a.nyq_in ? static_cast<const MC*>(a.nyq_in)[ls] : in[t == 0 ? M : 0]);
+      for (int r = 0; r < LN::E; ++r) v[r] = to_reg<T>(sh, in[t + r * P]);
+      nyq = to_reg<T>(sh, a.nyq_in ? static_cast<const MC*>(a.nyq_in)[ls] : in[t == 0 ? M : 0]);
     }
 #pragma unroll
     for (int r = 0; r < LN::E; ++r) xw(t + r * P, v[r]);
@@ -474,7 +476,7 @@ __device__ __forceinline__ void zc2r_tile(const ContigArgs& a, long long tile) {
     }
     return c_conj(c2r_merge(xk, xm, c_conj(ld_tw(twp + p))));
   };
-  auto st = [&](int p, V x) { x.y = -x.y; if (valid) out[p] = to_mem<T>(x); };
+  auto st = [&](int p, V x) { x.y = -x.y; if (valid) out[p] = to_mem<T>(sh, x); };
   LN::template run<false, true>(t, static_cast<const V*>(a.tw), ld, st, xw, xr);
 }
 
@@ -498,7 +500,7 @@ k_zsym(const ContigArgs a) {
   MC* out = reinterpret_cast<MC*>(static_cast<MR*>(a.out) + ls * a.out_dist);
   const MC* acc = ACC ? reinterpret_cast<const MC*>(static_cast<const MR*>(a.acc) + ls * a.out_dist) : nullptr;
   const V* tw = static_cast<const V*>(a.tw);
-  auto ld = [&](int p) { return to_reg<T>(in[p]); };
+  auto ld = [&](int p) { return to_reg<T>(sh, in[p]); };
   LN::template run<true, false>(t, tw, ld, xw, xw, xr);
   __syncthreads();
   const V* twp = static_cast<const V*>(a.tw_post);
@@ -530,7 +532,7 @@ k_zsym(const ContigArgs a) {
   if constexpr (!ACC) {
     auto gst = [&](int p, V x) {
       x.y = -x.y;
-      if (valid) out[p] = to_mem<T>(x);
+      if (valid) out[p] = to_mem<T>(sh, x);
     };
     LN::template run<false, true>(t, tw, xr, gst, xw, xr);
     return;
@@ -547,10 +549,10 @@ k_zsym(const ContigArgs a) {
     V av[CH];
 #pragma unroll
     for (int j = 0; j < CH; ++j)
-      if (r0 + j < LN::E) av[j] = to_reg<T>(acc[t + (r0 + j) * P]);
+      if (r0 + j < LN::E) av[j] = to_reg<T>(sh, acc[t + (r0 + j) * P]);
 #pragma unroll
     for (int j = 0; j < CH; ++j)
-      if (valid && r0 + j < LN::E) out[t + (r0 + j) * P] = to_mem<T>(c_add(xr(t + (r0 + j) * P), av[j]));
+      if (valid && r0 + j < LN::E) out[t + (r0 + j) * P] = to_mem<T>(sh, c_add(xr(t + (r0 + j) * P), av[j]));
   }
 }
 

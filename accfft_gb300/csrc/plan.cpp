@@ -147,8 +147,10 @@ struct accfft_c_plan {
   // kernels set *tc_err when a completion wait timed out
   int tc = 0;
   int* tc_err = nullptr;
-  // double plan whose kernels compute in double-float (ACCFFT_C_F64_DF)
+  // double plan whose kernels compute in double-float (ACCFFT_C_F64_DF);
+  // df_exp receives the largest biased exponent of each transform's input
   bool df = false;
+  int* df_exp = nullptr;
   // per-kernel CUDA-event profiling (accfft_c_set_profiling)
   bool profile = false;
   std::vector<cudaEvent_t> pev;
@@ -316,6 +318,7 @@ accfft_c_plan* make_plan(int kind, bool dbl, const int* n, void* data, void* dat
   if (e == cudaSuccess) e = cudaMemcpy(p->tw_block, host.data(), total, cudaMemcpyHostToDevice);
   if (e == cudaSuccess && kind == 1) e = cudaMalloc(&p->scratch, (size_t)p->alloc_max);
   if (e == cudaSuccess && p->tc) e = cudaMalloc(&p->tc_err, sizeof(int));
+  if (e == cudaSuccess && p->df) e = cudaMalloc(&p->df_exp, 16);
   if (e == cudaSuccess && p->tc) e = cudaMemset(p->tc_err, 0, sizeof(int));
   if (e == cudaSuccess) e = cudaEventCreate(&p->ev0);
   if (e == cudaSuccess) e = cudaEventCreate(&p->ev1);
@@ -389,6 +392,13 @@ struct Exec {
     if (p->blocking || timer) cudaEventRecord(p->ev0, p->stream);
   }
   bool ok() const { return rc == ACCFFT_C_OK; }
+  // double-float plans: the largest exponent of the transform's input (rows
+  // of len doubles, stride apart), read by every pass of the transform
+  void df_scan(const void* x, long long rows, long long len, long long stride) {
+    if (!ok() || !p->df) return;
+    if (!timed("df_scan", p->stream, [&] { return launch_df_scan(x, rows, len, stride, p->df_exp, p->stream); }))
+      rc = fail(ACCFFT_C_ECUDA, "double-float input scan: launch failed");
+  }
   // run one launcher; with profiling on, bracket it with CUDA events on its stream
   template <class F>
   bool timed(const char* label, cudaStream_t st, F&& launch) {
@@ -428,6 +438,7 @@ struct Exec {
                long long line, int inverse) {
     if (!ok()) return;
     StridedArgs a{};
+    a.dfx = p->df_exp;
     a.in = in;
     a.out = out;
     a.tw = tw;
@@ -445,6 +456,7 @@ struct Exec {
                    long long slab, long long line, const SymArgs& sym, const char* label) {
     if (!ok()) return;
     StridedArgs a{};
+    a.dfx = p->df_exp;
     a.in = in;
     a.out = out;
     a.acc = acc;
@@ -469,6 +481,7 @@ struct Exec {
   void zr2c(const void* in, void* out, long long in_row) {
     if (!ok()) return;
     ContigArgs a{};
+    a.dfx = p->df_exp;
     a.weight = weight;
     a.in = in;
     a.out = out;
@@ -486,6 +499,7 @@ struct Exec {
   void zc2r(const void* in, void* out, long long out_row) {
     if (!ok()) return;
     ContigArgs a{};
+    a.dfx = p->df_exp;
     a.weight = weight;
     a.in = in;
     a.out = out;
@@ -506,6 +520,7 @@ struct Exec {
     if (!ok()) return;
     const long long N1 = p->n[1];
     ContigArgs a{};
+    a.dfx = p->df_exp;
     a.weight = weight;
     a.in = in;
     a.out = static_cast<char*>(out) + s0 * N1 * p->H2() * 2 * p->esz();
@@ -520,6 +535,7 @@ struct Exec {
     if (!ok()) return;
     const long long N1 = p->n[1];
     ContigArgs a{};
+    a.dfx = p->df_exp;
     a.weight = weight;
     a.in = static_cast<const char*>(in) + s0 * N1 * p->H2() * 2 * p->esz();
     a.out = out;
@@ -535,6 +551,7 @@ struct Exec {
     const long long N1 = p->n[1], h = p->H2();
     const long long off = s0 * N1 * h * 2 * p->esz();
     StridedArgs a{};
+    a.dfx = p->df_exp;
     a.in = static_cast<const char*>(in) + off;
     a.out = static_cast<char*>(out) + off;
     a.tw = p->tw_y;
@@ -604,9 +621,11 @@ struct Exec {
       return;
     }
     ContigArgs z{};
+    z.dfx = p->df_exp;
     z.tw = p->tw_z;
     z.tw_post = p->tw_post;
     StridedArgs y{};
+    y.dfx = p->df_exp;
     y.tw = p->tw_y;
     y.in_line = y.out_line = H;
     if (forward) {
@@ -718,6 +737,7 @@ struct Exec {
   void zc2c(const void* in, void* out, int inverse) {
     if (!ok()) return;
     ContigArgs a{};
+    a.dfx = p->df_exp;
     a.in = in;
     a.out = out;
     a.tw = p->tw_z;
@@ -730,6 +750,7 @@ struct Exec {
   void zsym(const void* in, void* out, const void* acc, long long row, const SymArgs& sym) {
     if (!ok()) return;
     ContigArgs a{};
+    a.dfx = p->df_exp;
     a.in = in;
     a.out = out;
     a.acc = acc;
@@ -764,6 +785,7 @@ struct Exec {
     const long long N0 = p->n[0], N1 = p->n[1], N2 = p->n[2];
     const long long pr = N2 / 2;   // complex pairs per real row
     StridedArgs a{};
+    a.dfx = p->df_exp;
     a.in = in;
     a.out = out;
     int L;
@@ -802,6 +824,7 @@ struct Exec {
   void zr2c_split(const void* in, long long in_row) {
     if (!ok()) return;
     ContigArgs a{};
+    a.dfx = p->df_exp;
     a.in = in;
     a.out = main_buf();
     a.nyq_out = nyq_buf();
@@ -817,6 +840,7 @@ struct Exec {
   void zc2r_split(void* out, long long out_row) {
     if (!ok()) return;
     ContigArgs a{};
+    a.dfx = p->df_exp;
     a.in = main_buf();
     a.nyq_in = nyq_buf();
     a.out = out;
@@ -835,6 +859,7 @@ struct Exec {
     if (!ok()) return;
     const long long N0 = p->n[0], N1 = p->n[1], M = p->M();
     StridedArgs a{};
+    a.dfx = p->df_exp;
     a.in = a.out = main_buf();
     a.tw = p->tw_y;
     a.ncols_main = N0 * M;
@@ -855,6 +880,7 @@ struct Exec {
     if (!ok()) return;
     const long long N1 = p->n[1], M = p->M();
     StridedArgs a{};
+    a.dfx = p->df_exp;
     a.in = a.out = main_buf();
     a.tw = p->tw_x;
     a.ncols_main = N1 * M;
@@ -970,8 +996,13 @@ int exec_r2c_plan(accfft_c_plan* p, int direction, void* in, void* out, double* 
     }
     return ex.finish();
   }
+  if (p->df && (host_in || host_out))
+    return fail(ACCFFT_C_EUNSUPPORTED, "execute: double-float plans take device arrays");
   Exec ex(p, timer);
   ex.weight = weight;
+  const long long spec_doubles = 2LL * p->n[0] * p->n[1] * h;
+  if (direction == -1 && (xyz & ZB)) ex.df_scan(in, (long long)p->n[0] * p->n[1], p->n[2], p->rrow());
+  else ex.df_scan(in, 1, spec_doubles, spec_doubles);
   if (direction == -1) {
     void* work = in;   // with z skipped the reference transforms the input in place
     if ((xyz & ZB) && (xyz & YB)) {
@@ -1023,6 +1054,8 @@ int exec_c2c_plan(accfft_c_plan* p, int direction, void* in, void* out, double* 
   const int inv = direction == 1;
   const long long h = p->n[2];
   Exec ex(p, timer);
+  const long long cdoubles = 2LL * p->n[0] * p->n[1] * p->n[2];
+  ex.df_scan(in, 1, cdoubles, cdoubles);
   // the axes are independent, so the backward transform also starts with z
   // (in -> out) and never writes its input
   void* work = in;
@@ -1156,6 +1189,7 @@ void accfft_c_destroy_plan(accfft_c_plan* p) {
   if (p->hstage) cudaFree(p->hstage);
   if (p->tc_err) cudaFree(p->tc_err);
   if (p->zy_ctl) cudaFree(p->zy_ctl);
+  if (p->df_exp) cudaFree(p->df_exp);
   if (p->ev0) cudaEventDestroy(p->ev0);
   if (p->ev1) cudaEventDestroy(p->ev1);
   for (cudaEvent_t e : p->evb)

@@ -111,3 +111,60 @@ def test_df_512_round_trip(cuda, native):
     assert ((back / u.numel() - u).norm() / u.norm()).item() < TOL
     pd.destroy()
     pf.destroy()
+
+
+@pytest.mark.parametrize("scale_exp", [-900, -400, -60, 60, 400, 900])
+def test_df_scale_invariance(cuda, native, scale_exp):
+    """Each transform scales by the exact power of two that puts its input's
+    largest magnitude in [1, 2): data far outside float's exponent range
+    transforms to the same bits times the same power of two."""
+    torch = cuda
+    n = (32, 24, 40)
+    u = torch.from_numpy(rng(37).standard_normal(n)).cuda()
+    f = 2.0 ** scale_exp
+    plan = native.PlanR2C(n, "float64", flags=native.F64_DF)
+    h = (n[0], n[1], n[2] // 2 + 1, 2)
+    a, b = torch.empty(h, dtype=torch.float64, device="cuda"), torch.empty(h, dtype=torch.float64, device="cuda")
+    plan.r2c(u, a)
+    plan.r2c(u * f, b)
+    assert torch.equal(b, a * f)
+    ra, rb = torch.empty_like(u), torch.empty_like(u)
+    plan.c2r(a, ra)
+    plan.c2r(b, rb)
+    assert torch.equal(rb, ra * f)
+    c = torch.from_numpy(rng(38).standard_normal(n + (2,))).cuda()
+    pc = native.PlanC2C(n, "float64", flags=native.F64_DF)
+    ca, cb = torch.empty_like(c), torch.empty_like(c)
+    pc.c2c(-1, c, ca)
+    pc.c2c(-1, c * f, cb)
+    assert torch.equal(cb, ca * f)
+    plan.destroy()
+    pc.destroy()
+
+
+def test_df_wide_dynamic_range(cuda, native, oracle):
+    """Entries spanning 2^-300 .. 2^300 in one field: normwise accuracy is
+    set by the largest ones, as in IEEE double."""
+    torch = cuda
+    n = (16, 20, 24)
+    r = rng(39)
+    u = r.standard_normal(n) * np.exp2(r.integers(-300, 300, size=n))
+    plan = native.PlanR2C(n, "float64", flags=native.F64_DF)
+    dh = empty(torch, (n[0], n[1], n[2] // 2 + 1, 2), "float64")
+    plan.r2c(to_dev(torch, u, "float64"), dh)
+    assert oracle.rel_l2(from_dev(dh, True), oracle.r2c(u)) < TOL
+    z = torch.zeros(n, dtype=torch.float64, device="cuda")
+    plan.r2c(z, dh)
+    assert not dh.any()
+    plan.destroy()
+
+
+def test_df_plans_reject_host_arrays(cuda, native):
+    torch = cuda
+    n = (8, 8, 8)
+    plan = native.PlanR2C(n, "float64", flags=native.F64_DF)
+    hu = torch.zeros(n, dtype=torch.float64).pin_memory()
+    with pytest.raises(native.AccfftError) as e:
+        plan.r2c(hu, torch.empty((8, 8, 5, 2), dtype=torch.float64, device="cuda"))
+    assert e.value.code == native.EUNSUPPORTED
+    plan.destroy()
