@@ -544,9 +544,10 @@ def precision_workload(args):
     """1024^3 real field from a turbulence-like random Fourier series
     (amplitude N(0,1)|k|^-5/3 for 0 < |k| <= 256, uniform phases), rounded to
     float32; r2c + c2r in float32 with CUDA-core radix stages, with the
-    radix-16 stages on the tensor cores (3xTF32 and split BF16), and with the
-    FP64 drop-in, each result against the oracle (double, host cores) applied
-    to the same input."""
+    radix-16 stages on the tensor cores (3xTF32 and split BF16), with the
+    FP64 drop-in, and with double plans computing in double-float, each
+    result against the oracle (double, host cores) applied to the same
+    input."""
     import torch
 
     import accfft_gb300 as ag
@@ -579,7 +580,8 @@ def precision_workload(args):
     ref_spec = orc.r2c(host_u)
     oracle_s = time.perf_counter() - t0
     variants = (("fp32_cuda_core", "float32", 0), ("fp32_tensor_core_3xtf32", "float32", ag.TC_TF32),
-                ("fp32_tensor_core_split_bf16", "float32", ag.TC_BF16), ("fp64_drop_in", "float64", 0))
+                ("fp32_tensor_core_split_bf16", "float32", ag.TC_BF16), ("fp64_drop_in", "float64", 0),
+                ("fp64_double_float", "float64", ag.F64_DF))
     for name, dt, flags in variants:
         try:
             plan = ag.PlanR2C(n, dt, flags=flags) if flags else ag.PlanR2C(n, dt)
@@ -596,7 +598,7 @@ def precision_workload(args):
         e_fwd = orc.rel_l2(s[..., 0] + 1j * s[..., 1], ref_spec)
         e_rt = ((back.double() / N - uq).norm() / uq.norm()).item()
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        reps = 5 if dt == "float32" else 2
+        reps = 5 if (dt == "float32" or flags) else 2
         a.record()
         for _ in range(reps):
             plan.r2c(x, spec)
