@@ -26,7 +26,7 @@ struct df {
   float hi, lo;
   __host__ __device__ constexpr df() : hi(0.0f), lo(0.0f) {}
   // compile-time constants only: a run-time use would convert on the FP64 pipe
-  __host__ __device__ constexpr df(double d) : hi(float(d)), lo(float(d - double(float(d)))) {}
+  __host__ __device__ explicit constexpr df(double d) : hi(float(d)), lo(float(d - double(float(d)))) {}
   __host__ __device__ constexpr df(float h, float l, int) : hi(h), lo(l) {}
 };
 struct dfc {
