@@ -712,8 +712,6 @@ struct Exec {
     cudaStreamSynchronize(p->stream);
     cudaStreamSynchronize(p->stream2);
     if (p->hstage) cudaFree(p->hstage);
-  if (p->tc_err) cudaFree(p->tc_err);
-  if (p->zy_ctl) cudaFree(p->zy_ctl);
     p->hstage = nullptr;
     p->hstage_bytes = 0;
     cudaError_t e = cudaMalloc(&p->hstage, (size_t)need);

@@ -413,3 +413,26 @@ def test_pdl_on_off_bit_identical(cuda, native):
         plan.destroy()
     finally:
         native.set_pdl(prev)
+
+
+def test_host_staging_keeps_persistent_control_words(cuda, native, monkeypatch):
+    """The staging ring for host arrays is allocated on a plan's first host
+    call without releasing the plan's other device words: a persistent-
+    schedule plan still matches the separate passes after a host call."""
+    torch = cuda
+    n = (64, 256, 256)
+    h = (n[0], n[1], n[2] // 2 + 1, 2)
+    ref = native.PlanR2C(n, "float32")
+    monkeypatch.setenv("ACCFFT_GB300_ZY", "persistent")
+    plan = native.PlanR2C(n, "float32")
+    u = torch.randn(n, device="cuda")
+    a, b, c = (torch.empty(h, device="cuda") for _ in range(3))
+    ref.r2c(u, a)
+    plan.r2c(u.cpu().pin_memory(), b)        # host input: staged through the ring
+    torch.cuda.synchronize()
+    plan.r2c(u, c)                           # device input: persistent z+y kernel
+    torch.cuda.synchronize()
+    assert torch.allclose(b, a, rtol=0, atol=1e-3 * a.abs().max().item())
+    assert torch.equal(c, a)
+    plan.destroy()
+    ref.destroy()
