@@ -132,6 +132,11 @@ struct accfft_c_plan {
   int zy_lead = 32;   // slabs between a slab's first and second pass (ACCFFT_GB300_ZY_LEAD)
   // pinned-host real arrays: slab batches staged through a device ring
   static constexpr int kHostBatches = 16, kHostSlots = 3;
+  // slab batches per call (ACCFFT_GB300_HOST_BATCHES, 1..16).  Four measured
+  // best at 512^3 with three calls in flight: 98.8 % of the host link's
+  // duplex floor against 93 % for 16, whose ~230 API calls per r2c+c2r pair
+  // left the enqueue thread behind on a busy host
+  int host_batches = 4;
   void* hstage = nullptr;
   long long hstage_bytes = 0;
   static_assert(1 + kHostBatches + kHostSlots <= kMaxBatches + 1, "host path events fit evb");
@@ -342,6 +347,10 @@ accfft_c_plan* make_plan(int kind, bool dbl, const int* n, void* data, void* dat
     // complex are 128-byte aligned (M a multiple of 16 for float, 8 for double)
     const int M = n[2] / 2;
     p->split = M >= 8 && M % (dbl ? 8 : 16) == 0;
+    if (const char* hb = getenv("ACCFFT_GB300_HOST_BATCHES")) {
+      const int v = atoi(hb);
+      p->host_batches = v < 1 ? 1 : (v > accfft_c_plan::kHostBatches ? accfft_c_plan::kHostBatches : v);
+    }
     // ACCFFT_GB300_ZY = fused | batch<n> selects an alternative z+y schedule
     // for device-resident data (both measured slower on GB300 than the
     // default whole-grid passes; kept for comparison)
@@ -668,7 +677,7 @@ struct Exec {
   void zy_host(bool forward, const void* in, void* mid, void* out, long long row) {
     if (!ok()) return;
     const long long N0 = p->n[0], N1 = p->n[1];
-    const int nb = (int)std::min<long long>(N0, accfft_c_plan::kHostBatches);
+    const int nb = (int)std::min<long long>(N0, p->host_batches);
     const long long slab_rows = (N0 + nb - 1) / nb;                 // largest batch, in slabs
     const long long slot_bytes = slab_rows * N1 * row * p->esz();
     if (!ensure_stage(slot_bytes)) return;

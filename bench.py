@@ -393,7 +393,9 @@ def e2e_pairs_per_s(args, ag, torch, n, dt, u, stream, world, inflight=3):
     if world > 1:
         torch.distributed.barrier()
     e0.record(stream)
+    t_enq = time.perf_counter()
     run(ksteps)
+    enqueue_ms = (time.perf_counter() - t_enq) * 1000.0 / ksteps   # host time to issue one pair
     e1.record(stream)
     stream.synchronize()
     if world > 1:
@@ -409,7 +411,8 @@ def e2e_pairs_per_s(args, ag, torch, n, dt, u, stream, world, inflight=3):
     link["frac"] = link["floor_ms_per_pair"] / e2e_ms
     return {"value": world * 1000.0 / e2e_ms, "unit": "pairs/s", "h2d_bytes_per_step": int(hu.numel() * esz),
             "d2h_bytes_per_step": int(hu.numel() * esz), "ms_per_step": e2e_ms, "link": link,
-            "path": f"pinned host field copied in 16 slab batches each way through a device staging ring; "
+            "host_enqueue_ms_per_step": enqueue_ms,
+            "path": f"pinned host field copied in 4 slab batches each way through a device staging ring; "
                     f"{inflight} pairs in flight on {inflight} streams"}
 
 

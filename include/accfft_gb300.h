@@ -25,7 +25,7 @@
  *   - Arrays may be device memory or pinned host memory (cudaHostAlloc /
  *     cudaHostRegister); other host memory is rejected with ACCFFT_C_EINVAL.
  *     When an r2c input or a c2r output is pinned host memory, the plan
- *     moves it with the copy engines in 16 slab batches through a ring of
+ *     moves it with the copy engines in 4 slab batches through a ring of
  *     three device staging slots, overlapped with the z and y kernels of the
  *     batches already staged; other arrays in host memory are reached by the
  *     kernels over the host link.
