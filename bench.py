@@ -60,6 +60,8 @@ def parse():
     ap.add_argument("--call", default="r2c", choices=["r2c", "c2r", "laplace", "grad", "divergence", "c2c"])
     ap.add_argument("--tc", default="none", choices=["none", "tf32", "bf16"],
                     help="call workload: r2c/c2r through a tensor-core plan")
+    ap.add_argument("--df", action="store_true",
+                    help="call workload with --dtype float64: a double-float plan (ACCFFT_C_F64_DF)")
     ap.add_argument("--n", type=int, default=512)
     ap.add_argument("--grid", type=int, nargs=3, default=None,
                     help="non-cubic grid N0 N1 N2 (smaller cases of the same kernels for profiling)")
@@ -889,7 +891,7 @@ def call_workload(args):
         cs = torch.empty_like(cu)
         fn = lambda: plan.c2c(-1, cu, cs)
     else:
-        flags = {"none": 0, "tf32": ag.TC_TF32, "bf16": ag.TC_BF16}[args.tc]
+        flags = {"none": 0, "tf32": ag.TC_TF32, "bf16": ag.TC_BF16}[args.tc] | (ag.F64_DF if args.df else 0)
         plan = ag.PlanR2C(n, dt, flags=flags) if flags else ag.PlanR2C(n, dt)
         plan.r2c(u, spec)
         fn = {"r2c": lambda: plan.r2c(u, spec), "c2r": lambda: plan.c2r(spec, outs[0]),
@@ -905,7 +907,7 @@ def call_workload(args):
         fn()
     b.record()
     torch.cuda.synchronize()
-    print(json.dumps({"workload": "call", "call": args.call, "tc": args.tc, "grid": list(n), "dtype": dt,
+    print(json.dumps({"workload": "call", "call": args.call, "tc": args.tc, "df": args.df, "grid": list(n), "dtype": dt,
                       "ms_per_call": a.elapsed_time(b) / max(1, args.steps)}), flush=True)
 
 
