@@ -248,7 +248,7 @@ def test_pinned_host_real_arrays(cuda, native, oracle, n, dtype):
 def test_pinned_host_pipelines_in_flight(cuda, native):
     """Two plans on two non-blocking streams with pinned host arrays, several
     pairs in flight: every result equals the device path's; the copies show
-    up in the profile as 16 slab batches each way."""
+    up in the profile as 4 slab batches each way (the default count)."""
     torch = cuda
     n = (48, 40, 64)
     hu = [torch.randn(n).pin_memory() for _ in range(4)]
@@ -265,7 +265,7 @@ def test_pinned_host_pipelines_in_flight(cuda, native):
         p.c2r(spec, hb[k])
     torch.cuda.synchronize()
     prof = plans[0].profile()
-    assert prof["h2d"][0] == 2 * 16 and prof["d2h"][0] == 2 * 16
+    assert prof["h2d"][0] == 2 * 4 and prof["d2h"][0] == 2 * 4
     ref = native.PlanR2C(n, "float32")
     for k in range(4):
         du = hu[k].cuda()
