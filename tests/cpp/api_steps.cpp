@@ -18,7 +18,7 @@
 
 static int failures = 0;
 
-static void verdict(const char* name, double err, double tol) {
+static void report(const char* name, double err, double tol) {
   bool ok = err < tol;
   printf("%-36s rel_err %.3e (tol %.0e) %s\n", name, err, tol, ok ? "CORRECT" : "NOT CORRECT");
   if (!ok) ++failures;
@@ -75,7 +75,7 @@ static void step1_double(int* n, MPI_Comm c_comm) {
   accfft_execute_r2c_gpu(plan, u, uh, timer);
   accfft_execute_c2r_gpu(plan, uh, u2, timer);
   cudaMemcpy(back.data(), u2, N * sizeof(double), cudaMemcpyDeviceToHost);
-  verdict("step1 r2c/c2r double", rel_l1(back, h, n, n[2], (double)N), 1e-10);
+  report("step1 r2c/c2r double", rel_l1(back, h, n, n[2], (double)N), 1e-10);
   if (!(timer[4] > 0)) { printf("timer slot 4 not filled\n"); ++failures; }
   accfft_destroy_plan(plan);
   cudaFree(u); cudaFree(u2); cudaFree(uh);
@@ -94,7 +94,7 @@ static void step1_float(int* n, MPI_Comm c_comm) {
   accfft_execute_r2c_gpuf(plan, u, uh);
   accfft_execute_c2r_gpuf(plan, uh, u2);
   cudaMemcpy(back.data(), u2, N * sizeof(float), cudaMemcpyDeviceToHost);
-  verdict("step1 r2c/c2r float", rel_l1(back, h, n, n[2], (double)N), 1e-5);
+  report("step1 r2c/c2r float", rel_l1(back, h, n, n[2], (double)N), 1e-5);
   accfft_destroy_plan_gpu(plan);
   cudaFree(u); cudaFree(u2); cudaFree(uh);
 }
@@ -113,7 +113,7 @@ static void step2_inplace(int* n, MPI_Comm c_comm) {
   accfft_execute_r2c_gpu(plan, d, (Complex*)d);
   accfft_execute_c2r_gpu(plan, (Complex*)d, d);
   cudaMemcpy(back.data(), d, h.size() * sizeof(double), cudaMemcpyDeviceToHost);
-  verdict("step2 in-place r2c/c2r double", rel_l1(back, h, n, row, (double)N), 1e-10);
+  report("step2 in-place r2c/c2r double", rel_l1(back, h, n, row, (double)N), 1e-10);
   accfft_destroy_plan(plan);
   cudaFree(d);
 }
@@ -140,7 +140,7 @@ static void step3_c2c(int* n, MPI_Comm c_comm, const char* name, double tol) {
   cudaMemcpy(back.data(), a, 2 * N * sizeof(Real), cudaMemcpyDeviceToHost);
   double e = 0, s = 0;
   for (size_t q = 0; q < 2 * N; ++q) { e += std::fabs(back[q] / N - h[q]); s += std::fabs(h[q]); }
-  verdict(name, e / s, tol);
+  report(name, e / s, tol);
   accfft_destroy_plan(plan);
   cudaFree(a); cudaFree(b);
 }
@@ -192,14 +192,14 @@ static void step5_ops(int* n, MPI_Comm c_comm) {
   const char* gn[3] = {"step5 grad x double", "step5 grad y double", "step5 grad z double"};
   for (int d = 0; d < 3; ++d) {
     cudaMemcpy(back.data(), G[d], N * sizeof(double), cudaMemcpyDeviceToHost);
-    verdict(gn[d], rel_l1(back, *ref[d], n, n[2], 1.0), 1e-10);
+    report(gn[d], rel_l1(back, *ref[d], n, n[2], 1.0), 1e-10);
   }
   accfft_laplace_gpu(L, A, plan);
   cudaMemcpy(back.data(), L, N * sizeof(double), cudaMemcpyDeviceToHost);
-  verdict("step5 laplace double", rel_l1(back, la, n, n[2], 1.0), 1e-10);
+  report("step5 laplace double", rel_l1(back, la, n, n[2], 1.0), 1e-10);
   accfft_divergence_gpu(L, G[0], G[1], G[2], plan);
   cudaMemcpy(back.data(), L, N * sizeof(double), cudaMemcpyDeviceToHost);
-  verdict("step5 div(grad) double", rel_l1(back, la, n, n[2], 1.0), 1e-10);
+  report("step5 div(grad) double", rel_l1(back, la, n, n[2], 1.0), 1e-10);
   // inv_laplace(laplace(u)) returns u minus its mean (no Nyquist content at this resolution)
   accfft_laplace_gpu(L, A, plan);
   accfft_inv_laplace_gpu(G[0], L, plan);
@@ -209,7 +209,7 @@ static void step5_ops(int* n, MPI_Comm c_comm) {
   mean /= N;
   std::vector<double> am(N);
   for (size_t q = 0; q < N; ++q) am[q] = a[q] - mean;
-  verdict("inv_laplace(laplace) double", rel_l1(back, am, n, n[2], 1.0), 1e-9);
+  report("inv_laplace(laplace) double", rel_l1(back, am, n, n[2], 1.0), 1e-9);
   accfft_destroy_plan(plan);
   cudaFree(A); cudaFree(L); cudaFree(scratch);
   for (double* g : G) cudaFree(g);
