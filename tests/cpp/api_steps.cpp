@@ -60,22 +60,24 @@ static double rel_l1(const std::vector<T>& a, const std::vector<T>& b, const int
   return e / s;
 }
 
-// out-of-place round trip through the typed API of each precision
-static void step1_double(int* n, MPI_Comm c_comm) {
+// out-of-place round trip through the typed API of each precision (for
+// double also with the double-float flag, an extension of the flags word)
+static void step1_double(int* n, MPI_Comm c_comm, unsigned flags = ACCFFT_MEASURE,
+                         const char* name = "step1 r2c/c2r double") {
   int isize[3], osize[3], istart[3], ostart[3];
   int alloc_max = accfft_local_size_dft_r2c_gpu(n, isize, istart, osize, ostart, c_comm);
   size_t N = (size_t)n[0] * n[1] * n[2];
   double* u = dev<double>(N);
   double* u2 = dev<double>(N);
   Complex* uh = (Complex*)dev<char>(alloc_max);
-  accfft_plan_gpu* plan = accfft_plan_dft_3d_r2c_gpu(n, u, (double*)uh, c_comm, ACCFFT_MEASURE);
+  accfft_plan_gpu* plan = accfft_plan_dft_3d_r2c_gpu(n, u, (double*)uh, c_comm, flags);
   std::vector<double> h = field<double>(n, n[2]), back(N);
   cudaMemcpy(u, h.data(), N * sizeof(double), cudaMemcpyHostToDevice);
   double timer[5] = {0, 0, 0, 0, 0};
   accfft_execute_r2c_gpu(plan, u, uh, timer);
   accfft_execute_c2r_gpu(plan, uh, u2, timer);
   cudaMemcpy(back.data(), u2, N * sizeof(double), cudaMemcpyDeviceToHost);
-  report("step1 r2c/c2r double", rel_l1(back, h, n, n[2], (double)N), 1e-10);
+  report(name, rel_l1(back, h, n, n[2], (double)N), 1e-10);
   if (!(timer[4] > 0)) { printf("timer slot 4 not filled\n"); ++failures; }
   accfft_destroy_plan(plan);
   cudaFree(u); cudaFree(u2); cudaFree(uh);
@@ -228,6 +230,7 @@ int main(int argc, char** argv) {
   MPI_Comm c_comm;
   accfft_create_comm(MPI_COMM_WORLD, c_dims, &c_comm);
   step1_double(n, c_comm);
+  step1_double(n, c_comm, ACCFFT_MEASURE | ACCFFT_F64_DF, "step1 r2c/c2r double, double-float plan");
   step1_float(n, c_comm);
   step2_inplace(n, c_comm);
   step3_c2c<Complex, accfft_plan_gpu, double>(n, c_comm, "step3 c2c double", 1e-10);
