@@ -118,3 +118,17 @@ def test_double_float_flag_needs_a_double_plan(native):
         native.PlanR2C((8, 8, 8), "float32", flags=native.F64_DF)
     assert e.value.code == native.EUNSUPPORTED
     assert "double plans" in str(e.value)
+
+
+@pytest.mark.parametrize("env,mode", [("0", 0), ("1", 1), ("2", 2), ("7", 1), ("", 1), ("off", 1)])
+def test_pdl_mode_from_environment(native, env, mode):
+    """ACCFFT_GB300_PDL is read on first use: 0, 1 or 2, anything else the
+    default (1)."""
+    import os
+    import sys
+
+    code = "import accfft_gb300 as ag; print(ag.set_pdl(None))"
+    e = dict(os.environ, ACCFFT_GB300_PDL=env)
+    out = subprocess.run([sys.executable, "-c", code], env=e, capture_output=True, text=True, check=True,
+                         cwd=os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    assert int(out.stdout.strip().splitlines()[-1]) == mode
