@@ -68,6 +68,7 @@ def lib() -> ctypes.CDLL:
         "accfft_c_last_error_code": ([], i),
         "accfft_c_version": ([], i),
         "accfft_c_length_supported": ([i], i),
+        "accfft_c_line_plan": ([i, i, ip, ip, ip], i),
         "accfft_c_kernel_launches": ([], ctypes.c_ulonglong),
         "accfft_c_set_pdl": ([ctypes.c_int], ctypes.c_int),
         "accfft_c_dfft_get_local_size": ([i, i, i, ip, ip, i], ll),
@@ -124,6 +125,19 @@ def last_error() -> str:
 
 def kernel_launches() -> int:
     return int(lib().accfft_c_kernel_launches())
+
+
+def line_plan(length: int, precision: str = "float32") -> dict:
+    """The compiled radix plan of a line length (no plan, no GPU): first
+    radix E, threads per line P and the stage radices.  ``precision`` is
+    "float32", "float64" or "double-float"."""
+    prec = {"float32": 0, "float64": 1, "double-float": 2}[precision]
+    E, P = ctypes.c_int(0), ctypes.c_int(0)
+    rad = (ctypes.c_int * 16)()
+    ns = lib().accfft_c_line_plan(int(length), prec, ctypes.byref(E), ctypes.byref(P), rad)
+    if ns < 0:
+        raise AccfftError(EUNSUPPORTED, f"no radix plan for length {length}")
+    return {"E": E.value, "P": P.value, "radices": [rad[s] for s in range(ns)]}
 
 
 def set_pdl(mode: int | None = None) -> int:

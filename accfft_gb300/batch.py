@@ -32,7 +32,7 @@ import os
 
 import torch
 
-from . import AccfftError, PlanR2C, lib
+from . import AccfftError, PlanR2C, lib, line_plan
 
 OPS = {"r2c_c2r": 2, "laplace": 2, "inv_laplace": 2, "lap_invlap": 4}
 
@@ -40,31 +40,7 @@ OPS = {"r2c_c2r": 2, "laplace": 2, "inv_laplace": 2, "lap_invlap": 4}
 def radix_plan(length: int, dtype: str) -> dict:
     """The compiled radix plan of a line length: first radix E, threads per
     line P and the stage radices (for reports)."""
-    # mirrors line_plan.h plan_for(): fewest stages, E near the preferred size
-    dbl = dtype == "float64"
-    if length == 1:
-        return {"E": 1, "P": 1, "radices": []}
-    epref = (16 if length >= 256 else 8) if dbl else (32 if length >= 512 else 16)
-    pmin = 2 if dbl else 4
-    best = None
-    for E in range(2, min(length, 32) + 1):
-        if length % E:
-            continue
-        rem, rad, ok = length // E, [E], True
-        while rem > 1:
-            d = next((c for c in range(E, 1, -1) if E % c == 0 and rem % c == 0), 0)
-            if d == 0:
-                ok = False
-                break
-            rad.append(d)
-            rem //= d
-        if not ok:
-            continue
-        P = length // E
-        cost = 100 * len(rad) + (50 if P < pmin and length >= 2 * pmin else 0) + (30 if E > epref else 0) + abs(E - epref)
-        if best is None or cost < best[0]:
-            best = (cost, E, P, rad)
-    return {"E": best[1], "P": best[2], "radices": best[3]}
+    return line_plan(length, dtype)
 
 
 class _Instance:

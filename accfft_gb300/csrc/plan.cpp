@@ -1156,6 +1156,15 @@ const char* accfft_c_last_error(void) { return g_err.c_str(); }
 int accfft_c_last_error_code(void) { return g_err_code; }
 int accfft_c_version(void) { return 1; }
 int accfft_c_length_supported(int len) { return length_supported(len) ? 1 : 0; }
+int accfft_c_line_plan(int len, int precision, int* E, int* P, int* radices) {
+  if (len < 1 || precision < 0 || precision > 2 || !E || !P || !radices) return -1;
+  const LinePlan pl = plan_select(len, precision, 0);
+  if (pl.E == 0) return -1;
+  *E = pl.E;
+  *P = pl.P;
+  for (int s = 0; s < pl.ns; ++s) radices[s] = pl.radix[s];
+  return pl.ns;
+}
 unsigned long long accfft_c_kernel_launches(void) { return launch_count(); }
 int accfft_c_set_pdl(int mode) {
   const int was = pdl_mode();

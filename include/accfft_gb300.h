@@ -75,6 +75,12 @@ int accfft_c_version(void);
 /* 1 if an axis of this length has compiled kernels (complex length for
  * c2c axes; for the real z axis of an r2c plan the check is on N2/2) */
 int accfft_c_length_supported(int len);
+/* the compiled radix plan of a line length for the arithmetic `precision`
+ * (0 float, 1 double, 2 double-float): first radix *E, threads per line *P
+ * and the stage radices in radices[0..] (at most 16); returns the number of
+ * stages (0 for length 1), -1 when the length has no plan or an argument is
+ * invalid.  Needs no plan and no GPU. */
+int accfft_c_line_plan(int len, int precision, int* E, int* P, int* radices);
 /* kernels launched by this process through the library (for audits) */
 unsigned long long accfft_c_kernel_launches(void);
 /* programmatic dependent launch of the pass kernels (each pass waits in

@@ -1,8 +1,9 @@
 """Radix plans (accfft_gb300/csrc/line_plan.h), compiled on the host with
-g++: the report mirror in accfft_gb300.batch agrees with the compiled float
-and double plans for every supported length, and double-float plans keep
-the first radix at 8 or below wherever such a plan exists (falling back to
-the double plan elsewhere).  No GPU."""
+g++: the library's accfft_c_line_plan (what the batch reports print)
+returns exactly the header's plans for every supported length and all three
+arithmetic types, and double-float plans keep the first radix at 8 or below
+wherever such a plan exists (falling back to the double plan elsewhere).
+No GPU."""
 import os
 import shutil
 import subprocess
@@ -49,19 +50,17 @@ def plans(tmp_path_factory, native):
     return lengths, res
 
 
-def test_report_mirror_matches_compiled_plans(plans):
+def test_library_reports_the_compiled_plans(plans, native):
     from accfft_gb300.batch import radix_plan
 
     lengths, res = plans
     assert len(lengths) >= 30
     for L in lengths:
-        for cls, dt in ((0, "float32"), (1, "float64")):
-            got = res[(L, cls)]
-            want = radix_plan(L, dt)
-            if L == 1:
-                assert got["E"] == 1 and got["P"] == 1
-                continue
-            assert (got["E"], got["P"], got["radices"]) == (want["E"], want["P"], want["radices"]), (L, dt)
+        for cls, prec in ((0, "float32"), (1, "float64"), (2, "double-float")):
+            assert native.line_plan(L, prec) == res[(L, cls)], (L, prec)
+        assert radix_plan(L, "float32") == res[(L, 0)]
+    with pytest.raises(native.AccfftError):
+        native.line_plan(37)
 
 
 def _has_small_plan(L):
