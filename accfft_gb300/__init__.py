@@ -71,6 +71,8 @@ def lib() -> ctypes.CDLL:
         "accfft_c_line_plan": ([i, i, ip, ip, ip], i),
         "accfft_c_kernel_launches": ([], ctypes.c_ulonglong),
         "accfft_c_set_pdl": ([ctypes.c_int], ctypes.c_int),
+        "accfft_c_set_wait_limit": ([ll], ll),
+        "accfft_c_check": ([vp], i),
         "accfft_c_dfft_get_local_size": ([i, i, i, ip, ip, i], ll),
         "accfft_c_local_size_dft_r2c": ([ip, ip, ip, ip, ip, i], ll),
         "accfft_c_local_size_dft_c2c": ([ip, ip, ip, ip, ip, i], ll),
@@ -146,6 +148,14 @@ def set_pdl(mode: int | None = None) -> int:
     this one's CTAs finish (the default), 2 as they start.  ``None`` only
     queries.  Returns the previous mode."""
     return int(lib().accfft_c_set_pdl(-1 if mode is None else int(mode)))
+
+
+def set_wait_limit(polls: int | None = None) -> int:
+    """Polls a bounded device-side wait makes before it gives up (tensor-core
+    completion waits, the persistent z+y schedule's waits between items);
+    ``None`` restores the default.  A wait that gives up makes the call raise
+    AccfftError(ECUDA).  Returns the previous value."""
+    return int(lib().accfft_c_set_wait_limit(-1 if polls is None else int(polls)))
 
 
 def _check(rc: int):
@@ -237,6 +247,11 @@ class _Plan:
         """0: separate z and y passes (default); 1: cluster slab kernel;
         2: persistent z+y kernel (r2c plans, where the grid has the kernel)"""
         _check(lib().accfft_c_set_zy_schedule(self._h, int(mode)))
+
+    def check(self):
+        """Wait for the plan's stream; raise AccfftError(ECUDA) when a bounded
+        device-side wait of an earlier non-blocking call gave up."""
+        _check(lib().accfft_c_check(self._h))
 
     def destroy(self):
         if getattr(self, "_h", None):

@@ -59,6 +59,9 @@ struct StridedArgs {
   // double-float plans: the largest biased exponent of the transform's input
   // (the passes scale by an exact power of two around their arithmetic)
   const int* dfx;
+  // polls a device-side wait makes before it gives up (tensor-core and
+  // persistent kernels; accfft_c_set_wait_limit)
+  unsigned wait_limit;
 };
 
 struct ContigArgs {
@@ -80,6 +83,7 @@ struct ContigArgs {
   SymArgs sym;
   int early_trigger;        // set by the launcher: release the next pass at CTA start
   const int* dfx;           // as StridedArgs::dfx
+  unsigned wait_limit;      // as StridedArgs::wait_limit
 };
 
 struct SlabArgs {

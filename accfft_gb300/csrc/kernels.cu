@@ -6,6 +6,7 @@
 //   AFG_KIND 0 = strided (MODE 0..4), 1 = zc2c, 2 = zr2c, 3 = zc2r, 4 = zsym (with and without accumulate)
 #include "passes.cuh"
 #include "launch.h"
+#include "per_device.h"
 
 #if !defined(AFG_PREC) || !defined(AFG_KIND) || !defined(AFG_GROUP)
 #error "AFG_PREC, AFG_KIND and AFG_GROUP must be defined"
@@ -48,23 +49,14 @@ typedef afg::df Real;
 
 namespace afg {
 
-// opt-in to more than 48 KB of dynamic shared memory; `done` lives in the
-// caller's per-kernel instantiation
-template <typename K>
-static void prepare(K kernel, size_t smem, bool& done) {
-  if (!done) {
-    if (smem > 48 * 1024) cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-    done = true;
-  }
-}
 
 #if AFG_KIND == 0
 template <int L, int MODE>
 static void run_strided(const StridedArgs& a, cudaStream_t s) {
   typedef StridedShape<Real, L> SH;
   auto k = k_strided<Real, L, MODE>;
-  static bool done = false;
-  prepare(k, SH::smem, done);
+  static PerDevice prepared;   // per instantiation, per device
+  prepare_smem(prepared, k, SH::smem);
   unsigned grid = unsigned((a.ncols + SH::TC - 1) / SH::TC);
   StridedArgs b = a;
   b.early_trigger = pdl_mode() == 2;
@@ -125,8 +117,8 @@ static void run_contig(const ContigArgs& a, cudaStream_t s) {
 #else
   auto k = k_zsym<Real, L, 0, 0, ACC>;
 #endif
-  static bool done = false;
-  prepare(k, SH::smem, done);
+  static PerDevice prepared;   // per instantiation, per device
+  prepare_smem(prepared, k, SH::smem);
   unsigned grid = unsigned((a.nlines + SH::TL - 1) / SH::TL);
   ContigArgs b = a;
   b.early_trigger = pdl_mode() == 2;

@@ -49,20 +49,27 @@ bool launch_slab(bool dbl, int N1, int N2, bool forward, const SlabArgs& a, cuda
 
 // tensor-core forms of the r2c/c2r passes (float; form 1 = 3xTF32, 2 = split
 // BF16): lengths 128, 256, 512, 1024 (strided) and 128, 256, 512 (z half
-// length); err is a device word set when a completion wait timed out
+// length); err is a device word set when a completion wait gave up (after
+// a.wait_limit polls)
 bool tc_length_supported(int len, bool contig);
 bool launch_strided_tc(int form, int L, const StridedArgs& a, int* err, cudaStream_t s);
 bool launch_z_tc(int form, bool r2c, int M, const ContigArgs& a, int* err, cudaStream_t s);
 
 // persistent z+y kernels (zy_fused.cu): grids whose z rows and y columns
-// run on the same tile shape; ctl holds 2 + n0 zeroed words
+// run on the same tile shape; ctl holds 1 + n0 zeroed words; *err is set
+// when a wait between items gave up (after z.wait_limit / y.wait_limit polls)
 bool zy_persistent_available(bool dbl, int M, int L);
 bool launch_zy_persistent(bool dbl, bool forward, int M, int L, const ContigArgs& z, const StridedArgs& y,
-                          unsigned* ctl, int n0, int lead, cudaStream_t s);
+                          unsigned* ctl, int* err, int n0, int lead, cudaStream_t s);
 
 // double-float plans: the largest biased exponent of `rows` rows of `len`
 // doubles, `stride` apart, into *out (zeroed first), on stream s
 bool launch_df_scan(const void* x, long long rows, long long len, long long stride, int* out, cudaStream_t s);
+
+// out[r][c] += in[r][c], c < len, over `rows` rows with their own strides
+// (reals of the plan's precision), on stream s
+bool launch_add_rows(bool dbl, void* out, long long out_row, const void* in, long long in_row, long long rows,
+                     int len, cudaStream_t s);
 
 // number of kernel launches issued by this process through the launchers
 unsigned long long launch_count();

@@ -7,6 +7,7 @@
 
 #include <cmath>
 #include <cstdlib>
+#include <atomic>
 #include <cstdarg>
 #include <cstdint>
 #include <initializer_list>
@@ -43,6 +44,11 @@ int fail(int code, const char* fmt, ...) {
 int cuda_fail(cudaError_t e, const char* what) {
   return fail(ACCFFT_C_ECUDA, "%s: %s", what, cudaGetErrorString(e));
 }
+
+// polls a bounded device-side wait makes before it gives up
+// (accfft_c_set_wait_limit); the default is about half a second
+constexpr unsigned kDefaultWaitLimit = 1u << 22;
+std::atomic<unsigned> g_wait_limit{kDefaultWaitLimit};
 
 // exp(-2*pi*i*m/d) with exact integer octant reduction and long-double
 // evaluation on [0, pi/4]
@@ -127,7 +133,7 @@ struct accfft_c_plan {
   int zy_batches = 1;
   cudaStream_t stream2 = nullptr;
   static constexpr int kMaxBatches = 64;
-  // control words of the persistent z+y kernels (2 + N0, zeroed per launch)
+  // control words of the persistent z+y kernels (1 + N0, zeroed per launch)
   unsigned* zy_ctl = nullptr;
   int zy_lead = 32;   // slabs between a slab's first and second pass (ACCFFT_GB300_ZY_LEAD)
   // pinned-host real arrays: slab batches staged through a device ring
@@ -148,10 +154,14 @@ struct accfft_c_plan {
   // main [N0][N1][M] (rows of M = N2/2 complex, 128-byte aligned) and the
   // Nyquist plane [N0][N1] (kz = N2/2) after it
   bool split = false;
-  // tensor-core form (ACCFFT_C_TC_*): 0 none, 1 3xTF32, 2 split BF16; its
-  // kernels set *tc_err when a completion wait timed out
+  // tensor-core form (ACCFFT_C_TC_*): 0 none, 1 3xTF32, 2 split BF16
   int tc = 0;
-  int* tc_err = nullptr;
+  // device word set by a kernel whose bounded wait gave up (tensor-core
+  // completion waits, the persistent z+y kernel's waits between items).  It
+  // stays set until a blocking or timed call (or accfft_c_check) reads and
+  // clears it; waits_used marks plans that have launched such kernels.
+  int* wait_err = nullptr;
+  bool waits_used = false;
   // double plan whose kernels compute in double-float (ACCFFT_C_F64_DF);
   // df_exp receives the largest biased exponent of each transform's input
   bool df = false;
@@ -322,9 +332,9 @@ accfft_c_plan* make_plan(int kind, bool dbl, const int* n, void* data, void* dat
   cudaError_t e = cudaMalloc(&p->tw_block, total);
   if (e == cudaSuccess) e = cudaMemcpy(p->tw_block, host.data(), total, cudaMemcpyHostToDevice);
   if (e == cudaSuccess && kind == 1) e = cudaMalloc(&p->scratch, (size_t)p->alloc_max);
-  if (e == cudaSuccess && p->tc) e = cudaMalloc(&p->tc_err, sizeof(int));
+  if (e == cudaSuccess) e = cudaMalloc(&p->wait_err, sizeof(int));
   if (e == cudaSuccess && p->df) e = cudaMalloc(&p->df_exp, 16);
-  if (e == cudaSuccess && p->tc) e = cudaMemset(p->tc_err, 0, sizeof(int));
+  if (e == cudaSuccess) e = cudaMemset(p->wait_err, 0, sizeof(int));
   if (e == cudaSuccess) e = cudaEventCreate(&p->ev0);
   if (e == cudaSuccess) e = cudaEventCreate(&p->ev1);
   if (e != cudaSuccess) {
@@ -389,6 +399,23 @@ struct DeviceGuard {
     if (prev >= 0) cudaSetDevice(prev);
   }
 };
+
+// Reads and clears the plan's wait-error word once the plan's stream is idle:
+// ACCFFT_C_ECUDA when a bounded device-side wait of this call, or of an
+// earlier asynchronous call of the plan, gave up.
+int take_wait_error(accfft_c_plan* p, const char* fn) {
+  if (!p->waits_used || !p->wait_err) return ACCFFT_C_OK;
+  int flag = 0;
+  cudaError_t e = cudaMemcpy(&flag, p->wait_err, sizeof(int), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_fail(e, "reading the wait-error word");
+  if (!flag) return ACCFFT_C_OK;
+  cudaMemset(p->wait_err, 0, sizeof(int));
+  return fail(ACCFFT_C_ECUDA,
+              "%s: a device-side wait gave up (%s) in this call or an earlier asynchronous call of the plan; "
+              "its results are not valid",
+              fn, p->tc ? "a tensor-core stage waiting for its matrix products"
+                        : "the persistent z+y kernel waiting for another item");
+}
 
 struct Exec {
   DeviceGuard guard;   // first member: constructed before anything touches the device
@@ -456,8 +483,10 @@ struct Exec {
     a.in_slab = a.out_slab = slab;
     a.in_line = a.out_line = line;
     a.inverse = inverse;
+    a.wait_limit = g_wait_limit.load();
+    if (p->tc) p->waits_used = true;
     if (!timed(tw == p->tw_x ? (inverse ? "x_inv" : "x") : (inverse ? "y_inv" : "y"), p->stream, [&] {
-          return p->tc ? launch_strided_tc(p->tc, L, a, p->tc_err, p->stream) : launch_strided(p->prec(), L, 0, a, p->stream);
+          return p->tc ? launch_strided_tc(p->tc, L, a, p->wait_err, p->stream) : launch_strided(p->prec(), L, 0, a, p->stream);
         }))
       unsupported("strided pass", L);
   }
@@ -499,8 +528,10 @@ struct Exec {
     a.nlines = (long long)p->n[0] * p->n[1];
     a.in_dist = in_row;
     a.out_dist = p->H2();
+    a.wait_limit = g_wait_limit.load();
+    if (p->tc) p->waits_used = true;
     if (!timed("z_r2c", p->stream, [&] {
-          return p->tc ? launch_z_tc(p->tc, true, p->M(), a, p->tc_err, p->stream)
+          return p->tc ? launch_z_tc(p->tc, true, p->M(), a, p->wait_err, p->stream)
                        : launch_zr2c(p->prec(), p->M(), a, p->stream);
         }))
       unsupported("z r2c pass", p->M());
@@ -517,11 +548,19 @@ struct Exec {
     a.nlines = (long long)p->n[0] * p->n[1];
     a.in_dist = p->H2();
     a.out_dist = out_row;
+    a.wait_limit = g_wait_limit.load();
+    if (p->tc) p->waits_used = true;
     if (!timed("z_c2r", p->stream, [&] {
-          return p->tc ? launch_z_tc(p->tc, false, p->M(), a, p->tc_err, p->stream)
+          return p->tc ? launch_z_tc(p->tc, false, p->M(), a, p->wait_err, p->stream)
                        : launch_zc2r(p->prec(), p->M(), a, p->stream);
         }))
       unsupported("z c2r pass", p->M());
+  }
+  // out[r][c] += in[r][c] over the plan's N0*N1 real rows
+  void add_rows(void* out, long long out_row, const void* in, long long in_row, long long rows, int len) {
+    if (!ok()) return;
+    if (!timed("add", p->stream, [&] { return launch_add_rows(p->dbl, out, out_row, in, in_row, rows, len, p->stream); }))
+      rc = fail(ACCFFT_C_ECUDA, "row accumulation: launch failed");
   }
   // z passes and y pass restricted to slabs [s0, s0 + ns) on stream st
   // (the real side `in` / `out` points at the batch's first row)
@@ -615,7 +654,7 @@ struct Exec {
   // backward y pass writes and the z c2r pass reads
   void zy_persistent(bool forward, const void* in, void* mid, void* out, long long row) {
     const long long N0 = p->n[0], H = p->H2();
-    const size_t ctl_bytes = size_t(2 + N0) * sizeof(unsigned);
+    const size_t ctl_bytes = size_t(1 + N0) * sizeof(unsigned);
     if (!p->zy_ctl) {
       cudaError_t e = cudaMalloc(&p->zy_ctl, ctl_bytes);
       if (e != cudaSuccess) {
@@ -652,10 +691,13 @@ struct Exec {
       z.out = out;
       z.out_dist = row;
     }
+    z.wait_limit = y.wait_limit = g_wait_limit.load();
+    p->waits_used = true;
     int lead = p->zy_lead;
     if (lead > N0) lead = int(N0);
     if (!timed(forward ? "zy_persistent" : "yz_persistent", p->stream, [&] {
-          return launch_zy_persistent(p->dbl, forward, p->M(), p->n[1], z, y, p->zy_ctl, int(N0), lead, p->stream);
+          return launch_zy_persistent(p->dbl, forward, p->M(), p->n[1], z, y, p->zy_ctl, p->wait_err, int(N0), lead,
+                                      p->stream);
         }))
       unsupported("persistent z+y pass", p->M());
   }
@@ -915,14 +957,7 @@ struct Exec {
         cudaEventElapsedTime(&ms, p->ev0, p->ev1);
         timer[4] += ms / 1000.0;
       }
-      if (ok() && p->tc) {
-        int flag = 0;
-        cudaMemcpy(&flag, p->tc_err, sizeof(int), cudaMemcpyDeviceToHost);
-        if (flag) {
-          cudaMemset(p->tc_err, 0, sizeof(int));
-          rc = fail(ACCFFT_C_ECUDA, "execute: a tensor-core stage gave up waiting for its matrix products");
-        }
-      }
+      if (ok()) rc = take_wait_error(p, "execute");
     }
     return rc;
   }
@@ -1171,6 +1206,17 @@ int accfft_c_set_pdl(int mode) {
   if (mode >= 0) set_pdl(mode);
   return was;
 }
+long long accfft_c_set_wait_limit(long long polls) {
+  const unsigned v = polls < 0 ? kDefaultWaitLimit : polls > 0xFFFFFFFFLL ? 0xFFFFFFFFu : unsigned(polls);
+  return (long long)g_wait_limit.exchange(v);
+}
+int accfft_c_check(accfft_c_plan* p) {
+  if (!p) return fail(ACCFFT_C_EINVAL, "check: NULL plan");
+  DeviceGuard guard(p->device);
+  cudaError_t e = cudaStreamSynchronize(p->stream);
+  if (e != cudaSuccess) return cuda_fail(e, "check: stream synchronisation");
+  return take_wait_error(p, "check");
+}
 
 long long accfft_c_dfft_get_local_size(int N0, int N1, int tuple, int isize[3], int istart[3], int real_bytes) {
   return local_size(N0, N1, tuple, isize, istart, real_bytes);
@@ -1203,7 +1249,7 @@ void accfft_c_destroy_plan(accfft_c_plan* p) {
   if (p->tw_block) cudaFree(p->tw_block);
   if (p->scratch) cudaFree(p->scratch);
   if (p->hstage) cudaFree(p->hstage);
-  if (p->tc_err) cudaFree(p->tc_err);
+  if (p->wait_err) cudaFree(p->wait_err);
   if (p->zy_ctl) cudaFree(p->zy_ctl);
   if (p->df_exp) cudaFree(p->df_exp);
   if (p->ev0) cudaEventDestroy(p->ev0);
@@ -1391,9 +1437,42 @@ int accfft_c_divergence(accfft_c_plan* p, void* divA, const void* A_x, const voi
   return ex.finish();
 }
 
+// The reference's slow divergence (src/operators_gpu.txx:337-446, CPU
+// src/operators.txx:1019-1119) transforms each component over two axes only:
+// A_x over {x, z}, A_y over {y, z}, A_z over {z}, multiplies by i*k/(N_j N2)
+// with the 3-D multipliers' filter (index N_j/2 -> 0 with integer N_j/2) and
+// transforms back.  On an odd axis that filter is not Hermitian-consistent,
+// and the c2r's real projection then gives a result different from the fast
+// divergence, so this keeps the reference's pass structure: z r2c, one fused
+// forward/multiply/inverse pass along x (or y), z c2r; the y term's c2r lands
+// in the padded rows of the scratch and is added by a row kernel; the z term
+// is the accumulating z derivative pass.
 int accfft_c_divergence_slow(accfft_c_plan* p, void* divA, const void* A_x, const void* A_y, const void* A_z,
                              double* timer) {
-  return accfft_c_divergence(p, divA, A_x, A_y, A_z, timer);
+  int rc = check_plan(p, 1, -1, "divergence_slow");
+  if (rc) return rc;
+  if (!divA || !A_x || !A_y || !A_z) return fail(ACCFFT_C_EINVAL, "divergence_slow: NULL array");
+  if (int a = check_align(p, "divergence_slow", {divA, A_x, A_y, A_z})) return a;
+  if (int a = check_addressable("divergence_slow", {divA, A_x, A_y, A_z})) return a;
+  const long long h = p->H2(), rr = p->rrow();
+  const int N0 = p->n[0], N1 = p->n[1], N2 = p->n[2];
+  void* s = p->scratch;
+  Exec ex(p, timer);
+  // x term over {x, z}: lines along x of the half spectrum
+  ex.zr2c(A_x, s, rr);
+  const long long c = (long long)N1 * h;
+  ex.strided_sym(s, s, nullptr, p->tw_x, N0, c, c, 0, c, make_sym(p, SYM_GRADX, 1.0 / ((double)N0 * N2)), "x_sym");
+  ex.zc2r(s, divA, rr);
+  // y term over {y, z}: the x multiplier's fold applied along the y lines
+  ex.zr2c(A_y, s, rr);
+  SymArgs sy = make_sym(p, SYM_GRADX, 1.0 / ((double)N1 * N2));
+  sy.n0 = N1;
+  ex.strided_sym(s, s, nullptr, p->tw_y, N1, (long long)N0 * h, h, (long long)N1 * h, h, sy, "y_sym");
+  ex.zc2r(s, s, 2 * h);
+  ex.add_rows(divA, rr, s, 2 * h, (long long)N0 * N1, N2);
+  // z term over {z}
+  deriv_axis(ex, p, 2, divA, A_z, divA);
+  return ex.finish();
 }
 
 // --- adjoints (no counterpart in the reference; used by the autograd layer)

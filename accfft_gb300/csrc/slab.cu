@@ -21,6 +21,7 @@
 
 #include "launch.h"
 #include "passes.cuh"
+#include "per_device.h"
 
 namespace cg = cooperative_groups;
 
@@ -199,24 +200,22 @@ bool cluster_launch(K kernel, int C, int threads, size_t smem, long long grid, c
   return cudaLaunchKernelEx(&cfg, kernel, a) == cudaSuccess;
 }
 
-// -1: not yet checked, 0: the cluster cannot be scheduled, 1: usable
+// whether the kernels' clusters can be scheduled, checked once per device
 template <typename T, int N1, int M, int C>
 struct SlabKernels {
   typedef SlabShape<T, N1, M, C> SH;
-  static int state;
-  static bool ready() {
-    if (state >= 0) return state == 1;
-    state = 0;
+  static PerDevice state;   // 1: usable, -1: not on this device
+  static int check() {
     auto kf = k_slab_fwd<T, N1, M, C>;
     auto ki = k_slab_inv<T, N1, M, C>;
     for (auto k : {kf, ki}) {
       if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SH::smem) != cudaSuccess) {
         cudaGetLastError();
-        return false;
+        return -1;
       }
       if (C > 8 && cudaFuncSetAttribute(k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
         cudaGetLastError();
-        return false;
+        return -1;
       }
       cudaLaunchConfig_t cfg = {};
       cfg.gridDim = dim3(C, 1, 1);
@@ -232,12 +231,12 @@ struct SlabKernels {
       int n = 0;
       if (cudaOccupancyMaxActiveClusters(&n, k, &cfg) != cudaSuccess || n < 1) {
         cudaGetLastError();
-        return false;
+        return -1;
       }
     }
-    state = 1;
-    return true;
+    return 1;
   }
+  static bool ready() { return per_device(state, check) == 1; }
   static bool launch(bool fwd, const SlabArgs& a, cudaStream_t s) {
     if (!ready()) return false;
     bool ok = fwd ? cluster_launch(k_slab_fwd<T, N1, M, C>, C, SH::threads, SH::smem, (long long)a.n0 * C, a, s)
@@ -247,7 +246,7 @@ struct SlabKernels {
   }
 };
 template <typename T, int N1, int M, int C>
-int SlabKernels<T, N1, M, C>::state = -1;
+PerDevice SlabKernels<T, N1, M, C>::state;
 
 }  // namespace
 

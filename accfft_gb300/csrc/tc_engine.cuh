@@ -21,9 +21,11 @@
 // 8-row x 16-byte core matrices, adjacent along K at LBO = 128 B, adjacent
 // 8-row groups at SBO = (row bytes / 16) * 128 B.
 //
-// Every wait on the MMA-completion mbarrier is bounded; a timeout sets the
-// error word and the engine stops issuing and waiting, so the kernel always
-// reaches its end, where the TMEM columns are freed.
+// Every wait on the MMA-completion mbarrier is bounded (TcCtx::limit polls).
+// A wait that gives up sets the error word, then drains: it waits again, up
+// to kTcDrainPolls, for the products already issued, so no MMA still writes
+// tensor memory when the kernel frees it.  After that the engine issues and
+// waits no more, and the kernel always reaches its end.
 #pragma once
 #include <cstdint>
 #include "fft_core.cuh"
@@ -125,9 +127,13 @@ struct TcCtx {
   uint32_t* tmem_slot;   // tensor-memory base address written by tcgen05.alloc
   uint32_t tmem;
   uint32_t phase;
-  bool dead;             // a wait timed out: issue and wait no more
-  int* err;              // global error word (nonzero: a wait timed out)
+  bool dead;             // a wait gave up: issue and wait no more
+  int* err;              // global error word (nonzero: a wait gave up)
+  unsigned limit;        // polls of a completion wait before it gives up
 };
+
+// polls of the drain that follows a wait that gave up (about a second)
+constexpr unsigned kTcDrainPolls = 1u << 22;
 
 // shared-memory bytes the engine adds after the exchange buffer (which must
 // hold at least threads * row_bytes)
@@ -173,7 +179,8 @@ __device__ __forceinline__ void tc_split(float x, float& hi, float& lo) {
 // set up: W^T operands, mbarrier, tensor memory (cols >= 32 * blocks, a power
 // of two); threads must be a multiple of 128
 template <TcForm F, int THREADS>
-__device__ __forceinline__ void tc_begin(TcCtx& c, unsigned char* exchange, unsigned char* extra, int* err) {
+__device__ __forceinline__ void tc_begin(TcCtx& c, unsigned char* exchange, unsigned char* extra, int* err,
+                                         unsigned limit) {
   static_assert(THREADS % 128 == 0, "tensor-core stages use M = 128 row blocks");
   constexpr int RB = TcTraits<F>::row_bytes;
   c.a_hi = exchange;
@@ -185,6 +192,7 @@ __device__ __forceinline__ void tc_begin(TcCtx& c, unsigned char* exchange, unsi
   c.phase = 0;
   c.dead = false;
   c.err = err;
+  c.limit = limit;
   // B[n][k] = Wreal[n][k]: rows 0-15 give Yr, 16-31 Yi; columns 0-15 take
   // Xr, 16-31 Xi; W = exp(-2 pi i n k / 16)
   for (int e = threadIdx.x; e < 32 * 32; e += THREADS) {
@@ -287,10 +295,11 @@ __device__ __forceinline__ void tc_dft16(TcCtx& c, float2 (&v)[16]) {
   }
   if (!c.dead) {
     bool ok = false;
-    for (int i = 0; i < (1 << 22) && !ok; ++i) ok = mbar_try(smem_u32(c.mbar), c.phase);
+    for (unsigned i = 0; i < c.limit && !ok; ++i) ok = mbar_try(smem_u32(c.mbar), c.phase);
     if (!ok) {
       c.dead = true;
       atomicExch(c.err, 1);
+      for (unsigned i = 0; i < kTcDrainPolls && !ok; ++i) ok = mbar_try(smem_u32(c.mbar), c.phase);
     }
   }
   c.phase ^= 1u;

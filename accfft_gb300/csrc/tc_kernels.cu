@@ -7,6 +7,7 @@
 
 #include "launch.h"
 #include "passes.cuh"
+#include "per_device.h"
 #include "tc_engine.cuh"
 
 namespace afg {
@@ -41,7 +42,7 @@ k_strided_tc(const StridedArgs a, int* err) {
   extern __shared__ __align__(16) unsigned char smraw[];
   V* sm = reinterpret_cast<V*>(smraw);
   TcCtx ctx;
-  tc_begin<F, SH::threads>(ctx, smraw, smraw + SH::exch, err);
+  tc_begin<F, SH::threads>(ctx, smraw, smraw + SH::exch, err, a.wait_limit);
   const int c = threadIdx.x % TC;
   const int t = threadIdx.x / TC;
   const long long g = (long long)blockIdx.x * TC + c;
@@ -76,7 +77,7 @@ k_zr2c_tc(const ContigArgs a, int* err) {
   extern __shared__ __align__(16) unsigned char smraw[];
   V* sm = reinterpret_cast<V*>(smraw);
   TcCtx ctx;
-  tc_begin<F, TS::threads>(ctx, smraw, smraw + TS::exch, err);
+  tc_begin<F, TS::threads>(ctx, smraw, smraw + TS::exch, err, a.wait_limit);
   const int t = threadIdx.x % P, li = threadIdx.x / P;
   const long long line = (long long)blockIdx.x * TL + li;
   const bool valid = line < a.nlines;
@@ -116,7 +117,7 @@ k_zc2r_tc(const ContigArgs a, int* err) {
   extern __shared__ __align__(16) unsigned char smraw[];
   V* sm = reinterpret_cast<V*>(smraw);
   TcCtx ctx;
-  tc_begin<F, TS::threads>(ctx, smraw, smraw + TS::exch, err);
+  tc_begin<F, TS::threads>(ctx, smraw, smraw + TS::exch, err, a.wait_limit);
   const int t = threadIdx.x % P, li = threadIdx.x / P;
   const long long line = (long long)blockIdx.x * TL + li;
   const bool valid = line < a.nlines;
@@ -155,17 +156,13 @@ k_zc2r_tc(const ContigArgs a, int* err) {
 }
 
 // ------------------------------------------------------------------ launches
-template <typename K>
-static bool tc_prepare(K kernel, size_t smem) {
-  return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)) == cudaSuccess;
-}
 
 template <int L, TcForm F>
 static bool run_strided_tc(const StridedArgs& a, int* err, cudaStream_t s) {
   typedef TcStridedShape<L, F> SH;
   auto k = k_strided_tc<L, F>;
-  static bool ready = tc_prepare(k, SH::smem);
-  if (!ready) return false;
+  static PerDevice prepared;
+  if (!prepare_smem(prepared, k, SH::smem)) return false;
   k<<<unsigned((a.ncols + SH::TC - 1) / SH::TC), SH::threads, SH::smem, s>>>(a, err);
   count_launch();
   return true;
@@ -175,8 +172,8 @@ template <int M, TcForm F, bool R2C>
 static bool run_contig_tc(const ContigArgs& a, int* err, cudaStream_t s) {
   typedef TcContigShape<M, F> SH;
   auto k = R2C ? k_zr2c_tc<M, F> : k_zc2r_tc<M, F>;
-  static bool ready = tc_prepare(k, SH::smem);
-  if (!ready) return false;
+  static PerDevice prepared;
+  if (!prepare_smem(prepared, k, SH::smem)) return false;
   k<<<unsigned((a.nlines + SH::CS::TL - 1) / SH::CS::TL), SH::threads, SH::smem, s>>>(a, err);
   count_launch();
   return true;

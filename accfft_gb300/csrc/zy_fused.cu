@@ -9,10 +9,13 @@
 //
 // Deadlock freedom: every item an item waits for was handed out earlier, to a
 // CTA that is running it, and items of the first kind wait for nothing.  The
-// waits are bounded anyway (about half a second); a timeout sets the error
-// word and the item goes ahead.
+// waits are bounded anyway (wait_limit polls of at least 128 ns; the default
+// is about half a second): a wait that gives up sets the plan's error word,
+// which the host reports, and its item is skipped, so nothing reads a slab
+// that is only partly written and the kernel always ends.
 #include "launch.h"
 #include "passes.cuh"
+#include "per_device.h"
 
 namespace afg {
 
@@ -59,19 +62,26 @@ __device__ __forceinline__ void zy_decode(long long item, int n0, int lead, int 
   }
 }
 
-// thread 0 waits (bounded) until `count` items of the slab are done
-__device__ __forceinline__ void zy_wait(unsigned* done, int* err, int slab, unsigned count) {
+// thread 0 waits until `count` items of the slab are done, polling at most
+// `limit` times; false (for the whole CTA) when it gave up
+__device__ __forceinline__ bool zy_wait(const unsigned* done, int* err, int slab, unsigned count, unsigned limit) {
+  __shared__ int s_ok;
   if (threadIdx.x == 0) {
-    volatile unsigned* d = done + slab;
+    const volatile unsigned* d = done + slab;
     bool ok = false;
-    for (int it = 0; it < (1 << 22) && !ok; ++it) {
-      ok = *d >= count;
-      if (!ok) __nanosleep(128);
+    for (unsigned it = 0; it < limit; ++it) {
+      if (*d >= count) {
+        ok = true;
+        break;
+      }
+      __nanosleep(128);
     }
     if (!ok) atomicExch(err, 1);
     __threadfence();
+    s_ok = ok;
   }
   __syncthreads();
+  return s_ok != 0;
 }
 
 __device__ __forceinline__ void zy_signal(unsigned* done, int slab) {
@@ -82,16 +92,16 @@ __device__ __forceinline__ void zy_signal(unsigned* done, int slab) {
   }
 }
 
-// control words: [0] next item, [1] error, [2 + s] items done in slab s
+// control words (zeroed per launch): [0] next item, [1 + s] items done in
+// slab s; err is the plan's error word (sticky until the host reads it)
 template <typename T, int M, int L, bool FWD>
 __global__ void __launch_bounds__(ZyShape<T, M, L>::threads, 2)
-k_zy_persistent(const ContigArgs z, const StridedArgs y, unsigned* ctl, int n0, int lead) {
+k_zy_persistent(const ContigArgs z, const StridedArgs y, unsigned* ctl, int* err, int n0, int lead) {
   typedef ZyShape<T, M, L> SH;
   typedef typename CT<T>::V V;
   __shared__ long long s_item;
   unsigned* next = ctl;
-  int* err = reinterpret_cast<int*>(ctl + 1);
-  unsigned* done = ctl + 2;
+  unsigned* done = ctl + 1;
   const int n_first = FWD ? SH::ZI : SH::YI, n_second = FWD ? SH::YI : SH::ZI;
   const long long total = (long long)n0 * (SH::ZI + SH::YI);
   const long long zslab = (long long)L;                       // z rows per slab
@@ -110,17 +120,16 @@ k_zy_persistent(const ContigArgs z, const StridedArgs y, unsigned* ctl, int n0, 
       if (FWD) {
         a.in = static_cast<const T*>(z.in) + slab * zslab * z.in_dist;
         a.out = static_cast<V*>(z.out) + slab * zslab * z.out_dist;
-      } else {
-        zy_wait(done, err, slab, SH::YI);
+        a.nlines = zslab;
+        zr2c_tile<T, M>(a, sub);
+        zy_signal(done, slab);
+      } else if (zy_wait(done, err, slab, SH::YI, z.wait_limit)) {
         a.in = static_cast<const V*>(z.in) + slab * zslab * z.in_dist;
         a.out = static_cast<T*>(z.out) + slab * zslab * z.out_dist;
+        a.nlines = zslab;
+        zc2r_tile<T, M, 0, 0, true>(a, sub);
       }
-      a.nlines = zslab;
-      if (FWD) zr2c_tile<T, M>(a, sub);
-      else zc2r_tile<T, M, 0, 0, true>(a, sub);
-      if (FWD) zy_signal(done, slab);
-    } else {
-      if (FWD) zy_wait(done, err, slab, SH::ZI);
+    } else if (!FWD || zy_wait(done, err, slab, SH::ZI, y.wait_limit)) {
       StridedArgs a = y;
       a.in = static_cast<const V*>(y.in) + slab * spec_slab;
       a.out = static_cast<V*>(y.out) + slab * spec_slab;
@@ -133,25 +142,27 @@ k_zy_persistent(const ContigArgs z, const StridedArgs y, unsigned* ctl, int n0, 
 }
 
 template <typename T, int M, int L>
-static bool run_zy(bool forward, const ContigArgs& z, const StridedArgs& y, unsigned* ctl, int n0, int lead,
-                   cudaStream_t s) {
+static bool run_zy(bool forward, const ContigArgs& z, const StridedArgs& y, unsigned* ctl, int* err, int n0,
+                   int lead, cudaStream_t s) {
   typedef ZyShape<T, M, L> SH;
   static_assert(SH::ok, "z and y tiles of the persistent kernel have one thread count");
   auto k = forward ? k_zy_persistent<T, M, L, true> : k_zy_persistent<T, M, L, false>;
-  static int blocks[2] = {0, 0};
-  int& nb = blocks[forward ? 0 : 1];
-  if (nb == 0) {
-    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(SH::smem)) != cudaSuccess) return false;
+  // resident CTAs on the whole device (the grid of a persistent kernel), per
+  // device and direction; -1 when the kernel cannot run there
+  static PerDevice blocks[2];
+  const int nb = per_device(blocks[forward ? 0 : 1], [&] {
+    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(SH::smem)) != cudaSuccess) return -1;
     int per_sm = 0, dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, SH::threads, SH::smem) != cudaSuccess || per_sm < 1)
-      return false;
-    nb = per_sm * sms;
-  }
+      return -1;
+    return per_sm * sms;
+  });
+  if (nb < 1) return false;
   const long long items = (long long)n0 * (SH::ZI + SH::YI);
   const unsigned grid = unsigned(items < nb ? items : nb);
-  k<<<grid, SH::threads, SH::smem, s>>>(z, y, ctl, n0, lead);
+  k<<<grid, SH::threads, SH::smem, s>>>(z, y, ctl, err, n0, lead);
   count_launch();
   return true;
 }
@@ -161,10 +172,10 @@ bool zy_persistent_available(bool dbl, int M, int L) {
 }
 
 bool launch_zy_persistent(bool dbl, bool forward, int M, int L, const ContigArgs& z, const StridedArgs& y,
-                          unsigned* ctl, int n0, int lead, cudaStream_t s) {
+                          unsigned* ctl, int* err, int n0, int lead, cudaStream_t s) {
   if (dbl) return false;
-  if (M == 256 && L == 512) return run_zy<float, 256, 512>(forward, z, y, ctl, n0, lead, s);
-  if (M == 128 && L == 256) return run_zy<float, 128, 256>(forward, z, y, ctl, n0, lead, s);
+  if (M == 256 && L == 512) return run_zy<float, 256, 512>(forward, z, y, ctl, err, n0, lead, s);
+  if (M == 128 && L == 256) return run_zy<float, 128, 256>(forward, z, y, ctl, err, n0, lead, s);
   return false;
 }
 

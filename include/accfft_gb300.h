@@ -91,6 +91,21 @@ unsigned long long accfft_c_kernel_launches(void);
  * value; mode >= 0 sets it for the process, -1 only queries; returns the
  * previous mode. */
 int accfft_c_set_pdl(int mode);
+/* extension: every device-side wait of the library's kernels is bounded (the
+ * tensor-core forms wait for their matrix products; the persistent z+y
+ * schedule's items wait for the items of their slab).  A wait gives up after
+ * `polls` polls (the default, 2^22, is about half a second), sets the plan's
+ * error word and lets the kernel finish without the missing data; the call
+ * (or, for a non-blocking call, the plan's next blocking or timed call, or
+ * accfft_c_check) then returns ACCFFT_C_ECUDA and its results are not valid.
+ * The reference's execute has no failure path of this kind (its waits are
+ * cuFFT's and the runtime's).  polls < 0 restores the default; the setting
+ * is per process; returns the previous value. */
+long long accfft_c_set_wait_limit(long long polls);
+/* extension: wait for everything enqueued by the plan and report a device-side
+ * wait that gave up since the plan's last blocking, timed or checked call
+ * (ACCFFT_C_ECUDA); ACCFFT_C_OK otherwise */
+int accfft_c_check(accfft_c_plan* plan);
 
 /* --- local sizes ------------------------------------------------------
  * Replaces dfft_get_local_size_t (src/accfft_common.cpp:49-91),

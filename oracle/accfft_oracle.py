@@ -324,6 +324,26 @@ def divergence(ax, ay, az, prec="d", nthreads=0):
     return out + deriv(az, 2, prec, nthreads)
 
 
+def divergence_slow(ax, ay, az, prec="d", nthreads=0):
+    """The slow divergence (accfft_divergence_gpu_slow_t, src/operators_gpu.txx:337-446;
+    CPU src/operators.txx:1019-1119): A_x transformed over {x, z} (xyz = 5),
+    A_y over {y, z} (6), A_z over {z} (4); each multiplied by i*fold(k_j)/(N_j*N2)
+    with the 3-D multipliers' filter (index N_j/2 -> 0, src/operators.txx:24-110)
+    and transformed back over the same axes; the terms summed x, y, z."""
+    n = ax.shape
+    out = None
+    for a, (f, xyz) in enumerate(((ax, 5), (ay, 6), (az, 4))):
+        s = r2c(f, xyz, prec, nthreads)
+        L = n[a]
+        w = fold(np.arange(s.shape[a]), L).astype(np.float64)
+        shape = [1, 1, 1]
+        shape[a] = s.shape[a]
+        scale = 1.0 / (L * n[2]) if a < 2 else 1.0 / n[2]
+        t = c2r(s * (1j * w * scale).reshape(shape), n[2], xyz, prec, nthreads)
+        out = t if out is None else out + t
+    return out
+
+
 # ---------------------------------------------------- numpy cross-check
 def np_r2c(u):
     return np.fft.rfftn(u, axes=(0, 1, 2))
