@@ -84,6 +84,7 @@ def lib() -> ctypes.CDLL:
         "accfft_c_plan_info": ([vp, ip, ip, ip, ip, ctypes.POINTER(ll)], i),
         "accfft_c_set_stream": ([vp, vp, i], i),
         "accfft_c_set_zy_schedule": ([vp, i], i),
+        "accfft_c_set_pass_order": ([vp, i], i),
         "accfft_c_set_profiling": ([vp, i], i),
         "accfft_c_profile_read": ([vp, i, ctypes.c_char_p, ctypes.POINTER(ll), dp], i),
         "accfft_c_execute_r2c_gpu": ([vp, vp, vp, dp, u], i),
@@ -112,6 +113,12 @@ def lib() -> ctypes.CDLL:
         "accfft_c_c2r_adjoint": ([vp, vp, vp, dp], i),
         "accfft_c_grad_adjoint": ([vp, vp, vp, vp, vp, dp], i),
         "accfft_c_divergence_adjoint": ([vp, vp, vp, vp, vp, dp], i),
+        "accfft_c_batch_create": ([], vp),
+        "accfft_c_batch_destroy": ([vp], None),
+        "accfft_c_batch_record": ([vp, vp, i], i),
+        "accfft_c_batch_finalize": ([vp], i),
+        "accfft_c_batch_run": ([vp, vp], i),
+        "accfft_c_batch_info": ([vp, ip, ip, ip, ip], i),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -247,6 +254,11 @@ class _Plan:
         """0: separate z and y passes (default); 1: cluster slab kernel;
         2: persistent z+y kernel (r2c plans, where the grid has the kernel)"""
         _check(lib().accfft_c_set_zy_schedule(self._h, int(mode)))
+
+    def set_pass_order(self, order):
+        """0: the reference's pass order (z, y, x); 1: packed (y and x over the
+        real field viewed as complex, then mirror-paired z lines)"""
+        _check(lib().accfft_c_set_pass_order(self._h, int(order)))
 
     def check(self):
         """Wait for the plan's stream; raise AccfftError(ECUDA) when a bounded
@@ -387,3 +399,60 @@ class PlanC2C(_Plan):
         f = lib().accfft_c_execute_c2c_gpu if self.dbl else lib().accfft_c_execute_c2c_gpuf
         _check(f(self._h, direction, _ptr(data), _ptr(data_out), tp, xyz))
         self._timer_back(buf, timer)
+
+
+class Batch:
+    """Independent transforms recorded pass by pass and run level by level,
+    one grouped kernel per (pass kind, line length) and level
+    (accfft_c_batch_* in include/accfft_gb300.h).
+
+        b = Batch()
+        with b.recording(plan):      # the plan's calls are recorded, not run
+            plan.r2c(u, spec)
+            plan.c2r(spec, back)
+        b.finalize()
+        b.run(stream)                # capturable into a CUDA graph
+    """
+
+    def __init__(self):
+        self._b = lib().accfft_c_batch_create()
+
+    def record(self, plan, on=True):
+        _check(lib().accfft_c_batch_record(self._b, plan.handle, 1 if on else 0))
+
+    def recording(self, plan):
+        batch = self
+
+        class _Rec:
+            def __enter__(self):
+                batch.record(plan, True)
+                return plan
+
+            def __exit__(self, *exc):
+                batch.record(plan, False)
+                return False
+
+        return _Rec()
+
+    def finalize(self):
+        _check(lib().accfft_c_batch_finalize(self._b))
+
+    def run(self, stream=None):
+        s = 0 if stream is None else getattr(stream, "cuda_stream", stream)
+        _check(lib().accfft_c_batch_run(self._b, s))
+
+    def info(self) -> dict:
+        vals = [ctypes.c_int() for _ in range(4)]
+        _check(lib().accfft_c_batch_info(self._b, *[ctypes.byref(v) for v in vals]))
+        return dict(zip(("instances", "levels", "launches", "tasks"), (v.value for v in vals)))
+
+    def destroy(self):
+        if getattr(self, "_b", None):
+            lib().accfft_c_batch_destroy(self._b)
+            self._b = None
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass

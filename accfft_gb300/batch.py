@@ -1,5 +1,14 @@
 """Many independent 3-D transforms of uneven sizes as one CUDA-graph launch.
 
+Two forms of the same batch:
+  * "streams": every instance's own kernels, forked over `streams` CUDA
+    streams inside the graph;
+  * "grouped": the instances' calls are recorded into an accfft_gb300.Batch
+    and run level by level, one grouped kernel per (pass kind, line length)
+    and level over the tiles of every instance (about 10 levels x a few
+    lengths instead of one launch per pass per instance).
+tune() times both and keeps the faster.
+
     bp = BatchPlan([((32, 32, 32), "r2c_c2r"), ((160, 180, 200), "lap_invlap"), ...])
     bp.set_inputs(list_of_tensors)      # or bp.inputs[i].copy_(...)
     bp.tune()                            # optional: per-shape schedule and stream count
@@ -32,7 +41,7 @@ import os
 
 import torch
 
-from . import AccfftError, PlanR2C, lib, line_plan
+from . import AccfftError, Batch, PlanR2C, lib, line_plan
 
 OPS = {"r2c_c2r": 2, "laplace": 2, "inv_laplace": 2, "lap_invlap": 4}
 
@@ -76,7 +85,7 @@ class _Instance:
 
 
 class BatchPlan:
-    def __init__(self, specs, dtype="float32", streams=4, cache=None, device="cuda"):
+    def __init__(self, specs, dtype="float32", streams=4, cache=None, device="cuda", form="streams"):
         for shape, op in specs:
             if op not in OPS:
                 raise ValueError(f"unknown operation {op!r}")
@@ -91,6 +100,8 @@ class BatchPlan:
         self.graph = None
         self._side = {}
         self.transforms = sum(OPS[i.op] for i in self.instances)
+        self.form = form
+        self._batch = None
 
     @property
     def inputs(self):
@@ -184,10 +195,19 @@ class BatchPlan:
             inst.make_plan(self.schedule[inst.shape])
         times = {k: self._time_eager(k) for k in stream_choices}
         self.streams = min(times, key=times.get)
+        grouped_ms = None
+        try:
+            grouped_ms = self._time_grouped()
+        except AccfftError:
+            pass                        # a length without grouped kernels
+        if grouped_ms is not None and grouped_ms < times[self.streams]:
+            self.form = "grouped"
+        else:
+            self.form = "streams"
         if self.cache:
             json.dump(cached, open(self.cache, "w"), indent=1)
         return {"schedule": {"x".join(map(str, s)): v for s, v in self.schedule.items()},
-                "streams": self.streams, "stream_ms": times}
+                "streams": self.streams, "stream_ms": times, "grouped_ms": grouped_ms, "form": self.form}
 
     def report(self):
         rows = []
@@ -197,16 +217,49 @@ class BatchPlan:
             rows.append({"grid": list(shape), "schedule": self.schedule.get(shape, "split"), "radix": axes})
         return rows
 
+    # ------------------------------------------------------- grouped form
+    def grouped(self):
+        """The recorded, level-by-level form of the batch (built once)."""
+        if self._batch is None:
+            b = Batch()
+            for inst in self.instances:
+                if inst.plan is None or self.schedule.get(inst.shape, "split") != "split":
+                    inst.make_plan("split")
+                with b.recording(inst.plan):
+                    inst.enqueue(torch.cuda.current_stream())
+            b.finalize()
+            self._batch = b
+        return self._batch
+
+    def _time_grouped(self, reps=3):
+        b = self.grouped()
+        main = torch.cuda.current_stream()
+        b.run(main)
+        torch.cuda.synchronize()
+        a, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(main)
+        for _ in range(reps):
+            b.run(main)
+        e.record(main)
+        torch.cuda.synchronize()
+        return a.elapsed_time(e) / reps
+
     # ------------------------------------------------------------- capture
+    def _enqueue_form(self, main):
+        if self.form == "grouped":
+            self.grouped().run(main)
+        else:
+            self._enqueue_all(main, self.streams)
+
     def capture(self):
         # every kernel and shared-memory attribute is set up by an eager run
         torch.cuda.synchronize()
-        self._enqueue_all(torch.cuda.current_stream(), self.streams)
+        self._enqueue_form(torch.cuda.current_stream())
         torch.cuda.synchronize()
         self.graph = torch.cuda.CUDAGraph()
         # relaxed: the plans query pointer attributes while enqueuing
         with torch.cuda.graph(self.graph, capture_error_mode="relaxed"):
-            self._enqueue_all(torch.cuda.current_stream(), self.streams)
+            self._enqueue_form(torch.cuda.current_stream())
         torch.cuda.synchronize()
 
     def run(self):

@@ -84,6 +84,11 @@ struct ContigArgs {
   int early_trigger;        // set by the launcher: release the next pass at CTA start
   const int* dfx;           // as StridedArgs::dfx
   unsigned wait_limit;      // as StridedArgs::wait_limit
+  // packed pass order (k_zr2c / k_zc2r only): when pair_n1 > 0 the lines are
+  // the z lines of an [pair_n0][pair_n1] grid taken in mirror pairs
+  // (x, y) / ((n0-x)%n0, (n1-y)%n1), both lines of a pair in one CTA; nlines
+  // is twice the number of pairs (pair_lines() in passes.cuh)
+  int pair_n0, pair_n1;
 };
 
 struct SlabArgs {

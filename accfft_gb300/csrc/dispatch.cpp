@@ -61,4 +61,35 @@ AFG_DISPATCH(zc2r, launch_zc2r_fdf_g0(L, a, s) || launch_zc2r_fdf_g1(L, a, s))
 AFG_DISPATCH(zsym, false)
 #undef AFG_DISPATCH
 
+long long grouped_tiles(int kind, int L, const void* args) {
+  long long t = -1;
+  if (kind == PK_STRIDED) {
+    const auto& a = *static_cast<const StridedArgs*>(args);
+    t = tiles_strided_f32_g0(L, a);
+    if (t < 0) t = tiles_strided_f32_g1(L, a);
+  } else if (kind == PK_ZR2C || kind == PK_ZC2R) {
+    const auto& a = *static_cast<const ContigArgs*>(args);
+    t = kind == PK_ZR2C ? tiles_zr2c_f32_g0(L, a) : tiles_zc2r_f32_g0(L, a);
+    if (t < 0) t = kind == PK_ZR2C ? tiles_zr2c_f32_g1(L, a) : tiles_zc2r_f32_g1(L, a);
+  }
+  return t;
+}
+
+bool launch_grouped(int kind, int L, int mode, const void* tab, const long long* starts, int ntasks, long long grid,
+                    cudaStream_t s) {
+  if (kind == PK_STRIDED) {
+    const auto* t = static_cast<const StridedArgs*>(tab);
+    return launch_strided_grouped_f32_g0(L, mode, t, starts, ntasks, grid, s) ||
+           launch_strided_grouped_f32_g1(L, mode, t, starts, ntasks, grid, s);
+  }
+  const auto* t = static_cast<const ContigArgs*>(tab);
+  if (kind == PK_ZR2C)
+    return launch_zr2c_grouped_f32_g0(L, t, starts, ntasks, grid, s) ||
+           launch_zr2c_grouped_f32_g1(L, t, starts, ntasks, grid, s);
+  if (kind == PK_ZC2R)
+    return launch_zc2r_grouped_f32_g0(L, t, starts, ntasks, grid, s) ||
+           launch_zc2r_grouped_f32_g1(L, t, starts, ntasks, grid, s);
+  return false;
+}
+
 }  // namespace afg

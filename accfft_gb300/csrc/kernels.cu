@@ -92,6 +92,56 @@ bool AFG_NAME(int L, int mode, const StridedArgs& a, cudaStream_t s) {
   }
 #endif
 }
+#if AFG_PREC == 0
+// grouped launches (float, lengths up to 256, modes 0 and 1): the batches'
+// passes; tiles per task are ceil(ncols / TC)
+template <int L>
+static long long tiles_strided(const StridedArgs& a) {
+  return (a.ncols + StridedShape<Real, L>::TC - 1) / StridedShape<Real, L>::TC;
+}
+template <int L, int MODE>
+static bool run_strided_grouped(const StridedArgs* tab, const long long* starts, int ntasks, long long grid,
+                                cudaStream_t s) {
+  typedef StridedShape<Real, L> SH;
+  auto k = k_strided_grouped<Real, L, MODE>;
+  static PerDevice prepared;
+  if (!prepare_smem(prepared, k, SH::smem)) return false;
+  return launch_pass(k, unsigned(grid), SH::threads, SH::smem, s, tab, starts, ntasks, int(pdl_mode() == 2)) ==
+         cudaSuccess;
+}
+// lengths above 256 have no grouped kernel (kept out of the build)
+template <int L>
+static long long tiles_strided_if(const StridedArgs& a) {
+  if constexpr (L <= 256) return tiles_strided<L>(a);
+  else return -1;
+}
+template <int L>
+static bool run_strided_grouped_if(int mode, const StridedArgs* tab, const long long* starts, int ntasks,
+                                   long long grid, cudaStream_t s) {
+  if constexpr (L <= 256) {
+    if (mode == 0) return run_strided_grouped<L, 0>(tab, starts, ntasks, grid, s);
+    if (mode == 1) return run_strided_grouped<L, 1>(tab, starts, ntasks, grid, s);
+  }
+  return false;
+}
+long long AFG_CAT4(tiles_strided, AFG_P, AFG_G)(int L, const StridedArgs& a) {
+  switch (L) {
+#define AFG_CASE(n) case n: return tiles_strided_if<n>(a);
+    AFG_LIST(AFG_CASE)
+#undef AFG_CASE
+    default: return -1;
+  }
+}
+bool AFG_CAT4(launch_strided_grouped, AFG_P, AFG_G)(int L, int mode, const StridedArgs* tab, const long long* starts,
+                                                    int ntasks, long long grid, cudaStream_t s) {
+  switch (L) {
+#define AFG_CASE(n) case n: return run_strided_grouped_if<n>(mode, tab, starts, ntasks, grid, s);
+    AFG_LIST(AFG_CASE)
+#undef AFG_CASE
+    default: return false;
+  }
+}
+#endif
 #else
 // float z c2r tiles of 256-point (and longer) half lines hold half the
 // default lines per CTA (more, smaller CTAs per SM: measured 5 % faster at
@@ -106,7 +156,7 @@ constexpr int contig_tl() {
 }
 
 template <int L, bool ACC = false>
-static void run_contig(const ContigArgs& a, cudaStream_t s) {
+static bool run_contig(const ContigArgs& a, cudaStream_t s) {
   typedef ContigShape<Real, L, 0, contig_tl<L>()> SH;
 #if AFG_KIND == 1
   auto k = k_zc2c<Real, L>;
@@ -119,27 +169,90 @@ static void run_contig(const ContigArgs& a, cudaStream_t s) {
 #endif
   static PerDevice prepared;   // per instantiation, per device
   prepare_smem(prepared, k, SH::smem);
-  unsigned grid = unsigned((a.nlines + SH::TL - 1) / SH::TL);
+  // pair mode (k_zr2c / k_zc2r): TL/2 mirror pairs per CTA
+  const long long per = a.pair_n1 > 0 ? SH::TL / 2 : SH::TL;
+  const long long units = a.pair_n1 > 0 ? a.nlines / 2 : a.nlines;
+  if (per < 1) return false;
+  unsigned grid = unsigned((units + per - 1) / per);
   ContigArgs b = a;
   b.early_trigger = pdl_mode() == 2;
   launch_pass(k, grid, SH::threads, SH::smem, s, b);
+  return true;
 }
 bool AFG_NAME(int L, const ContigArgs& a, cudaStream_t s) {
   switch (L) {
 #if AFG_KIND == 4
 #define AFG_CASE(n)                                   \
   case n:                                             \
-    if (a.acc) run_contig<n, true>(a, s);             \
-    else run_contig<n, false>(a, s);                  \
-    return true;
+    return a.acc ? run_contig<n, true>(a, s) : run_contig<n, false>(a, s);
 #else
-#define AFG_CASE(n) case n: run_contig<n>(a, s); return true;
+#define AFG_CASE(n) case n: return run_contig<n>(a, s);
 #endif
     AFG_LIST(AFG_CASE)
 #undef AFG_CASE
     default: return false;
   }
 }
+#if AFG_PREC == 0 && (AFG_KIND == 2 || AFG_KIND == 3)
+// grouped launches (float z r2c / c2r, half lengths up to 256): tiles per
+// task are ceil(nlines / TL), or ceil(pairs / (TL / 2)) in pair mode
+template <int L>
+static long long tiles_contig(const ContigArgs& a) {
+  constexpr int TL = ContigShape<Real, L, 0, contig_tl<L>()>::TL;
+  const long long per = a.pair_n1 > 0 ? TL / 2 : TL;
+  const long long units = a.pair_n1 > 0 ? a.nlines / 2 : a.nlines;
+  return per < 1 ? -1 : (units + per - 1) / per;
+}
+template <int L>
+static bool run_contig_grouped(const ContigArgs* tab, const long long* starts, int ntasks, long long grid,
+                               cudaStream_t s) {
+  typedef ContigShape<Real, L, 0, contig_tl<L>()> SH;
+#if AFG_KIND == 2
+  auto k = k_zr2c_grouped<Real, L>;
+#else
+  auto k = k_zc2r_grouped<Real, L, contig_tl<L>()>;
+#endif
+  static PerDevice prepared;
+  if (!prepare_smem(prepared, k, SH::smem)) return false;
+  return launch_pass(k, unsigned(grid), SH::threads, SH::smem, s, tab, starts, ntasks, int(pdl_mode() == 2)) ==
+         cudaSuccess;
+}
+template <int L>
+static long long tiles_contig_if(const ContigArgs& a) {
+  if constexpr (L <= 256) return tiles_contig<L>(a);
+  else return -1;
+}
+template <int L>
+static bool run_contig_grouped_if(const ContigArgs* tab, const long long* starts, int ntasks, long long grid,
+                                  cudaStream_t s) {
+  if constexpr (L <= 256) return run_contig_grouped<L>(tab, starts, ntasks, grid, s);
+  else return false;
+}
+#if AFG_KIND == 2
+#define AFG_GL launch_zr2c_grouped
+#define AFG_GT tiles_zr2c
+#else
+#define AFG_GL launch_zc2r_grouped
+#define AFG_GT tiles_zc2r
+#endif
+long long AFG_CAT4(AFG_GT, AFG_P, AFG_G)(int L, const ContigArgs& a) {
+  switch (L) {
+#define AFG_CASE(n) case n: return tiles_contig_if<n>(a);
+    AFG_LIST(AFG_CASE)
+#undef AFG_CASE
+    default: return -1;
+  }
+}
+bool AFG_CAT4(AFG_GL, AFG_P, AFG_G)(int L, const ContigArgs* tab, const long long* starts, int ntasks, long long grid,
+                                    cudaStream_t s) {
+  switch (L) {
+#define AFG_CASE(n) case n: return run_contig_grouped_if<n>(tab, starts, ntasks, grid, s);
+    AFG_LIST(AFG_CASE)
+#undef AFG_CASE
+    default: return false;
+  }
+}
+#endif
 #endif
 
 }  // namespace afg

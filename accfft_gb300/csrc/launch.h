@@ -32,6 +32,29 @@ AFG_DECL_LAUNCHERS(f64, g1)
 AFG_DECL_LAUNCHERS(fdf, g0)   // double-float: no zsym, strided mode 0 only
 AFG_DECL_LAUNCHERS(fdf, g1)
 
+// grouped launches (float; lengths up to 256): one grid over the tiles of
+// ntasks independent tasks whose arguments are tab[0..ntasks) in device
+// memory, task k owning CTAs [starts[k], starts[k+1]), grid CTAs in all.
+// tiles_* give a task's CTA count (-1: no grouped kernel for the length).
+long long tiles_strided_f32_g0(int L, const StridedArgs& a);
+long long tiles_strided_f32_g1(int L, const StridedArgs& a);
+long long tiles_zr2c_f32_g0(int M, const ContigArgs& a);
+long long tiles_zr2c_f32_g1(int M, const ContigArgs& a);
+long long tiles_zc2r_f32_g0(int M, const ContigArgs& a);
+long long tiles_zc2r_f32_g1(int M, const ContigArgs& a);
+bool launch_strided_grouped_f32_g0(int L, int mode, const StridedArgs* tab, const long long* starts, int ntasks,
+                                   long long grid, cudaStream_t s);
+bool launch_strided_grouped_f32_g1(int L, int mode, const StridedArgs* tab, const long long* starts, int ntasks,
+                                   long long grid, cudaStream_t s);
+bool launch_zr2c_grouped_f32_g0(int M, const ContigArgs* tab, const long long* starts, int ntasks, long long grid,
+                                cudaStream_t s);
+bool launch_zr2c_grouped_f32_g1(int M, const ContigArgs* tab, const long long* starts, int ntasks, long long grid,
+                                cudaStream_t s);
+bool launch_zc2r_grouped_f32_g0(int M, const ContigArgs* tab, const long long* starts, int ntasks, long long grid,
+                                cudaStream_t s);
+bool launch_zc2r_grouped_f32_g1(int M, const ContigArgs* tab, const long long* starts, int ntasks, long long grid,
+                                cudaStream_t s);
+
 // arithmetic of a plan's kernels (the arrays are float for PREC_F32, IEEE
 // double for the other two)
 enum Prec { PREC_F32 = 0, PREC_F64 = 1, PREC_DF = 2 };
@@ -70,6 +93,12 @@ bool launch_df_scan(const void* x, long long rows, long long len, long long stri
 // (reals of the plan's precision), on stream s
 bool launch_add_rows(bool dbl, void* out, long long out_row, const void* in, long long in_row, long long rows,
                      int len, cudaStream_t s);
+
+// pass kinds of a recorded batch task (plan.cpp) and their grouped launch
+enum PassKind { PK_STRIDED = 0, PK_ZR2C = 2, PK_ZC2R = 3 };
+long long grouped_tiles(int kind, int L, const void* args);
+bool launch_grouped(int kind, int L, int mode, const void* tab, const long long* starts, int ntasks, long long grid,
+                    cudaStream_t s);
 
 // number of kernel launches issued by this process through the launchers
 unsigned long long launch_count();

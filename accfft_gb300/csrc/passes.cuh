@@ -403,11 +403,64 @@ __device__ __forceinline__ V c2r_merge(V xk, V xm, V wc) {
   return c_make<V>(s.x - wd.y, s.y + wd.x);
 }
 
+// Mirror pairs of the packed pass order.  Pair q of the z lines of an
+// [n0][n1] grid: for q < xc*n1 (xc = (n0-1)/2) line (x, y) = (1 + q/n1, q%n1)
+// with its mirror (n0-x, (n1-y)%n1) in another x-slab; the rest pair lines
+// within slab 0 and, for even n0, slab n0/2: (x, y) with (x, (n1-y)%n1) for
+// y = 0..n1/2 (y = 0, and y = n1/2 for even n1, are their own mirror).
+// Pairs in all: xc*n1 + (1 + (n0 even)) * (n1/2 + 1).
+__device__ __forceinline__ void pair_lines(long long q, int n0, int n1, long long& i, long long& j) {
+  const long long xc = (n0 - 1) / 2;
+  long long x, y, xm;
+  if (q < xc * n1) {
+    x = 1 + q / n1;
+    y = q % n1;
+    xm = n0 - x;
+  } else {
+    const long long r = q - xc * n1, per = n1 / 2 + 1;
+    x = (r / per) * (n0 / 2);
+    y = r % per;
+    xm = x;
+  }
+  i = x * n1 + y;
+  j = xm * n1 + (n1 - y) % n1;
+}
+
+// Line of a contiguous-pass slot: the plain mapping (slot li of tile ->
+// line tile*TL + li) or, in pair mode, the slots (2m, 2m+1) of a CTA hold
+// pair tile*(TL/2) + m, first line and mirror (an odd TL leaves its last
+// slot idle).  wr: this slot stores (a self-mirror pair stores once).
+template <int TL>
+struct ContigSlot {
+  long long row;
+  bool valid, wr;
+  int partner;   // slot holding the mirror line (the slot itself in plain mode)
+  __device__ __forceinline__ ContigSlot(const ContigArgs& a, long long tile, int li) {
+    if (a.pair_n1 > 0) {
+      constexpr int PP = TL / 2;
+      const long long q = tile * PP + (li >> 1);
+      valid = li < 2 * PP && q < a.nlines / 2;
+      long long i = 0, j = 0;
+      pair_lines(valid ? q : 0, a.pair_n0, a.pair_n1, i, j);
+      row = (li & 1) ? j : i;
+      wr = valid && !((li & 1) && i == j);
+      partner = li ^ 1;
+    } else {
+      const long long line = tile * TL + li;
+      valid = wr = line < a.nlines;
+      row = valid ? line : 0;
+      partner = li;
+    }
+  }
+};
+
 template <typename T, int M, int EF = 0, int TLF = 0>
 __device__ __forceinline__ void zr2c_tile(const ContigArgs& a, long long tile) {
   AFG_CONTIG_PROLOGUE(M)
-  const MC* in = reinterpret_cast<const MC*>(static_cast<const MR*>(a.in) + ls * a.in_dist);
-  MC* out = static_cast<MC*>(a.out) + ls * a.out_dist;
+  const ContigSlot<TL> slot(a, tile, li);
+  const V* sp = sm + slot.partner * SH::LP;   // the mirror line's spectrum (pair mode), else this line's
+  const MC* in = reinterpret_cast<const MC*>(static_cast<const MR*>(a.in) + slot.row * a.in_dist);
+  MC* out = static_cast<MC*>(a.out) + slot.row * a.out_dist;
   auto ld = [&](int p) { return to_reg<T>(sh, in[p]); };
   LN::template run<true, false>(t, static_cast<const V*>(a.tw), ld, xw, xw, xr);
   __syncthreads();
@@ -417,15 +470,18 @@ __device__ __forceinline__ void zr2c_tile(const ContigArgs& a, long long tile) {
 #pragma unroll
   for (int r = 0; r < LN::E; ++r) {
     const int k = t + r * P;
-    V x = r2c_split(xr(k), xr(k == 0 ? 0 : M - k), ld_tw(twp + k));
+    V x = r2c_split(xr(k), sp[SH::pad(k == 0 ? 0 : M - k)], ld_tw(twp + k));
     if (k != 0) x = c_scale(x, wint);
-    if (valid) out[k] = to_mem<T>(sh, x);
+    if (slot.wr) out[k] = to_mem<T>(sh, x);
   }
   if (t == 0) {
-    V z0 = xr(0);
-    V xn = c_make<V>(z0.x - z0.y, T(0));
-    if (valid) {
-      if (a.nyq_out) static_cast<MC*>(a.nyq_out)[ls] = to_mem<T>(sh, xn);
+    // X[M] = r2c_split(Z[0], Zmirror[0], -1)
+    const V z0 = xr(0), zp = sp[SH::pad(0)];
+    const V xn = a.pair_n1 > 0
+                     ? c_make<V>(T(0.5) * ((z0.x + zp.x) - (z0.y + zp.y)), T(0.5) * ((z0.y - zp.y) + (z0.x - zp.x)))
+                     : c_make<V>(z0.x - z0.y, T(0));
+    if (slot.wr) {
+      if (a.nyq_out) static_cast<MC*>(a.nyq_out)[slot.row] = to_mem<T>(sh, xn);
       else out[M] = to_mem<T>(sh, xn);
     }
   }
@@ -442,8 +498,11 @@ k_zr2c(const ContigArgs a) {
 template <typename T, int M, int EF = 0, int TLF = 0, bool CG = false>
 __device__ __forceinline__ void zc2r_tile(const ContigArgs& a, long long tile) {
   AFG_CONTIG_PROLOGUE(M)
-  const MC* in = static_cast<const MC*>(a.in) + ls * a.in_dist;
-  MC* out = reinterpret_cast<MC*>(static_cast<MR*>(a.out) + ls * a.out_dist);
+  const ContigSlot<TL> slot(a, tile, li);
+  const long long ls2 = slot.row;
+  const V* sp = sm + slot.partner * SH::LP;   // the mirror line's entries (pair mode), else this line's
+  const MC* in = static_cast<const MC*>(a.in) + ls2 * a.in_dist;
+  MC* out = reinterpret_cast<MC*>(static_cast<MR*>(a.out) + ls2 * a.out_dist);
   {
     // stage the M+1 input entries: E independent loads per thread, then the
     // Nyquist entry by thread 0
@@ -456,7 +515,7 @@ __device__ __forceinline__ void zc2r_tile(const ContigArgs& a, long long tile) {
     } else {
 #pragma unroll
       for (int r = 0; r < LN::E; ++r) v[r] = to_reg<T>(sh, in[t + r * P]);
-      nyq = to_reg<T>(sh, a.nyq_in ? static_cast<const MC*>(a.nyq_in)[ls] : in[t == 0 ? M : 0]);
+      nyq = to_reg<T>(sh, a.nyq_in ? static_cast<const MC*>(a.nyq_in)[ls2] : in[t == 0 ? M : 0]);
     }
 #pragma unroll
     for (int r = 0; r < LN::E; ++r) xw(t + r * P, v[r]);
@@ -465,18 +524,25 @@ __device__ __forceinline__ void zc2r_tile(const ContigArgs& a, long long tile) {
   __syncthreads();
   const V* twp = static_cast<const V*>(a.tw_post);
   const T wint = a.weight == 1 ? T(0.5) : T(1);
+  // X[k] of this line with X[M-k] of the mirror line (this line in plain
+  // mode).  k = 0 and k = M enter as the Hermitian parts over the pair,
+  // H[k] = (X[k] + conj Xmirror[k]) / 2 (the merge takes conj H[M] as its
+  // second argument): the real part of a line that is its own mirror, which
+  // is what the reference's c2r reads there (x and y inverse passes first,
+  // then the imaginary parts of kz = 0 and N2/2 dropped).
   auto ld = [&](int p) {
-    V xk = xr(p), xm = xr(M - p);
+    V xk = xr(p), xm = sp[SH::pad(M - p)];
     if (p == 0) {
-      xk.y = T(0);
-      xm.y = T(0);
+      const V xp = sp[SH::pad(0)], xn = xr(M);
+      xk = c_make<V>(T(0.5) * (xk.x + xp.x), T(0.5) * (xk.y - xp.y));
+      xm = c_make<V>(T(0.5) * (xn.x + xm.x), T(0.5) * (xm.y - xn.y));
     } else {
       xk = c_scale(xk, wint);
       xm = c_scale(xm, wint);
     }
     return c_conj(c2r_merge(xk, xm, c_conj(ld_tw(twp + p))));
   };
-  auto st = [&](int p, V x) { x.y = -x.y; if (valid) out[p] = to_mem<T>(sh, x); };
+  auto st = [&](int p, V x) { x.y = -x.y; if (slot.wr) out[p] = to_mem<T>(sh, x); };
   LN::template run<false, true>(t, static_cast<const V*>(a.tw), ld, st, xw, xr);
 }
 
@@ -485,6 +551,45 @@ __global__ void __launch_bounds__(ContigShape<T, M, EF, TLF>::threads)
 k_zc2r(const ContigArgs a) {
   PassScope scope(a.early_trigger);
   zc2r_tile<T, M, EF, TLF>(a, blockIdx.x);
+}
+
+// ------------------------------------------------------- grouped launches
+// One grid over the tiles of several independent tasks of one line length
+// (the same pass of many transforms of a batch): task k owns the CTAs
+// [starts[k], starts[k+1]) and reads its arguments from tab[k] in global
+// memory.  The tile bodies are the single-task kernels'.
+__device__ __forceinline__ int group_task(const long long* __restrict__ starts, int ntasks, long long b) {
+  int lo = 0, hi = ntasks - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (__ldg(starts + mid) <= b) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+template <typename T, int L, int MODE>
+__global__ void __launch_bounds__(StridedShape<T, L>::threads, (strided_min_blocks<T, L, 0, 0>()))
+k_strided_grouped(const StridedArgs* __restrict__ tab, const long long* __restrict__ starts, int ntasks, int early) {
+  PassScope scope(early);
+  const int k = group_task(starts, ntasks, blockIdx.x);
+  strided_tile<T, L, MODE>(tab[k], blockIdx.x - __ldg(starts + k));
+}
+
+template <typename T, int M>
+__global__ void __launch_bounds__(ContigShape<T, M>::threads)
+k_zr2c_grouped(const ContigArgs* __restrict__ tab, const long long* __restrict__ starts, int ntasks, int early) {
+  PassScope scope(early);
+  const int k = group_task(starts, ntasks, blockIdx.x);
+  zr2c_tile<T, M>(tab[k], blockIdx.x - __ldg(starts + k));
+}
+
+template <typename T, int M, int TLF = 0>
+__global__ void __launch_bounds__(ContigShape<T, M, 0, TLF>::threads)
+k_zc2r_grouped(const ContigArgs* __restrict__ tab, const long long* __restrict__ starts, int ntasks, int early) {
+  PassScope scope(early);
+  const int k = group_task(starts, ntasks, blockIdx.x);
+  zc2r_tile<T, M, 0, TLF>(tab[k], blockIdx.x - __ldg(starts + k));
 }
 
 // real line r2c -> i k / N -> c2r, one pass (z-direction derivative: the

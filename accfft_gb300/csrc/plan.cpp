@@ -16,6 +16,8 @@
 #include <algorithm>
 #include <map>
 #include <string>
+#include <deque>
+#include <tuple>
 #include <vector>
 
 #include "../../include/accfft_gb300.h"
@@ -44,6 +46,8 @@ int fail(int code, const char* fmt, ...) {
 int cuda_fail(cudaError_t e, const char* what) {
   return fail(ACCFFT_C_ECUDA, "%s: %s", what, cudaGetErrorString(e));
 }
+
+bool packed_eligible(const accfft_c_plan* p);
 
 // polls a bounded device-side wait makes before it gives up
 // (accfft_c_set_wait_limit); the default is about half a second
@@ -106,6 +110,14 @@ constexpr unsigned XB = 1, YB = 2, ZB = 4;
 
 }  // namespace
 
+// one pass of a plan recorded into a batch (accfft_c_batch_record): the
+// kernel kind (afg::PassKind), line length, strided mode and arguments
+struct PassRecord {
+  int kind = 0, L = 0, mode = 0;
+  afg::StridedArgs s{};
+  afg::ContigArgs c{};
+};
+
 struct accfft_c_plan {
   int kind = 0;         // 1 = r2c, 2 = c2c
   bool dbl = false;
@@ -131,6 +143,16 @@ struct accfft_c_plan {
   // is still in L2 when the next pass reads it)
   int zy_mode = 0;
   int zy_batches = 1;
+  // packed pass order of full r2c / c2r transforms of device arrays
+  // (accfft_c_set_pass_order): y and x passes over the real field viewed as
+  // complex [N0][N1][N2/2] (rows of a multiple of 128 bytes for the usual
+  // sizes) in the plan scratch, then one z pass over mirror-paired lines that
+  // finishes the real transform and writes the natural spectrum in whole
+  // rows; c2r runs the same passes backwards.  Out-of-place float and double
+  // plans only.
+  bool packed = false;
+  // record mode: the plan's passes are appended here instead of launched
+  std::vector<PassRecord>* recording = nullptr;
   cudaStream_t stream2 = nullptr;
   static constexpr int kMaxBatches = 64;
   // control words of the persistent z+y kernels (1 + N0, zeroed per launch)
@@ -364,6 +386,9 @@ accfft_c_plan* make_plan(int kind, bool dbl, const int* n, void* data, void* dat
     // ACCFFT_GB300_ZY = fused | batch<n> selects an alternative z+y schedule
     // for device-resident data (both measured slower on GB300 than the
     // default whole-grid passes; kept for comparison)
+    // ACCFFT_GB300_ORDER = packed | natural: the pass order of full transforms
+    const char* ord = getenv("ACCFFT_GB300_ORDER");
+    p->packed = packed_eligible(p) && ord && std::string(ord) == "packed";
     const char* env = getenv("ACCFFT_GB300_ZY");
     std::string zy = env ? env : "";
     if (zy == "fused" && slab_available(dbl, n[1], n[2])) {
@@ -425,9 +450,45 @@ struct Exec {
   int weight = 0;   // adjoint weighting of the z passes (ContigArgs::weight)
 
   Exec(accfft_c_plan* plan, double* t) : guard(plan->device), p(plan), timer(t) {
-    if (p->blocking || timer) cudaEventRecord(p->ev0, p->stream);
+    if ((p->blocking || timer) && !p->recording) cudaEventRecord(p->ev0, p->stream);
   }
   bool ok() const { return rc == ACCFFT_C_OK; }
+  // launch, or append to the batch the plan is recording into (float passes
+  // with a grouped kernel only: strided modes 0 and 1, z r2c and z c2r)
+  bool record(int kind, int L, int mode, const StridedArgs* sa, const ContigArgs* ca) {
+    PassRecord r;
+    r.kind = kind;
+    r.L = L;
+    r.mode = mode;
+    if (sa) r.s = *sa;
+    if (ca) r.c = *ca;
+    const void* args = sa ? static_cast<const void*>(&r.s) : static_cast<const void*>(&r.c);
+    if ((kind == PK_STRIDED && mode > 1) || grouped_tiles(kind, L, args) < 0) {
+      if (ok()) rc = fail(ACCFFT_C_EUNSUPPORTED, "batch: pass of length %d has no grouped kernel "
+                          "(float plain and symbol passes of lengths up to 256)", L);
+      return true;
+    }
+    p->recording->push_back(r);
+    return true;
+  }
+  bool go_strided(int L, int mode, const StridedArgs& a, cudaStream_t st) {
+    if (p->recording) return record(PK_STRIDED, L, mode, &a, nullptr);
+    return launch_strided(p->prec(), L, mode, a, st);
+  }
+  bool go_zr2c(int M, const ContigArgs& a, cudaStream_t st) {
+    if (p->recording) return record(PK_ZR2C, M, 0, nullptr, &a);
+    return launch_zr2c(p->prec(), M, a, st);
+  }
+  bool go_zc2r(int M, const ContigArgs& a, cudaStream_t st) {
+    if (p->recording) return record(PK_ZC2R, M, 0, nullptr, &a);
+    return launch_zc2r(p->prec(), M, a, st);
+  }
+  // kernels a batch cannot record: the call fails while the plan records
+  bool not_recordable(const char* what) {
+    if (!p->recording) return false;
+    if (ok()) rc = fail(ACCFFT_C_EUNSUPPORTED, "batch: %s cannot be recorded into a batch", what);
+    return true;
+  }
   // double-float plans: the largest exponent of the transform's input (rows
   // of len doubles, stride apart), read by every pass of the transform
   void df_scan(const void* x, long long rows, long long len, long long stride) {
@@ -438,7 +499,7 @@ struct Exec {
   // run one launcher; with profiling on, bracket it with CUDA events on its stream
   template <class F>
   bool timed(const char* label, cudaStream_t st, F&& launch) {
-    if (!p->profile) return launch();
+    if (!p->profile || p->recording) return launch();
     size_t k = p->pending.size();
     if (k >= 512) {   // fold before the event pool grows further
       fold_profile(p);
@@ -486,7 +547,7 @@ struct Exec {
     a.wait_limit = g_wait_limit.load();
     if (p->tc) p->waits_used = true;
     if (!timed(tw == p->tw_x ? (inverse ? "x_inv" : "x") : (inverse ? "y_inv" : "y"), p->stream, [&] {
-          return p->tc ? launch_strided_tc(p->tc, L, a, p->wait_err, p->stream) : launch_strided(p->prec(), L, 0, a, p->stream);
+          return p->tc ? launch_strided_tc(p->tc, L, a, p->wait_err, p->stream) : go_strided(L, 0, a, p->stream);
         }))
       unsupported("strided pass", L);
   }
@@ -505,7 +566,7 @@ struct Exec {
     a.in_line = a.out_line = line;
     a.sym = sym;
     const int mode = acc ? 4 : 1;   // fused pass, with the accumulate input when given
-    if (!timed(label, p->stream, [&] { return launch_strided(p->prec(), L, mode, a, p->stream); }))
+    if (!timed(label, p->stream, [&] { return go_strided(L, mode, a, p->stream); }))
       unsupported("symbol pass", L);
   }
   // y pass over an [N0][N1][h] complex array, x pass over [N0][N1*h]
@@ -532,7 +593,7 @@ struct Exec {
     if (p->tc) p->waits_used = true;
     if (!timed("z_r2c", p->stream, [&] {
           return p->tc ? launch_z_tc(p->tc, true, p->M(), a, p->wait_err, p->stream)
-                       : launch_zr2c(p->prec(), p->M(), a, p->stream);
+                       : go_zr2c(p->M(), a, p->stream);
         }))
       unsupported("z r2c pass", p->M());
   }
@@ -552,13 +613,49 @@ struct Exec {
     if (p->tc) p->waits_used = true;
     if (!timed("z_c2r", p->stream, [&] {
           return p->tc ? launch_z_tc(p->tc, false, p->M(), a, p->wait_err, p->stream)
-                       : launch_zc2r(p->prec(), p->M(), a, p->stream);
+                       : go_zc2r(p->M(), a, p->stream);
         }))
       unsupported("z c2r pass", p->M());
   }
+  // z passes of the packed order: complex lines of M (the packed real field,
+  // dense rows) taken in mirror pairs <-> the natural half spectrum
+  long long mirror_pairs() const {
+    const long long n0 = p->n[0], n1 = p->n[1];
+    return (n0 - 1) / 2 * n1 + (1 + (n0 % 2 == 0)) * (n1 / 2 + 1);
+  }
+  void zr2c_pairs(const void* in, void* out) {
+    if (!ok()) return;
+    ContigArgs a{};
+    a.in = in;
+    a.out = out;
+    a.tw = p->tw_z;
+    a.tw_post = p->tw_post;
+    a.nlines = 2 * mirror_pairs();
+    a.in_dist = 2LL * p->M();
+    a.out_dist = p->H2();
+    a.pair_n0 = p->n[0];
+    a.pair_n1 = p->n[1];
+    if (!timed("z_r2c", p->stream, [&] { return go_zr2c(p->M(), a, p->stream); }))
+      unsupported("z r2c pass (mirror pairs)", p->M());
+  }
+  void zc2r_pairs(const void* in, void* out) {
+    if (!ok()) return;
+    ContigArgs a{};
+    a.in = in;
+    a.out = out;
+    a.tw = p->tw_z;
+    a.tw_post = p->tw_post;
+    a.nlines = 2 * mirror_pairs();
+    a.in_dist = p->H2();
+    a.out_dist = 2LL * p->M();
+    a.pair_n0 = p->n[0];
+    a.pair_n1 = p->n[1];
+    if (!timed("z_c2r", p->stream, [&] { return go_zc2r(p->M(), a, p->stream); }))
+      unsupported("z c2r pass (mirror pairs)", p->M());
+  }
   // out[r][c] += in[r][c] over the plan's N0*N1 real rows
   void add_rows(void* out, long long out_row, const void* in, long long in_row, long long rows, int len) {
-    if (!ok()) return;
+    if (!ok() || not_recordable("the row accumulation of divergence_slow")) return;
     if (!timed("add", p->stream, [&] { return launch_add_rows(p->dbl, out, out_row, in, in_row, rows, len, p->stream); }))
       rc = fail(ACCFFT_C_ECUDA, "row accumulation: launch failed");
   }
@@ -577,7 +674,7 @@ struct Exec {
     a.nlines = ns * N1;
     a.in_dist = in_row;
     a.out_dist = p->H2();
-    if (!timed("z_r2c", st, [&] { return launch_zr2c(p->prec(), p->M(), a, st); })) unsupported("z r2c pass", p->M());
+    if (!timed("z_r2c", st, [&] { return go_zr2c(p->M(), a, st); })) unsupported("z r2c pass", p->M());
   }
   void zc2r_slabs(const void* in, void* out, long long out_row, long long s0, long long ns, cudaStream_t st) {
     if (!ok()) return;
@@ -592,7 +689,7 @@ struct Exec {
     a.nlines = ns * N1;
     a.in_dist = p->H2();
     a.out_dist = out_row;
-    if (!timed("z_c2r", st, [&] { return launch_zc2r(p->prec(), p->M(), a, st); })) unsupported("z c2r pass", p->M());
+    if (!timed("z_c2r", st, [&] { return go_zc2r(p->M(), a, st); })) unsupported("z c2r pass", p->M());
   }
   void ypass_slabs(const void* in, void* out, int inverse, long long s0, long long ns, cudaStream_t st) {
     if (!ok()) return;
@@ -608,7 +705,7 @@ struct Exec {
     a.in_slab = a.out_slab = N1 * h;
     a.in_line = a.out_line = h;
     a.inverse = inverse;
-    if (!timed(inverse ? "y_inv" : "y", st, [&] { return launch_strided(p->prec(), p->n[1], 0, a, st); }))
+    if (!timed(inverse ? "y_inv" : "y", st, [&] { return go_strided(p->n[1], 0, a, st); }))
       unsupported("strided pass", p->n[1]);
   }
   // z r2c then y forward (forward = true), or y backward then z c2r, over
@@ -717,6 +814,7 @@ struct Exec {
   // Host-to-device and device-to-host copies use separate engines, so an
   // r2c on one plan overlaps a c2r on another.
   void zy_host(bool forward, const void* in, void* mid, void* out, long long row) {
+    if (not_recordable("a pinned-host array")) return;
     if (!ok()) return;
     const long long N0 = p->n[0], N1 = p->n[1];
     const int nb = (int)std::min<long long>(N0, p->host_batches);
@@ -784,7 +882,7 @@ struct Exec {
     if (e != cudaSuccess) rc = cuda_fail(e, "execute: host copy");
   }
   void zc2c(const void* in, void* out, int inverse) {
-    if (!ok()) return;
+    if (!ok() || not_recordable("a z c2c pass")) return;
     ContigArgs a{};
     a.dfx = p->df_exp;
     a.in = in;
@@ -797,7 +895,7 @@ struct Exec {
       unsupported("z c2c pass", p->n[2]);
   }
   void zsym(const void* in, void* out, const void* acc, long long row, const SymArgs& sym) {
-    if (!ok()) return;
+    if (!ok() || not_recordable("a z derivative pass")) return;
     ContigArgs a{};
     a.dfx = p->df_exp;
     a.in = in;
@@ -862,7 +960,7 @@ struct Exec {
     } else {
       a.in_slab = spec_slab; a.in_line = spec_line; a.out_slab = real_slab; a.out_line = real_line;
     }
-    if (!timed(axis == 0 ? "x_real" : "y_real", p->stream, [&] { return launch_strided(p->prec(), L, mode, a, p->stream); }))
+    if (!timed(axis == 0 ? "x_real" : "y_real", p->stream, [&] { return go_strided(L, mode, a, p->stream); }))
       unsupported("single-axis pass", L);
   }
   // ---- passes through the aligned intermediate layout (p->split)
@@ -883,7 +981,7 @@ struct Exec {
     a.nlines = (long long)p->n[0] * p->n[1];
     a.in_dist = in_row;
     a.out_dist = p->M();
-    if (!timed("z_r2c", p->stream, [&] { return launch_zr2c(p->prec(), p->M(), a, p->stream); }))
+    if (!timed("z_r2c", p->stream, [&] { return go_zr2c(p->M(), a, p->stream); }))
       unsupported("z r2c pass", p->M());
   }
   void zc2r_split(void* out, long long out_row) {
@@ -899,7 +997,7 @@ struct Exec {
     a.nlines = (long long)p->n[0] * p->n[1];
     a.in_dist = p->M();
     a.out_dist = out_row;
-    if (!timed("z_c2r", p->stream, [&] { return launch_zc2r(p->prec(), p->M(), a, p->stream); }))
+    if (!timed("z_c2r", p->stream, [&] { return go_zc2r(p->M(), a, p->stream); }))
       unsupported("z c2r pass", p->M());
   }
   // y lines of the main part (aligned columns) and, as extra columns of the
@@ -920,7 +1018,7 @@ struct Exec {
     a.nyq_slab = N1;
     a.nyq_line = 1;
     a.inverse = inverse;
-    if (!timed(inverse ? "y_inv" : "y", p->stream, [&] { return launch_strided(p->prec(), (int)N1, 0, a, p->stream); }))
+    if (!timed(inverse ? "y_inv" : "y", p->stream, [&] { return go_strided((int)N1, 0, a, p->stream); }))
       unsupported("strided pass", (int)N1);
   }
   // fused x pass of a 3-D operator on the split layout (in place, aligned;
@@ -942,10 +1040,11 @@ struct Exec {
     a.nyq_line = N1;
     sym.h2 = (int)M;
     a.sym = sym;
-    if (!timed("x_sym", p->stream, [&] { return launch_strided(p->prec(), p->n[0], 1, a, p->stream); }))
+    if (!timed("x_sym", p->stream, [&] { return go_strided(p->n[0], 1, a, p->stream); }))
       unsupported("symbol pass", p->n[0]);
   }
   int finish() {
+    if (p->recording) return rc;
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess && ok()) rc = cuda_fail(e, "kernel launch");
     if (p->blocking || timer) {
@@ -962,6 +1061,11 @@ struct Exec {
     return rc;
   }
 };
+
+// plans that can run the packed pass order (exec_r2c_plan)
+bool packed_eligible(const accfft_c_plan* p) {
+  return p->kind == 1 && !p->inplace && !p->tc && !p->df && p->scratch != nullptr;
+}
 
 // every array is accessed as whole complex elements (8 or 16 bytes)
 int check_align(const accfft_c_plan* p, const char* fn, std::initializer_list<const void*> ptrs) {
@@ -1040,6 +1144,25 @@ int exec_r2c_plan(accfft_c_plan* p, int direction, void* in, void* out, double* 
   }
   if (p->df && (host_in || host_out))
     return fail(ACCFFT_C_EUNSUPPORTED, "execute: double-float plans take device arrays");
+  if (p->packed && (xyz & 7) == 7 && !host_in && !host_out && weight == 0 && p->zy_mode == 0 &&
+      (direction == -1 || direction == 1)) {
+    // packed order: r2c = y, x over the packed real field (in -> scratch),
+    // then the mirror-pair z pass (scratch -> natural spectrum); c2r the
+    // reverse.  The input array is only read.
+    Exec ex(p, timer);
+    const long long M = p->M();
+    void* sc = p->scratch;
+    if (direction == -1) {
+      ex.ypass(in, sc, M, 0);
+      ex.xpass(sc, sc, M, 0);
+      ex.zr2c_pairs(sc, out);
+    } else {
+      ex.zc2r_pairs(in, sc);
+      ex.xpass(sc, sc, M, 1);
+      ex.ypass(sc, out, M, 1);
+    }
+    return ex.finish();
+  }
   Exec ex(p, timer);
   ex.weight = weight;
   const long long spec_doubles = 2LL * p->n[0] * p->n[1] * h;
@@ -1322,6 +1445,19 @@ int accfft_c_set_zy_schedule(accfft_c_plan* p, int mode) {
               "set_zy_schedule: mode must be 0 (separate passes), 1 (cluster slab kernel) or 2 (persistent z+y kernel)");
 }
 
+int accfft_c_set_pass_order(accfft_c_plan* p, int order) {
+  if (!p) return fail(ACCFFT_C_EINVAL, "set_pass_order: NULL plan");
+  if (order == 0) {
+    p->packed = false;
+    return ACCFFT_C_OK;
+  }
+  if (order != 1) return fail(ACCFFT_C_EINVAL, "set_pass_order: order must be 0 (natural) or 1 (packed)");
+  if (!packed_eligible(p))
+    return fail(ACCFFT_C_EUNSUPPORTED, "set_pass_order: the packed order needs an out-of-place float or double r2c plan");
+  p->packed = true;
+  return ACCFFT_C_OK;
+}
+
 int accfft_c_set_stream(accfft_c_plan* p, void* stream, int blocking) {
   if (!p) return fail(ACCFFT_C_EINVAL, "set_stream: NULL plan");
   p->stream = static_cast<cudaStream_t>(stream);
@@ -1534,3 +1670,160 @@ int accfft_c_poisson(accfft_c_plan* p, void* phi, const void* rho, int method, d
 }
 
 }  // extern "C"
+
+// --- batches of independent transforms (no counterpart in the reference)
+// Recorded per instance, run level by level: level k holds the k-th pass of
+// every instance, and each level launches one grouped kernel per (pass kind,
+// line length, mode) over all its instances' tiles.
+struct accfft_c_batch {
+  int device = 0;
+  std::deque<std::vector<PassRecord>> instances;   // a deque keeps recording plans' pointers valid
+  std::vector<const accfft_c_plan*> owners;   // one instance per plan
+  struct Launch {
+    int kind, L, mode, ntasks;
+    long long grid;
+    size_t tab_off, starts_off;   // bytes into dev
+  };
+  std::vector<Launch> launches;
+  std::vector<int> level_end;        // launches index where each level ends
+  void* dev = nullptr;
+  size_t dev_bytes = 0;
+  bool final = false;
+  int tasks = 0;
+};
+
+extern "C" {
+
+accfft_c_batch* accfft_c_batch_create(void) {
+  auto* b = new accfft_c_batch;
+  cudaGetDevice(&b->device);
+  return b;
+}
+
+void accfft_c_batch_destroy(accfft_c_batch* b) {
+  if (!b) return;
+  if (b->dev) {
+    DeviceGuard guard(b->device);
+    cudaFree(b->dev);
+  }
+  delete b;
+}
+
+int accfft_c_batch_record(accfft_c_batch* b, accfft_c_plan* p, int on) {
+  g_err.clear();
+  g_err_code = ACCFFT_C_OK;
+  if (!b || !p) return fail(ACCFFT_C_EINVAL, "batch_record: NULL batch or plan");
+  if (!on) {
+    if (!p->recording) return fail(ACCFFT_C_EINVAL, "batch_record: the plan is not recording");
+    p->recording = nullptr;
+    return ACCFFT_C_OK;
+  }
+  if (b->final) return fail(ACCFFT_C_EINVAL, "batch_record: the batch is finalised");
+  if (p->recording) return fail(ACCFFT_C_EINVAL, "batch_record: the plan is already recording");
+  if (p->kind != 1 || p->dbl || p->tc || p->zy_mode != 0)
+    return fail(ACCFFT_C_EUNSUPPORTED, "batch_record: batches take float r2c plans with the default z+y schedule");
+  if (p->device != b->device) return fail(ACCFFT_C_EINVAL, "batch_record: plan and batch on different devices");
+  for (const accfft_c_plan* q : b->owners)
+    if (q == p) return fail(ACCFFT_C_EINVAL, "batch_record: a plan holds one instance of a batch (its scratch is shared)");
+  b->owners.push_back(p);
+  b->instances.emplace_back();
+  p->recording = &b->instances.back();
+  return ACCFFT_C_OK;
+}
+
+int accfft_c_batch_finalize(accfft_c_batch* b) {
+  g_err.clear();
+  g_err_code = ACCFFT_C_OK;
+  if (!b) return fail(ACCFFT_C_EINVAL, "batch_finalize: NULL batch");
+  if (b->final) return ACCFFT_C_OK;
+  for (const accfft_c_plan* q : b->owners)
+    if (q->recording) return fail(ACCFFT_C_EINVAL, "batch_finalize: a plan is still recording");
+  size_t levels = 0;
+  for (auto& v : b->instances) levels = std::max(levels, v.size());
+  std::vector<unsigned char> host;
+  auto align = [&](size_t a) { host.resize((host.size() + a - 1) / a * a); };
+  b->tasks = 0;
+  for (size_t lv = 0; lv < levels; ++lv) {
+    // the level's tasks, grouped by (kind, length, mode) in first-seen order
+    std::vector<std::pair<std::tuple<int, int, int>, std::vector<const PassRecord*>>> groups;
+    for (auto& v : b->instances) {
+      if (lv >= v.size()) continue;
+      const PassRecord& r = v[lv];
+      auto key = std::make_tuple(r.kind, r.L, r.mode);
+      auto it = std::find_if(groups.begin(), groups.end(), [&](auto& g) { return g.first == key; });
+      if (it == groups.end()) {
+        groups.push_back({key, {}});
+        it = groups.end() - 1;
+      }
+      it->second.push_back(&r);
+    }
+    for (auto& g : groups) {
+      accfft_c_batch::Launch ln{};
+      std::tie(ln.kind, ln.L, ln.mode) = g.first;
+      ln.ntasks = (int)g.second.size();
+      const bool str = ln.kind == PK_STRIDED;
+      const size_t rec = str ? sizeof(StridedArgs) : sizeof(ContigArgs);
+      align(256);
+      ln.tab_off = host.size();
+      host.resize(host.size() + rec * g.second.size());
+      std::vector<long long> starts;
+      long long grid = 0;
+      for (size_t k = 0; k < g.second.size(); ++k) {
+        const PassRecord* r = g.second[k];
+        const void* args = str ? static_cast<const void*>(&r->s) : static_cast<const void*>(&r->c);
+        memcpy(&host[ln.tab_off + k * rec], args, rec);
+        const long long t = grouped_tiles(ln.kind, ln.L, args);
+        if (t < 0) return fail(ACCFFT_C_EUNSUPPORTED, "batch_finalize: no grouped kernel for length %d", ln.L);
+        starts.push_back(grid);
+        grid += t;
+      }
+      if (grid >= (1LL << 31)) return fail(ACCFFT_C_EOVERFLOW, "batch_finalize: a level needs more than 2^31 CTAs");
+      ln.grid = grid;
+      align(16);
+      ln.starts_off = host.size();
+      host.resize(host.size() + starts.size() * sizeof(long long));
+      memcpy(&host[ln.starts_off], starts.data(), starts.size() * sizeof(long long));
+      b->launches.push_back(ln);
+      b->tasks += ln.ntasks;
+    }
+    b->level_end.push_back((int)b->launches.size());
+  }
+  DeviceGuard guard(b->device);
+  if (!host.empty()) {
+    cudaError_t e = cudaMalloc(&b->dev, host.size());
+    if (e == cudaSuccess) e = cudaMemcpy(b->dev, host.data(), host.size(), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return cuda_fail(e, "batch_finalize: descriptor tables");
+    b->dev_bytes = host.size();
+  }
+  b->final = true;
+  return ACCFFT_C_OK;
+}
+
+int accfft_c_batch_run(accfft_c_batch* b, void* stream) {
+  g_err.clear();
+  g_err_code = ACCFFT_C_OK;
+  if (!b) return fail(ACCFFT_C_EINVAL, "batch_run: NULL batch");
+  if (!b->final) return fail(ACCFFT_C_ENOTBAKED, "batch_run: finalise the batch first");
+  DeviceGuard guard(b->device);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  auto* base = static_cast<unsigned char*>(b->dev);
+  for (const auto& ln : b->launches) {
+    if (!launch_grouped(ln.kind, ln.L, ln.mode, base + ln.tab_off,
+                        reinterpret_cast<const long long*>(base + ln.starts_off), ln.ntasks, ln.grid, st))
+      return fail(ACCFFT_C_ECUDA, "batch_run: grouped launch of length %d failed", ln.L);
+  }
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? ACCFFT_C_OK : cuda_fail(e, "batch_run");
+}
+
+int accfft_c_batch_info(const accfft_c_batch* b, int* instances, int* levels, int* launches, int* tasks) {
+  if (!b) return fail(ACCFFT_C_EINVAL, "batch_info: NULL batch");
+  if (instances) *instances = (int)b->instances.size();
+  if (levels) *levels = (int)b->level_end.size();
+  if (launches) *launches = (int)b->launches.size();
+  if (tasks) *tasks = b->tasks;
+  return ACCFFT_C_OK;
+}
+
+}  // extern "C"
+

@@ -68,6 +68,8 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--inflight", type=int, default=3, help="e2e: pairs in flight (plans on their own streams)")
     ap.add_argument("--dtype", default="float32", choices=["float32", "float64"])
+    ap.add_argument("--order", default="packed", choices=["packed", "natural"],
+                    help="pass order of the r2c/c2r plan (accfft_c_set_pass_order)")
     ap.add_argument("--no-baseline", action="store_true")
     ap.add_argument("--no-variants", action="store_true", help="skip the tensor-core and FP64 forms of the pair")
     return ap.parse_args()
@@ -99,14 +101,21 @@ def replicas_value(steps, world, max_ms):
     return world * steps / (max_ms / 1000.0)
 
 
-def algorithmic_bytes(n, esz):
+def algorithmic_bytes(n, esz, packed=False):
     """Bytes each kernel launch must move (its input read once, its output
-    written once), per profiling label of the plan (accfft_c_profile_read)."""
+    written once), per profiling label of the plan (accfft_c_profile_read).
+    In the packed pass order the y and x passes move the real field viewed as
+    D = N0*N1*N2/2 complex values, and the z passes D complex one way and the
+    half spectrum the other."""
     N0, N1, N2 = n
     N = N0 * N1 * N2
     M = N2 // 2
     H = N0 * N1 * (M + 1)
     c = 2 * esz
+    if packed:
+        D = N0 * N1 * M
+        return {"y": 2 * D * c, "y_inv": 2 * D * c, "x": 2 * D * c, "x_inv": 2 * D * c,
+                "z_r2c": D * c + H * c, "z_c2r": H * c + D * c}
     return {
         "z_r2c": N * esz + H * c,           # real field in, half spectrum out
         "z_c2r": H * c + N * esz,
@@ -118,11 +127,14 @@ def algorithmic_bytes(n, esz):
     }
 
 
-# dram__bytes_read.sum + dram__bytes_write.sum per launch from one ncu capture
-# of this bench (profiles/launches_512cube_f32_r2c_c2r.md); writes still in L2
-# at the end of a launch reach DRAM during the next one
+# dram__bytes_read.sum + dram__bytes_write.sum per launch, from one ncu
+# capture of this bench's own launches (the gpu__time_duration launch list
+# plus the two DRAM counters, one pass each, on the full-size workload),
+# keyed by (grid, dtype, pass order); writes still in L2 at the end of a
+# launch reach DRAM during the next one.  Re-captured whenever the kernels of
+# that configuration change.
 TRAFFIC = {
-    ((512, 512, 512), "float32"): {
+    ((512, 512, 512), "float32", "natural"): {
         "z_r2c": 537037056 + 479984384, "y": 539036672 + 480273664, "x": 539024384 + 475256320,
         "x_inv": 539027712 + 484878080, "y_inv": 539026176 + 480036096, "z_c2r": 539017728 + 481038080,
     },
@@ -437,6 +449,8 @@ def ours(args):
     N0, N1, N2 = n
     H2 = N2 // 2 + 1
     plan = ag.PlanR2C(n, dt)
+    packed = args.order == "packed"
+    plan.set_pass_order(1 if packed else 0)
     stream = torch.cuda.Stream()
     plan.set_stream(stream, blocking=False)
     g = torch.Generator(device="cuda").manual_seed(1234 + rank)
@@ -491,7 +505,7 @@ def ours(args):
     ms_step = total_ms / args.steps
     value = replicas_value(args.steps, world, total_ms)
 
-    nbytes = algorithmic_bytes(n, esz)
+    nbytes = algorithmic_bytes(n, esz, packed)
     per = {lab: tot / cnt for lab, (cnt, tot) in prof.items()}                 # ms per launch
     share = {lab: tot / args.steps for lab, (cnt, tot) in prof.items()}        # ms per step
     dom = max(share, key=share.get)
@@ -509,14 +523,14 @@ def ours(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32" if dt == "float32" else "f64",
         "data": "synthetic N(0,1), seeded",
-        "config": {"workload": f"{label} {dt} r2c+c2r round trip", "grid": list(n),
+        "config": {"workload": f"{label} {dt} r2c+c2r round trip", "grid": list(n), "pass_order": args.order,
                    "flush": "inputs_larger_than_l2", "parallelism": f"replicas{world}"},
         "gpu_launches": int(launches),
         "pdl_mode": ag.set_pdl(None),
         "profiled_ms_per_step": prof_total_ms / args.steps,
         "roofline": {"bound": "hbm", "kernel": KERNEL_OF.get(dom, dom), "pass": dom, "achieved": achieved,
                      "peak": peak, "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": TRAFFIC.get((n, dt), {}).get(dom), "bytes_per_launch": dom_bytes,
+                     "traffic": TRAFFIC.get((n, dt, args.order), {}).get(dom), "bytes_per_launch": dom_bytes,
                      "ms_per_launch": per[dom]},
         "kernel_ms_per_launch": per,
         "kernel_ms_per_step": share,

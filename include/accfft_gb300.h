@@ -140,6 +140,18 @@ int accfft_c_plan_info(const accfft_c_plan* plan, int n[3], int* kind, int* is_d
  * of a slab reads it from L2 (ACCFFT_C_EUNSUPPORTED when the grid has no
  * such kernel) */
 int accfft_c_set_zy_schedule(accfft_c_plan* plan, int mode);
+/* extension: pass order of full r2c / c2r transforms (xyz = 111) of device
+ * arrays.  0 = the reference's order (src/accfft_gpu.cpp:470-603): z r2c,
+ * then y and x passes on the [N0][N1][N2/2+1] spectrum, whose rows of N2/2+1
+ * complex are not 16-byte aligned.  1 = packed: the y and x passes run on the
+ * real field viewed as complex [N0][N1][N2/2] (aligned rows) in the plan
+ * scratch, and one z pass over mirror-paired lines (x, y) / (-x, -y)
+ * completes the real transform and writes the natural spectrum row by row;
+ * c2r runs the same passes backwards and only reads its input.  Same
+ * results to rounding.  Out-of-place float and double plans only
+ * (ACCFFT_C_EUNSUPPORTED otherwise).  ACCFFT_GB300_ORDER=packed|natural in
+ * the environment sets it at plan creation. */
+int accfft_c_set_pass_order(accfft_c_plan* plan, int order);
 /* extension: per-kernel device times.  With profiling on, every kernel the
  * plan launches is bracketed by CUDA events on its stream;
  * accfft_c_profile_read waits for them and returns, per pass label ("z_r2c",
@@ -238,6 +250,27 @@ int accfft_c_c2r_adjoint(accfft_c_plan* plan, const void* dx, void* dY, double* 
 int accfft_c_grad_adjoint(accfft_c_plan* plan, void* out, const void* g_x, const void* g_y, const void* g_z,
                           double* timer);
 int accfft_c_divergence_adjoint(accfft_c_plan* plan, void* a_x, void* a_y, void* a_z, const void* d, double* timer);
+
+/* --- batches (extension; no counterpart in the reference) ---------------
+ * Many independent transforms of uneven sizes in one pass-by-pass schedule.
+ * While a float r2c plan records (accfft_c_batch_record(b, plan, 1)), its
+ * execute and 3-D operator calls append their passes to the batch as one
+ * instance instead of launching them (r2c, c2r in either pass order,
+ * laplace, biharmonic, inv_laplace, inv_biharmonic, heat, helmholtz,
+ * poisson, grad_slow; other calls return ACCFFT_C_EUNSUPPORTED).
+ * accfft_c_batch_finalize groups level k (the k-th pass of every instance)
+ * by pass kind and line length and uploads one descriptor table per group;
+ * accfft_c_batch_run launches one kernel per group, level after level, on
+ * `stream` (capturable into a CUDA graph).  Line lengths up to 256.  One
+ * instance per plan (the plan's scratch belongs to it); the arrays given to
+ * the recorded calls must stay valid and distinct between instances. */
+typedef struct accfft_c_batch accfft_c_batch;
+accfft_c_batch* accfft_c_batch_create(void);
+void accfft_c_batch_destroy(accfft_c_batch* batch);
+int accfft_c_batch_record(accfft_c_batch* batch, accfft_c_plan* plan, int on);
+int accfft_c_batch_finalize(accfft_c_batch* batch);
+int accfft_c_batch_run(accfft_c_batch* batch, void* stream);
+int accfft_c_batch_info(const accfft_c_batch* batch, int* instances, int* levels, int* launches, int* tasks);
 
 /* --- Laplacian without device allocation ------------------------------
  * No counterpart in the reference.  For callers that may not call cudaMalloc

@@ -100,7 +100,11 @@ def fft1d(x, sign=-1, prec="d"):
 # ----------------------------------------------------------- passes
 def c2c_axis(data: np.ndarray, axis: int, sign: int, prec="d", nthreads=0) -> np.ndarray:
     """Complex transform along `axis` of a complex [n0][n1][w] array (returns a new array)."""
-    d = np.array(data, dtype=np.complex128, order="C", copy=True)
+    return _c2c_axis_inplace(np.array(data, dtype=np.complex128, order="C", copy=True), axis, sign, prec, nthreads)
+
+
+def _c2c_axis_inplace(d: np.ndarray, axis: int, sign: int, prec="d", nthreads=0) -> np.ndarray:
+    """c2c_axis on an array the caller owns (C-contiguous complex128), in place."""
     n0, n1, w = d.shape
     _check(lib().orc_c2c_axis(n0, n1, w, axis, _dp(d), sign, _prec(prec), _threads(nthreads)), "c2c_axis")
     return d
@@ -157,21 +161,21 @@ def r2c(u: np.ndarray, xyz: int = 7, prec="d", nthreads=0) -> np.ndarray:
     if xyz & 4:
         s = r2c_z(u, prec, nthreads)
     else:
-        s = np.array(u, dtype=np.complex128)
+        s = np.array(u, dtype=np.complex128, order="C")
     if xyz & 2:
-        s = c2c_axis(s, 1, -1, prec, nthreads)
+        _c2c_axis_inplace(s, 1, -1, prec, nthreads)
     if xyz & 1:
-        s = c2c_axis(s, 0, -1, prec, nthreads)
+        _c2c_axis_inplace(s, 0, -1, prec, nthreads)
     return s
 
 
 def c2r(s: np.ndarray, n2: int, xyz: int = 7, prec="d", nthreads=0) -> np.ndarray:
     """Backward real 3-D transform (src/accfft_gpu.cpp:540-603): x c2c, y c2c, z c2r; unnormalised."""
-    s = np.array(s, dtype=np.complex128)
+    s = np.array(s, dtype=np.complex128, order="C")
     if xyz & 1:
-        s = c2c_axis(s, 0, +1, prec, nthreads)
+        _c2c_axis_inplace(s, 0, +1, prec, nthreads)
     if xyz & 2:
-        s = c2c_axis(s, 1, +1, prec, nthreads)
+        _c2c_axis_inplace(s, 1, +1, prec, nthreads)
     if xyz & 4:
         return c2r_z(s, n2, prec, nthreads)
     return s
@@ -179,11 +183,11 @@ def c2r(s: np.ndarray, n2: int, xyz: int = 7, prec="d", nthreads=0) -> np.ndarra
 
 def c2c(d: np.ndarray, direction: int, xyz: int = 7, prec="d", nthreads=0) -> np.ndarray:
     """Complex 3-D transform (src/accfft_gpu.cpp:943-1136), direction -1 or +1, unnormalised."""
-    s = np.array(d, dtype=np.complex128)
+    s = np.array(d, dtype=np.complex128, order="C")
     order = (2, 1, 0) if direction == -1 else (0, 1, 2)
     for ax in order:
         if xyz & (1 << ax):
-            s = c2c_axis(s, ax, direction, prec, nthreads)
+            _c2c_axis_inplace(s, ax, direction, prec, nthreads)
     return s
 
 

@@ -23,8 +23,9 @@ GPU_SHAPES = [(8, 6, 10), (5, 9, 4), (6, 5, 12), (2, 4, 6), (16, 12, 10), (9, 10
 OPS1 = ("laplace", "biharmonic", "inv_laplace", "inv_biharmonic")
 
 
-def run_case(torch, native, n, dtype, case, inp):
-    """The CUDA path's result for one fixture case (numpy, GPU-path layouts)."""
+def run_case(torch, native, n, dtype, case, inp, order=0):
+    """The CUDA path's result for one fixture case (numpy, GPU-path layouts);
+    order 1 runs full r2c / c2r in the packed pass order."""
     h = (n[0], n[1], n[2] // 2 + 1)
     dev = lambda a: to_dev(torch, a, dtype)                       # noqa: E731
     new = lambda shape: empty(torch, shape, dtype)                # noqa: E731
@@ -47,6 +48,8 @@ def run_case(torch, native, n, dtype, case, inp):
         plan.c2c(-1 if case[3] == "f" else 1, d, o, xyz=xyz)
         return from_dev(o if xyz & 4 else d, True)
     plan = native.PlanR2C(n, dtype)
+    if order:
+        plan.set_pass_order(order)
     if case.startswith("r2c_"):
         _, f, xyz = case.split("_")
         xyz = int(xyz)
@@ -104,3 +107,15 @@ def test_cuda_path_matches_reference(cuda, native, oracle, n, dtype):
         if not e <= TOL[dtype]:
             bad.append((case, e))
     assert not bad, bad
+
+
+@pytest.mark.parametrize("dtype", ["float64", "float32"])
+@pytest.mark.parametrize("n", GPU_SHAPES)
+def test_packed_order_matches_reference(cuda, native, oracle, n, dtype):
+    """Full r2c / c2r in the packed pass order against the reference's own results."""
+    z = np.load(FIX)
+    t = "x".join(map(str, n))
+    inp = inputs(z, t)
+    for case in ("r2c_u_7", "r2c_nyq_7", "c2r_7"):
+        got = run_case(cuda, native, n, dtype, case, inp, order=1)
+        assert oracle.rel_l2(got, fixture(z, t, case)) <= TOL[dtype], case

@@ -95,6 +95,66 @@ def test_r2c_inplace_padded(cuda, native, oracle, dtype):
     assert oracle.rel_l2(back, u) < TOL[dtype]
 
 
+PACKED_SHAPES = [(1, 6, 8), (2, 4, 6), (5, 9, 4), (9, 10, 8), (16, 12, 10), (32, 64, 16), (48, 96, 64),
+                 (128, 128, 128), (90, 100, 180), (160, 180, 200), (256, 256, 256), (512, 512, 512)]
+
+
+@pytest.mark.parametrize("dtype", ["float64", "float32"])
+@pytest.mark.parametrize("n", PACKED_SHAPES)
+def test_packed_pass_order(cuda, native, oracle, n, dtype):
+    """The packed order (y and x passes over the real field viewed as complex
+    [N0][N1][N2/2], then mirror-paired z lines) against the oracle and the
+    reference's order: odd and even N0 / N1, N0 = 1 and 2 (every line its own
+    mirror or paired within its slab), non-Hermitian c2r input."""
+    torch = cuda
+    h = (n[0], n[1], n[2] // 2 + 1)
+    u = rng(13).standard_normal(n)
+    plan = native.PlanR2C(n, dtype)
+    plan.set_pass_order(1)
+    ref_plan = native.PlanR2C(n, dtype)
+    du = to_dev(torch, u, dtype)
+    keep = du.clone()
+    dh = empty(torch, h + (2,), dtype)
+    plan.r2c(du, dh)
+    assert torch.equal(du, keep)
+    uq = u.astype(dtype).astype(np.float64)
+    if np.prod(n) <= 2 ** 22:
+        assert oracle.rel_l2(from_dev(dh, True), oracle.r2c(uq)) < TOL[dtype]
+    dn = empty(torch, h + (2,), dtype)
+    ref_plan.r2c(du, dn)
+    assert ((dh.double() - dn.double()).norm() / dn.double().norm()).item() < TOL[dtype]
+    s = rng(14).standard_normal(h) + 1j * rng(15).standard_normal(h)
+    ds = to_dev(torch, s, dtype)
+    keep = ds.clone()
+    db = empty(torch, n, dtype)
+    plan.c2r(ds, db)
+    assert torch.equal(ds, keep)
+    if np.prod(n) <= 2 ** 22:
+        assert oracle.rel_l2(from_dev(db), oracle.c2r(from_dev(keep, True), n[2])) < TOL[dtype]
+    dbn = empty(torch, n, dtype)
+    ref_plan.c2r(ds, dbn)
+    assert ((db.double() - dbn.double()).norm() / dbn.double().norm()).item() < TOL[dtype]
+    before = native.kernel_launches()
+    plan.r2c(du, dh)
+    plan.c2r(dh, db)
+    assert native.kernel_launches() - before == 6
+    assert ((db.double() / np.prod(n) - du.double()).norm() / du.double().norm()).item() < TOL[dtype]
+
+
+def test_packed_pass_order_eligibility(cuda, native):
+    torch = cuda
+    n = (16, 16, 16)
+    buf = torch.zeros((16, 16, 18), device="cuda")
+    inplace = native.PlanR2C(n, "float32", data=buf, data_out=buf)
+    with pytest.raises(native.AccfftError):
+        inplace.set_pass_order(1)
+    with pytest.raises(native.AccfftError):
+        native.PlanC2C(n, "float32").set_pass_order(1)
+    tc = native.PlanR2C((128, 128, 256), "float32", flags=native.TC_TF32)
+    with pytest.raises(native.AccfftError):
+        tc.set_pass_order(1)
+
+
 @pytest.mark.parametrize("dtype", ["float64", "float32"])
 @pytest.mark.parametrize("xyz", [1, 2, 3, 4, 5, 6])
 def test_partial_axes(cuda, native, oracle, dtype, xyz):
