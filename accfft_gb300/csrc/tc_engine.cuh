@@ -13,38 +13,64 @@
 // LineFFT is unchanged.
 //
 // Precision forms (FP32 accumulation in both):
-//   TcForm::TF32x3  x = hi + lo with hi = tf32(x), lo = x - hi;
-//                   D = A_hi B_hi + A_hi B_lo + A_lo B_hi   (kind::tf32, K = 8 per MMA)
-//   TcForm::BF16x3  the same split with bf16 parts           (kind::f16 bf16, K = 16 per MMA)
+//   TcForm::TF32x3  x = hi + lo, hi = tf32(x), lo = tf32(x - hi), for the
+//                   data and the DFT matrix; D = A_lo B_hi + A_hi B_lo +
+//                   A_hi B_hi (kind::tf32, K = 8 per MMA)
+//   TcForm::BF16x6  x = hi + mid + lo, three bf16 parts (24 bits: exact for
+//                   float data, DFT matrix split from the double value);
+//                   D = the six products down to relative order 2^-16
+//                   (A_lo B_hi + A_mid B_mid + A_hi B_lo, A_mid B_hi + A_hi
+//                   B_mid, A_hi B_hi; smallest first), FP32-class accuracy
+//                   (kind::f16 with bf16 operands, K = 16 per MMA)
 //
-// Shared-memory operands use the canonical K-major layout without swizzle:
-// 8-row x 16-byte core matrices, adjacent along K at LBO = 128 B, adjacent
-// 8-row groups at SBO = (row bytes / 16) * 128 B.
+// Operands: A in tensor memory, written by each thread from its registers
+// with tcgen05.st (row i of a 128-row block = lane i, one part per 32
+// columns: bf16 pairs or tf32 values along K), so the data never passes
+// through shared memory on its way to the tensor core.  B (= W^T, 32 x 32,
+// one matrix per part) sits in shared memory in the canonical K-major layout
+// without swizzle: 8-row x 16-byte core matrices, adjacent along K at LBO =
+// 128 B, adjacent 8-row groups at SBO = (row bytes / 16) * 128 B.  Each
+// 128-row block owns 128 tensor-memory columns: the A parts at 0, 32 (and
+// 64), D at 96.
 //
-// Every wait on the MMA-completion mbarrier is bounded (TcCtx::limit polls).
-// A wait that gives up sets the error word, then drains: it waits again, up
-// to kTcDrainPolls, for the products already issued, so no MMA still writes
-// tensor memory when the kernel frees it.  After that the engine issues and
-// waits no more, and the kernel always reaches its end.
+// Every wait on the MMA-completion mbarrier is bounded (TcCtx::limit polls,
+// by lane 0 of each warp).  A wait that gives up sets the error word, then
+// drains: it waits again, up to kTcDrainPolls, for the products already
+// issued, so no MMA still writes tensor memory when the kernel frees it.
+// After that the engine issues and waits no more, and the kernel always
+// reaches its end.
 #pragma once
 #include <cstdint>
 #include "fft_core.cuh"
 
 namespace afg {
 
-enum class TcForm : int { TF32x3 = 1, BF16x3 = 2 };
+enum class TcForm : int { TF32x3 = 1, BF16x6 = 2 };
 
 template <TcForm F> struct TcTraits;
 template <> struct TcTraits<TcForm::TF32x3> {
-  static constexpr int row_bytes = 128;     // 32 tf32 per row
+  static constexpr int parts = 2;           // hi, lo
+  static constexpr int row_bytes = 128;     // a B row: 32 tf32
   static constexpr int kstep = 8;           // K per MMA
   static constexpr uint32_t fmt = 2;        // TF32 in the A/B format fields
+  static constexpr int nprod = 3;
+  // products (A part, B part), smallest first
+  __host__ __device__ static constexpr int pa(int i) { return i == 0 ? 1 : 0; }
+  __host__ __device__ static constexpr int pb(int i) { return i == 1 ? 1 : 0; }
 };
-template <> struct TcTraits<TcForm::BF16x3> {
-  static constexpr int row_bytes = 64;      // 32 bf16 per row
+template <> struct TcTraits<TcForm::BF16x6> {
+  static constexpr int parts = 3;           // hi, mid, lo
+  static constexpr int row_bytes = 64;      // a B row: 32 bf16
   static constexpr int kstep = 16;
   static constexpr uint32_t fmt = 1;        // BF16
+  static constexpr int nprod = 6;
+  __host__ __device__ static constexpr int pa(int i) { return i == 0 ? 2 : i == 1 ? 1 : i == 2 ? 0 : i == 3 ? 1 : 0; }
+  __host__ __device__ static constexpr int pb(int i) { return i == 0 ? 0 : i == 1 ? 1 : i == 2 ? 2 : i == 3 ? 0 : i == 4 ? 1 : 0; }
 };
+
+// tensor-memory columns of one 128-row block: A part q at 32 q, D at 96
+constexpr int kTcBlockCols = 128;
+constexpr int kTcDCol = 96;
 
 // ---------------------------------------------------------------- PTX helpers
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -78,20 +104,21 @@ __device__ __forceinline__ float tf32_round(float x) {
   return __uint_as_float(r);
 }
 
+// D (tensor memory) += A (tensor memory) * B (shared-memory descriptor)
 template <TcForm F>
-__device__ __forceinline__ void mma_issue(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
-                                          uint32_t accumulate) {
+__device__ __forceinline__ void mma_tmem_a(uint32_t d_tmem, uint32_t a_tmem, uint64_t bdesc, uint32_t idesc,
+                                           uint32_t accumulate) {
   if constexpr (F == TcForm::TF32x3) {
     asm volatile(
         "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-        "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
-        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        "tcgen05.mma.cta_group::1.kind::tf32 [%0], [%1], %2, %3, p;\n\t}" ::"r"(d_tmem),
+        "r"(a_tmem), "l"(bdesc), "r"(idesc), "r"(accumulate)
         : "memory");
   } else {
     asm volatile(
         "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
-        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n\t}" ::"r"(d_tmem),
+        "r"(a_tmem), "l"(bdesc), "r"(idesc), "r"(accumulate)
         : "memory");
   }
 }
@@ -107,6 +134,26 @@ __device__ __forceinline__ bool mbar_try(uint32_t mbar, uint32_t parity) {
   return done != 0;
 }
 
+// this warp's 32 lanes x 16 / 32 consecutive columns from registers
+__device__ __forceinline__ void tmem_st16(uint32_t taddr, const uint32_t (&r)[16]) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};" ::"r"(
+          taddr),
+      "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]), "r"(r[8]), "r"(r[9]),
+      "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]), "r"(r[15])
+      : "memory");
+}
+__device__ __forceinline__ void tmem_st32(uint32_t taddr, const uint32_t (&r)[32]) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,"
+      "%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,%32};" ::"r"(taddr),
+      "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]), "r"(r[8]), "r"(r[9]),
+      "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]), "r"(r[15]), "r"(r[16]), "r"(r[17]), "r"(r[18]),
+      "r"(r[19]), "r"(r[20]), "r"(r[21]), "r"(r[22]), "r"(r[23]), "r"(r[24]), "r"(r[25]), "r"(r[26]), "r"(r[27]),
+      "r"(r[28]), "r"(r[29]), "r"(r[30]), "r"(r[31])
+      : "memory");
+}
+
 // cos(2 pi m / 16), m = 0..15, evaluated by the compiler (sin(2 pi m / 16) =
 // cos(2 pi (m - 4) / 16)); the device reads them, it never evaluates them
 __constant__ double kTcCos16[16] = {
@@ -117,12 +164,9 @@ __constant__ double kTcCos16[16] = {
 
 // ----------------------------------------------------------- per-CTA context
 // Shared-memory state of the engine; tc_begin() sets it up, tc_end() frees
-// the tensor memory.  All threads of the CTA take part in every call.
+// the tensor memory.
 struct TcCtx {
-  unsigned char* a_hi;   // threads x row_bytes (the line exchange buffer, free during a stage)
-  unsigned char* a_lo;   // threads x row_bytes
-  unsigned char* b_hi;   // 32 x row_bytes: W^T high parts
-  unsigned char* b_lo;   // 32 x row_bytes: W^T low parts
+  unsigned char* b;      // parts x 32 x row_bytes: the parts of W^T
   uint64_t* mbar;        // MMA completion
   uint32_t* tmem_slot;   // tensor-memory base address written by tcgen05.alloc
   uint32_t tmem;
@@ -135,11 +179,15 @@ struct TcCtx {
 // polls of the drain that follows a wait that gave up (about a second)
 constexpr unsigned kTcDrainPolls = 1u << 22;
 
-// shared-memory bytes the engine adds after the exchange buffer (which must
-// hold at least threads * row_bytes)
+// shared-memory bytes the engine needs beyond the caller's exchange buffer
 template <TcForm F>
-__host__ __device__ constexpr size_t tc_extra_smem(int threads) {
-  return size_t(threads) * TcTraits<F>::row_bytes + 2 * 32 * TcTraits<F>::row_bytes + 16;
+__host__ __device__ constexpr size_t tc_extra_smem(int) {
+  return size_t(TcTraits<F>::parts) * 32 * TcTraits<F>::row_bytes + 16;
+}
+// tensor-memory columns of a CTA (a power of two >= 32)
+template <int THREADS>
+__host__ __device__ constexpr uint32_t tc_tmem_cols() {
+  return THREADS / 128 * kTcBlockCols <= 128 ? 128 : THREADS / 128 * kTcBlockCols <= 256 ? 256 : 512;
 }
 
 // byte offset of (row, byte b within the row) in the canonical layout
@@ -150,51 +198,28 @@ __device__ __forceinline__ uint32_t tc_off(int row, int b) {
   return uint32_t((row >> 3) * SBO + (b >> 4) * 128 + (row & 7) * 16 + (b & 15));
 }
 
-template <TcForm F>
-__device__ __forceinline__ void tc_store4(unsigned char* base, int row, int k0, float a, float b, float c, float d) {
-  if constexpr (F == TcForm::TF32x3) {
-    *reinterpret_cast<float4*>(base + tc_off<F>(row, k0 * 4)) = make_float4(a, b, c, d);
-  } else {
-    __nv_bfloat162 lo2 = __floats2bfloat162_rn(a, b), hi2 = __floats2bfloat162_rn(c, d);
-    uint2 u;
-    u.x = *reinterpret_cast<uint32_t*>(&lo2);
-    u.y = *reinterpret_cast<uint32_t*>(&hi2);
-    *reinterpret_cast<uint2*>(base + tc_off<F>(row, k0 * 2)) = u;
-  }
+// bf16 bits of x rounded to nearest even, and the float they stand for
+__device__ __forceinline__ uint32_t bf16_bits(float x, float& back) {
+  const __nv_bfloat16 h = __float2bfloat16_rn(x);
+  back = __bfloat162float(h);
+  return static_cast<uint32_t>(*reinterpret_cast<const unsigned short*>(&h));
 }
 
-// split x into the form's high and low parts, both rounded to the form's
-// type (the MMA would otherwise truncate the low part's tf32 mantissa)
-template <TcForm F>
-__device__ __forceinline__ void tc_split(float x, float& hi, float& lo) {
-  if constexpr (F == TcForm::TF32x3) {
-    hi = tf32_round(x);
-    lo = tf32_round(x - hi);
-  } else {
-    hi = __bfloat162float(__float2bfloat16_rn(x));
-    lo = x - hi;
-  }
-}
-
-// set up: W^T operands, mbarrier, tensor memory (cols >= 32 * blocks, a power
-// of two); threads must be a multiple of 128
+// set up: W^T parts, mbarrier, tensor memory; threads a multiple of 128
 template <TcForm F, int THREADS>
-__device__ __forceinline__ void tc_begin(TcCtx& c, unsigned char* exchange, unsigned char* extra, int* err,
-                                         unsigned limit) {
+__device__ __forceinline__ void tc_begin(TcCtx& c, unsigned char* extra, int* err, unsigned limit) {
   static_assert(THREADS % 128 == 0, "tensor-core stages use M = 128 row blocks");
-  constexpr int RB = TcTraits<F>::row_bytes;
-  c.a_hi = exchange;
-  c.a_lo = extra;
-  c.b_hi = extra + size_t(THREADS) * RB;
-  c.b_lo = c.b_hi + 32 * RB;
-  c.mbar = reinterpret_cast<uint64_t*>(c.b_lo + 32 * RB);
+  typedef TcTraits<F> TR;
+  constexpr int RB = TR::row_bytes;
+  c.b = extra;
+  c.mbar = reinterpret_cast<uint64_t*>(c.b + TR::parts * 32 * RB);
   c.tmem_slot = reinterpret_cast<uint32_t*>(c.mbar + 1);
   c.phase = 0;
   c.dead = false;
   c.err = err;
   c.limit = limit;
   // B[n][k] = Wreal[n][k]: rows 0-15 give Yr, 16-31 Yi; columns 0-15 take
-  // Xr, 16-31 Xi; W = exp(-2 pi i n k / 16)
+  // Xr, 16-31 Xi; W = exp(-2 pi i n k / 16); parts split from the double value
   for (int e = threadIdx.x; e < 32 * 32; e += THREADS) {
     const int n = e >> 5, k = e & 31;
     const int m = ((n & 15) * (k & 15)) & 15;
@@ -202,21 +227,21 @@ __device__ __forceinline__ void tc_begin(TcCtx& c, unsigned char* exchange, unsi
     double w;
     if (n < 16) w = k < 16 ? cs : sn;       // Wr | -Wi  (Wi = -sin)
     else w = k < 16 ? -sn : cs;             // Wi | Wr
-    const float wf = static_cast<float>(w);
-    float hi, lo;
-    tc_split<F>(wf, hi, lo);
-    lo = static_cast<float>(w - static_cast<double>(hi));
-    if constexpr (F == TcForm::TF32x3) lo = tf32_round(lo);
-    if constexpr (F == TcForm::TF32x3) {
-      *reinterpret_cast<float*>(c.b_hi + tc_off<F>(n, k * 4)) = hi;
-      *reinterpret_cast<float*>(c.b_lo + tc_off<F>(n, k * 4)) = lo;
-    } else {
-      *reinterpret_cast<__nv_bfloat16*>(c.b_hi + tc_off<F>(n, k * 2)) = __float2bfloat16_rn(hi);
-      *reinterpret_cast<__nv_bfloat16*>(c.b_lo + tc_off<F>(n, k * 2)) = __float2bfloat16_rn(lo);
+    double rest = w;
+#pragma unroll
+    for (int q = 0; q < TR::parts; ++q) {
+      if constexpr (F == TcForm::TF32x3) {
+        const float part = tf32_round(static_cast<float>(rest));
+        *reinterpret_cast<float*>(c.b + q * 32 * RB + tc_off<F>(n, k * 4)) = part;
+        rest -= static_cast<double>(part);
+      } else {
+        const __nv_bfloat16 part = __float2bfloat16_rn(static_cast<float>(rest));
+        *reinterpret_cast<__nv_bfloat16*>(c.b + q * 32 * RB + tc_off<F>(n, k * 2)) = part;
+        rest -= static_cast<double>(__bfloat162float(part));
+      }
     }
   }
-  constexpr uint32_t cols = THREADS / 128 * 32 <= 32 ? 32 : THREADS / 128 * 32 <= 64 ? 64
-                           : THREADS / 128 * 32 <= 128 ? 128 : 256;
+  constexpr uint32_t cols = tc_tmem_cols<THREADS>();
   if (threadIdx.x < 32) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(c.tmem_slot)),
                  "n"(cols)
@@ -239,54 +264,78 @@ __device__ __forceinline__ void tc_end(TcCtx& c) {
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   if (threadIdx.x < 32) {
-    constexpr uint32_t cols = THREADS / 128 * 32 <= 32 ? 32 : THREADS / 128 * 32 <= 64 ? 64
-                             : THREADS / 128 * 32 <= 128 ? 128 : 256;
+    constexpr uint32_t cols = tc_tmem_cols<THREADS>();
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(c.tmem), "n"(cols) : "memory");
   }
 }
 
 // One radix-16 DFT per thread, in place on v[0..15], on the tensor cores.
-// The caller guarantees that every thread of the CTA calls it together and
-// that nobody reads the exchange buffer (it holds A_hi during the call).
+// Every thread of the CTA calls it together; it touches no shared memory
+// but the engine's own (B, mbarrier).
 template <TcForm F, int THREADS>
 __device__ __forceinline__ void tc_dft16(TcCtx& c, float2 (&v)[16]) {
   typedef TcTraits<F> TR;
   constexpr int RB = TR::row_bytes;
   constexpr int KSTEPS = 32 / TR::kstep;
-  constexpr int BLOCK_BYTES = 128 * RB;
-  const int row = threadIdx.x;
-  // this thread's A row: 32 reals (Re of the 16 inputs, then Im), split
+  constexpr uint32_t SBO = RB / 16 * 128;
+  const int warp = threadIdx.x >> 5;
+  // this warp's lanes (32 (warp % 4) ...) and its 128-row block's columns
+  const uint32_t tbase = c.tmem + (uint32_t((warp & 3) * 32) << 16) + uint32_t((warp >> 2) * kTcBlockCols);
+  // this thread's A row, K = 32 reals (Re of the 16 inputs, then Im), in parts
+  if constexpr (F == TcForm::BF16x6) {
+    uint32_t p0[16], p1[16], p2[16];
 #pragma unroll
-  for (int q = 0; q < 8; ++q) {
-    float x[4], h[4], l[4];
+    for (int j = 0; j < 16; ++j) {
+      uint32_t h[2], m[2], l[2];
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      const int k = 4 * q + j;
-      x[j] = k < 16 ? v[k].x : v[k - 16].y;
-      tc_split<F>(x[j], h[j], l[j]);
+      for (int e = 0; e < 2; ++e) {
+        const int k = 2 * j + e;
+        const float x = k < 16 ? v[k].x : v[k - 16].y;
+        float bh, bm, bl;
+        h[e] = bf16_bits(x, bh);
+        const float r1 = x - bh;               // exact
+        m[e] = bf16_bits(r1, bm);
+        l[e] = bf16_bits(r1 - bm, bl);         // r1 - bm exact; its bf16 rounding loses bits below 2^-24 |x|
+      }
+      p0[j] = h[0] | (h[1] << 16);
+      p1[j] = m[0] | (m[1] << 16);
+      p2[j] = l[0] | (l[1] << 16);
     }
-    tc_store4<F>(c.a_hi, row, 4 * q, h[0], h[1], h[2], h[3]);
-    tc_store4<F>(c.a_lo, row, 4 * q, l[0], l[1], l[2], l[3]);
+    tmem_st16(tbase + 0, p0);
+    tmem_st16(tbase + 32, p1);
+    tmem_st16(tbase + 64, p2);
+  } else {
+    uint32_t q0[32], q1[32];
+#pragma unroll
+    for (int k = 0; k < 32; ++k) {
+      const float x = k < 16 ? v[k].x : v[k - 16].y;
+      const float hi = tf32_round(x);
+      q0[k] = __float_as_uint(hi);
+      q1[k] = __float_as_uint(tf32_round(x - hi));
+    }
+    tmem_st32(tbase + 0, q0);
+    tmem_st32(tbase + 32, q1);
   }
-  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   if (threadIdx.x == 0 && !c.dead) {
     constexpr uint32_t idesc = instr_desc<F>(128, 32);
-    constexpr uint32_t SBO = RB / 16 * 128;
-    const uint32_t ah = smem_u32(c.a_hi), al = smem_u32(c.a_lo);
-    const uint32_t bh = smem_u32(c.b_hi), bl = smem_u32(c.b_lo);
+    const uint32_t bbase = smem_u32(c.b);
 #pragma unroll
     for (int blk = 0; blk < THREADS / 128; ++blk) {
-      const uint32_t d = c.tmem + uint32_t(blk * 32);
-      const uint32_t ab = uint32_t(blk * BLOCK_BYTES);
+      const uint32_t col = c.tmem + uint32_t(blk * kTcBlockCols);
 #pragma unroll
-      for (int ks = 0; ks < KSTEPS; ++ks) {
-        const uint32_t ko = uint32_t(ks * 256);   // one K step = two core matrices along K
-        mma_issue<F>(d, smem_desc(ah + ab + ko, 128, SBO), smem_desc(bh + ko, 128, SBO), idesc, ks > 0);
-        mma_issue<F>(d, smem_desc(ah + ab + ko, 128, SBO), smem_desc(bl + ko, 128, SBO), idesc, 1);
-        mma_issue<F>(d, smem_desc(al + ab + ko, 128, SBO), smem_desc(bh + ko, 128, SBO), idesc, 1);
+      for (int pr = 0; pr < TR::nprod; ++pr) {
+#pragma unroll
+        for (int ks = 0; ks < KSTEPS; ++ks) {
+          // one K step of A = kstep elements = 8 columns (tf32: 1, bf16: 2 per column);
+          // of B = two core matrices along K
+          const uint32_t a = col + uint32_t(32 * TR::pa(pr) + 8 * ks);
+          const uint64_t b = smem_desc(bbase + uint32_t(TR::pb(pr) * 32 * RB + ks * 256), 128, SBO);
+          mma_tmem_a<F>(col + kTcDCol, a, b, idesc, (pr > 0 || ks > 0) ? 1u : 0u);
+        }
       }
     }
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
@@ -294,19 +343,22 @@ __device__ __forceinline__ void tc_dft16(TcCtx& c, float2 (&v)[16]) {
                  : "memory");
   }
   if (!c.dead) {
-    bool ok = false;
-    for (unsigned i = 0; i < c.limit && !ok; ++i) ok = mbar_try(smem_u32(c.mbar), c.phase);
-    if (!ok) {
-      c.dead = true;
-      atomicExch(c.err, 1);
-      for (unsigned i = 0; i < kTcDrainPolls && !ok; ++i) ok = mbar_try(smem_u32(c.mbar), c.phase);
+    // lane 0 of each warp polls; the warp takes its verdict
+    int ok = 1;
+    if ((threadIdx.x & 31) == 0) {
+      bool done = false;
+      for (unsigned i = 0; i < c.limit && !done; ++i) done = mbar_try(smem_u32(c.mbar), c.phase);
+      if (!done) {
+        atomicExch(c.err, 1);
+        for (unsigned i = 0; i < kTcDrainPolls && !done; ++i) done = mbar_try(smem_u32(c.mbar), c.phase);
+        ok = 0;
+      }
     }
+    ok = __shfl_sync(0xffffffffu, ok, 0);
+    if (!ok) c.dead = true;
   }
   c.phase ^= 1u;
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-  // this warp's 32 rows of its 128-row block: lanes 32*(warp % 4) ...
-  const int warp = threadIdx.x >> 5;
-  const uint32_t taddr = c.tmem + (uint32_t((warp & 3) * 32) << 16) + uint32_t((warp >> 2) * 32);
   uint32_t r[32];
   asm volatile(
       "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
@@ -316,7 +368,7 @@ __device__ __forceinline__ void tc_dft16(TcCtx& c, float2 (&v)[16]) {
         "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]),
         "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]),
         "=r"(r[30]), "=r"(r[31])
-      : "r"(taddr)
+      : "r"(tbase + uint32_t(kTcDCol))
       : "memory");
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
@@ -350,7 +402,7 @@ struct LineFFTTC {
       constexpr int Nsp = plan_ns_before(pl, s - 1);
       constexpr int Ns = plan_ns_before(pl, s);
       constexpr int two = plan_tw_offset(pl, s);
-      __syncthreads();   // the previous stage's MMAs read A_hi in the exchange buffer
+      __syncthreads();   // every thread has read the previous exchange
 #pragma unroll
       for (int b = 0; b < E / Rp; ++b) {
         const int j = t + b * P;
@@ -373,8 +425,7 @@ struct LineFFTTC {
         for (int r = 1; r < R; ++r) v[b * R + r] = c_mul(v[b * R + r], __ldg(tw + two + (r - 1) * Ns + k));
       }
       if constexpr (R == 16) {
-        __syncthreads();   // every thread has read this stage's inputs: A_hi may overwrite them
-        tc_dft16<F, THREADS>(c, v);
+        tc_dft16<F, THREADS>(c, v);   // its barrier also ends this stage's exchange reads
       } else {
 #pragma unroll
         for (int b = 0; b < E / R; ++b) Dft<R, 1>::run(v + b * R);

@@ -12,28 +12,41 @@
 
 namespace afg {
 
-// strided tiles: TC columns x L, 256 threads for L <= 512 (512 for 1024):
-// the tensor-core operands take 2 x threads x 128 B of shared memory, and
-// two CTAs per SM let one CTA's loads run while the other waits on its MMAs
+// Shared memory of a tensor-core CTA: the exchange buffer of the line engine
+// plus the engine's B operands; at least kTcSmemFloor per 256 threads so that
+// no more CTAs share an SM than its 512 tensor-memory columns hold (each
+// 128-row block takes 128 columns: two 256-thread CTAs, one 512-thread CTA)
+template <int THREADS>
+constexpr size_t tc_smem_floor() {
+  return THREADS <= 256 ? size_t(80) * 1024 : size_t(120) * 1024;
+}
+
+// CTAs per SM the register budget aims at (as many as tensor memory holds)
+template <int THREADS>
+constexpr int tc_min_blocks() {
+  return THREADS <= 256 ? 2 : 1;
+}
+
+// strided tiles: TC columns x L, 256 threads for L <= 512 (512 for 1024)
 template <int L, TcForm F> struct TcStridedShape {
   static constexpr int P = L / 16;
   static constexpr int TC = P >= 32 ? 8 : 16;
   static constexpr int threads = P * TC;
-  static constexpr size_t exch = size_t(L) * TC * sizeof(float2);   // = threads * 128 B
-  static constexpr size_t smem = exch + tc_extra_smem<F>(threads);
-  static_assert(exch >= size_t(threads) * TcTraits<F>::row_bytes, "A_hi fits the exchange buffer");
+  static constexpr size_t exch = size_t(L) * TC * sizeof(float2);
+  static constexpr size_t need = exch + tc_extra_smem<F>(threads);
+  static constexpr size_t smem = need > tc_smem_floor<threads>() ? need : tc_smem_floor<threads>();
 };
 
 template <int M, TcForm F> struct TcContigShape {
   typedef ContigShape<float, M, 16> CS;
   static constexpr int threads = CS::threads;
-  static constexpr size_t exch = CS::smem;
-  static constexpr size_t smem = exch + tc_extra_smem<F>(threads);
-  static_assert(exch >= size_t(threads) * TcTraits<F>::row_bytes, "A_hi fits the exchange buffer");
+  static constexpr size_t exch = (CS::smem + 15) / 16 * 16;
+  static constexpr size_t need = exch + tc_extra_smem<F>(threads);
+  static constexpr size_t smem = need > tc_smem_floor<threads>() ? need : tc_smem_floor<threads>();
 };
 
 template <int L, TcForm F>
-__global__ void __launch_bounds__(TcStridedShape<L, F>::threads, 1)
+__global__ void __launch_bounds__(TcStridedShape<L, F>::threads, tc_min_blocks<TcStridedShape<L, F>::threads>())
 k_strided_tc(const StridedArgs a, int* err) {
   typedef TcStridedShape<L, F> SH;
   typedef LineFFTTC<L, F, SH::threads> LN;
@@ -42,7 +55,7 @@ k_strided_tc(const StridedArgs a, int* err) {
   extern __shared__ __align__(16) unsigned char smraw[];
   V* sm = reinterpret_cast<V*>(smraw);
   TcCtx ctx;
-  tc_begin<F, SH::threads>(ctx, smraw, smraw + SH::exch, err, a.wait_limit);
+  tc_begin<F, SH::threads>(ctx, smraw + SH::exch, err, a.wait_limit);
   const int c = threadIdx.x % TC;
   const int t = threadIdx.x / TC;
   const long long g = (long long)blockIdx.x * TC + c;
@@ -67,7 +80,7 @@ k_strided_tc(const StridedArgs a, int* err) {
 }
 
 template <int M, TcForm F>
-__global__ void __launch_bounds__(TcContigShape<M, F>::threads, 1)
+__global__ void __launch_bounds__(TcContigShape<M, F>::threads, tc_min_blocks<TcContigShape<M, F>::threads>())
 k_zr2c_tc(const ContigArgs a, int* err) {
   typedef TcContigShape<M, F> TS;
   typedef LineFFTTC<M, F, TS::threads> LN;
@@ -77,7 +90,7 @@ k_zr2c_tc(const ContigArgs a, int* err) {
   extern __shared__ __align__(16) unsigned char smraw[];
   V* sm = reinterpret_cast<V*>(smraw);
   TcCtx ctx;
-  tc_begin<F, TS::threads>(ctx, smraw, smraw + TS::exch, err, a.wait_limit);
+  tc_begin<F, TS::threads>(ctx, smraw + TS::exch, err, a.wait_limit);
   const int t = threadIdx.x % P, li = threadIdx.x / P;
   const long long line = (long long)blockIdx.x * TL + li;
   const bool valid = line < a.nlines;
@@ -107,7 +120,7 @@ k_zr2c_tc(const ContigArgs a, int* err) {
 }
 
 template <int M, TcForm F>
-__global__ void __launch_bounds__(TcContigShape<M, F>::threads, 1)
+__global__ void __launch_bounds__(TcContigShape<M, F>::threads, tc_min_blocks<TcContigShape<M, F>::threads>())
 k_zc2r_tc(const ContigArgs a, int* err) {
   typedef TcContigShape<M, F> TS;
   typedef LineFFTTC<M, F, TS::threads> LN;
@@ -117,7 +130,7 @@ k_zc2r_tc(const ContigArgs a, int* err) {
   extern __shared__ __align__(16) unsigned char smraw[];
   V* sm = reinterpret_cast<V*>(smraw);
   TcCtx ctx;
-  tc_begin<F, TS::threads>(ctx, smraw, smraw + TS::exch, err, a.wait_limit);
+  tc_begin<F, TS::threads>(ctx, smraw + TS::exch, err, a.wait_limit);
   const int t = threadIdx.x % P, li = threadIdx.x / P;
   const long long line = (long long)blockIdx.x * TL + li;
   const bool valid = line < a.nlines;
@@ -186,7 +199,7 @@ bool tc_length_supported(int len, bool contig) {
 bool launch_strided_tc(int form, int L, const StridedArgs& a, int* err, cudaStream_t s) {
 #define AFG_TC_S(n)                                                                          \
   case n:                                                                                    \
-    return form == 1 ? run_strided_tc<n, TcForm::TF32x3>(a, err, s) : run_strided_tc<n, TcForm::BF16x3>(a, err, s);
+    return form == 1 ? run_strided_tc<n, TcForm::TF32x3>(a, err, s) : run_strided_tc<n, TcForm::BF16x6>(a, err, s);
   switch (L) {
     AFG_TC_S(128) AFG_TC_S(256) AFG_TC_S(512) AFG_TC_S(1024)
     default: return false;
@@ -199,7 +212,7 @@ bool launch_z_tc(int form, bool r2c, int M, const ContigArgs& a, int* err, cudaS
   case n:                                                                                          \
     if (form == 1) return r2c ? run_contig_tc<n, TcForm::TF32x3, true>(a, err, s)                  \
                               : run_contig_tc<n, TcForm::TF32x3, false>(a, err, s);                \
-    return r2c ? run_contig_tc<n, TcForm::BF16x3, true>(a, err, s) : run_contig_tc<n, TcForm::BF16x3, false>(a, err, s);
+    return r2c ? run_contig_tc<n, TcForm::BF16x6, true>(a, err, s) : run_contig_tc<n, TcForm::BF16x6, false>(a, err, s);
   switch (M) {
     AFG_TC_Z(128) AFG_TC_Z(256) AFG_TC_Z(512)
     default: return false;

@@ -48,10 +48,12 @@ extern "C" {
 /* Plan flags beside the reference's ACCFFT_ESTIMATE/MEASURE/PATIENT (1, 2,
  * 4; accepted and ignored).  Extensions with no counterpart in the
  * reference: float r2c plans whose radix-16 line stages run on the tensor
- * cores as 32x32 real matrix products with FP32 accumulation, splitting
- * every operand in a high and a low part (3 products): 3xTF32 or BF16.
- * Such plans run full r2c / c2r transforms (xyz = 7) of device arrays
- * only; x and y lengths 128, 256, 512 or 1024, N2/2 128, 256 or 512. */
+ * cores as 32x32 real matrix products with FP32 accumulation, the data held
+ * in tensor memory: ACCFFT_C_TC_TF32 splits every operand in a high and a
+ * low TF32 part (3 products); ACCFFT_C_TC_BF16 in three BF16 parts (exact
+ * for float data; 6 products, FP32-class accuracy).  Such plans run full
+ * r2c / c2r transforms (xyz = 7) of device arrays only; x and y lengths 128,
+ * 256, 512 or 1024, N2/2 128, 256 or 512. */
 #define ACCFFT_C_TC_TF32 0x100u
 #define ACCFFT_C_TC_BF16 0x200u
 /* Double plans whose kernels compute in double-float: every value a pair

@@ -1,6 +1,7 @@
 """Tensor-core forms of the float r2c / c2r path (ACCFFT_C_TC_TF32 and
 ACCFFT_C_TC_BF16): radix-16 stages as 32x32 real matrix products with FP32
-accumulation, against the FP64 oracle and against the CUDA-core form."""
+accumulation, A operands in tensor memory, against the FP64 oracle and
+against the CUDA-core form."""
 import numpy as np
 import pytest
 
@@ -9,9 +10,10 @@ from test_gpu_transforms import empty, from_dev, to_dev
 
 pytestmark = pytest.mark.gpu
 
-# rel-L2 bounds vs the FP64 oracle: 3xTF32 keeps ~21 bits per operand, the
-# BF16 split ~16
-TOL = {"tf32": 1e-5, "bf16": 2e-4}
+# rel-L2 bounds vs the FP64 oracle: the three-way BF16 split (six products)
+# is exact for float data and drops only products below 2^-16 relative, so it
+# is held to the benchmark spec's bound 1e-6; 3xTF32 keeps about 22 bits per operand
+TOL = {"tf32": 5e-6, "bf16": 1e-6}
 
 
 def flag(native, form):
