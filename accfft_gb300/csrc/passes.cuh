@@ -444,7 +444,8 @@ struct ContigSlot {
       pair_lines(valid ? q : 0, a.pair_n0, a.pair_n1, i, j);
       row = (li & 1) ? j : i;
       wr = valid && !((li & 1) && i == j);
-      partner = li ^ 1;
+      // the idle last slot of an odd TL has no partner slot in the CTA
+      partner = li < 2 * PP ? (li ^ 1) : li;
     } else {
       const long long line = tile * TL + li;
       valid = wr = line < a.nlines;

@@ -388,7 +388,7 @@ accfft_c_plan* make_plan(int kind, bool dbl, const int* n, void* data, void* dat
     // default whole-grid passes; kept for comparison)
     // ACCFFT_GB300_ORDER = packed | natural: the pass order of full transforms
     const char* ord = getenv("ACCFFT_GB300_ORDER");
-    p->packed = packed_eligible(p) && ord && std::string(ord) == "packed";
+    p->packed = packed_eligible(p) && !(ord && std::string(ord) == "natural");
     const char* env = getenv("ACCFFT_GB300_ZY");
     std::string zy = env ? env : "";
     if (zy == "fused" && slab_available(dbl, n[1], n[2])) {
@@ -854,6 +854,76 @@ struct Exec {
     cudaEventRecord(p->evb[accfft_c_plan::kMaxBatches + 1], C);
     cudaStreamWaitEvent(A, p->evb[accfft_c_plan::kMaxBatches + 1], 0);
   }
+  // y pass of the packed order over ns slabs of dense rows (M complex), from
+  // in_base to out_base (the first slab of each), on stream st
+  void ypass_dense(const void* in_base, void* out_base, int inverse, long long ns, cudaStream_t st) {
+    if (!ok()) return;
+    const long long N1 = p->n[1], M = p->M();
+    StridedArgs a{};
+    a.in = in_base;
+    a.out = out_base;
+    a.tw = p->tw_y;
+    a.ncols = ns * M;
+    a.cps = M;
+    a.in_slab = a.out_slab = N1 * M;
+    a.in_line = a.out_line = M;
+    a.inverse = inverse;
+    if (!timed(inverse ? "y_inv" : "y", st, [&] { return go_strided(p->n[1], 0, a, st); }))
+      unsupported("strided pass", p->n[1]);
+  }
+  // The packed order with the real array in pinned host memory (r2c input or
+  // c2r output), moved in slab batches through the staging ring on the
+  // plan's second stream, overlapped with the y passes of the batches
+  // already staged; the x and z passes follow (r2c) or precede (c2r) on the
+  // plan's stream.  Same kernels, so the same results as device arrays.
+  void packed_host(bool forward, const void* in, void* out) {
+    if (not_recordable("a pinned-host array")) return;
+    if (!ok()) return;
+    const long long N0 = p->n[0], N1 = p->n[1], M = p->M(), row = p->n[2];
+    const int nb = (int)std::min<long long>(N0, p->host_batches);
+    const long long slab_rows = (N0 + nb - 1) / nb;
+    const long long slot_bytes = slab_rows * N1 * row * p->esz();
+    if (!ensure_stage(slot_bytes)) return;
+    auto slot = [&](int b) { return static_cast<char*>(p->hstage) + (b % accfft_c_plan::kHostSlots) * slot_bytes; };
+    auto dense_at = [&](long long s0) { return static_cast<char*>(p->scratch) + s0 * N1 * M * 2 * p->esz(); };
+    cudaStream_t A = p->stream, C = p->stream2;
+    cudaEvent_t* ev_start = &p->evb[0];
+    cudaEvent_t* ev_copy = &p->evb[1];
+    cudaEvent_t* ev_free = &p->evb[1 + accfft_c_plan::kHostBatches];
+    void* sc = p->scratch;
+    if (!forward) {
+      zc2r_pairs(in, sc);
+      xpass(sc, sc, M, 1);
+    }
+    cudaEventRecord(*ev_start, A);
+    cudaStreamWaitEvent(C, *ev_start, 0);
+    for (int b = 0; b < nb && ok(); ++b) {
+      const long long s0 = N0 * b / nb, s1 = N0 * (b + 1) / nb, ns = s1 - s0;
+      const size_t bytes = (size_t)(ns * N1 * row * p->esz());
+      const int k = b % accfft_c_plan::kHostSlots;
+      if (forward) {
+        if (b >= accfft_c_plan::kHostSlots) cudaStreamWaitEvent(C, ev_free[k], 0);
+        copy("h2d", C, slot(b), real_at(in, s0, row), bytes);
+        cudaEventRecord(ev_copy[b], C);
+        cudaStreamWaitEvent(A, ev_copy[b], 0);
+        ypass_dense(slot(b), dense_at(s0), 0, ns, A);
+        cudaEventRecord(ev_free[k], A);
+      } else {
+        if (b >= accfft_c_plan::kHostSlots) cudaStreamWaitEvent(A, ev_free[k], 0);
+        ypass_dense(dense_at(s0), slot(b), 1, ns, A);
+        cudaEventRecord(ev_copy[b], A);
+        cudaStreamWaitEvent(C, ev_copy[b], 0);
+        copy("d2h", C, real_at(out, s0, row), slot(b), bytes);
+        cudaEventRecord(ev_free[k], C);
+      }
+    }
+    cudaEventRecord(p->evb[accfft_c_plan::kMaxBatches + 1], C);
+    cudaStreamWaitEvent(A, p->evb[accfft_c_plan::kMaxBatches + 1], 0);
+    if (forward) {
+      xpass(sc, sc, M, 0);
+      zr2c_pairs(sc, out);
+    }
+  }
   bool ensure_stage(long long slot_bytes) {
     const long long need = slot_bytes * accfft_c_plan::kHostSlots;
     if (p->hstage_bytes >= need) return true;
@@ -1144,15 +1214,18 @@ int exec_r2c_plan(accfft_c_plan* p, int direction, void* in, void* out, double* 
   }
   if (p->df && (host_in || host_out))
     return fail(ACCFFT_C_EUNSUPPORTED, "execute: double-float plans take device arrays");
-  if (p->packed && (xyz & 7) == 7 && !host_in && !host_out && weight == 0 && p->zy_mode == 0 &&
-      (direction == -1 || direction == 1)) {
+  if (p->packed && (xyz & 7) == 7 && weight == 0 && p->zy_mode == 0 && (direction == -1 || direction == 1)) {
     // packed order: r2c = y, x over the packed real field (in -> scratch),
     // then the mirror-pair z pass (scratch -> natural spectrum); c2r the
-    // reverse.  The input array is only read.
+    // reverse.  The input array is only read.  A real array in pinned host
+    // memory is staged through the device ring; other host arrays are
+    // reached by the kernels over the host link.
     Exec ex(p, timer);
     const long long M = p->M();
     void* sc = p->scratch;
-    if (direction == -1) {
+    if ((direction == -1 && host_in) || (direction == 1 && host_out)) {
+      ex.packed_host(direction == -1, in, out);
+    } else if (direction == -1) {
       ex.ypass(in, sc, M, 0);
       ex.xpass(sc, sc, M, 0);
       ex.zr2c_pairs(sc, out);

@@ -151,8 +151,8 @@ int accfft_c_set_zy_schedule(accfft_c_plan* plan, int mode);
  * completes the real transform and writes the natural spectrum row by row;
  * c2r runs the same passes backwards and only reads its input.  Same
  * results to rounding.  Out-of-place float and double plans only
- * (ACCFFT_C_EUNSUPPORTED otherwise).  ACCFFT_GB300_ORDER=packed|natural in
- * the environment sets it at plan creation. */
+ * (ACCFFT_C_EUNSUPPORTED otherwise), where it is the default;
+ * ACCFFT_GB300_ORDER=natural in the environment makes 0 the default. */
 int accfft_c_set_pass_order(accfft_c_plan* plan, int order);
 /* extension: per-kernel device times.  With profiling on, every kernel the
  * plan launches is bracketed by CUDA events on its stream;

@@ -25,7 +25,8 @@ OPS1 = ("laplace", "biharmonic", "inv_laplace", "inv_biharmonic")
 
 def run_case(torch, native, n, dtype, case, inp, order=0):
     """The CUDA path's result for one fixture case (numpy, GPU-path layouts);
-    order 1 runs full r2c / c2r in the packed pass order."""
+    order 0 runs full r2c / c2r in the reference's pass order, 1 in the
+    packed order."""
     h = (n[0], n[1], n[2] // 2 + 1)
     dev = lambda a: to_dev(torch, a, dtype)                       # noqa: E731
     new = lambda shape: empty(torch, shape, dtype)                # noqa: E731
@@ -48,8 +49,7 @@ def run_case(torch, native, n, dtype, case, inp, order=0):
         plan.c2c(-1 if case[3] == "f" else 1, d, o, xyz=xyz)
         return from_dev(o if xyz & 4 else d, True)
     plan = native.PlanR2C(n, dtype)
-    if order:
-        plan.set_pass_order(order)
+    plan.set_pass_order(order)
     if case.startswith("r2c_"):
         _, f, xyz = case.split("_")
         xyz = int(xyz)

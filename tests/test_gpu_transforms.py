@@ -112,6 +112,7 @@ def test_packed_pass_order(cuda, native, oracle, n, dtype):
     plan = native.PlanR2C(n, dtype)
     plan.set_pass_order(1)
     ref_plan = native.PlanR2C(n, dtype)
+    ref_plan.set_pass_order(0)
     du = to_dev(torch, u, dtype)
     keep = du.clone()
     dh = empty(torch, h + (2,), dtype)
@@ -400,6 +401,7 @@ def test_persistent_zy_schedule(cuda, native, monkeypatch, n):
     torch = cuda
     u = torch.randn(n, device="cuda")
     ref = native.PlanR2C(n, "float32")
+    ref.set_pass_order(0)                  # the reference's order, as the persistent schedule
     monkeypatch.setenv("ACCFFT_GB300_ZY", "persistent")
     plan = native.PlanR2C(n, "float32")
     h = (n[0], n[1], n[2] // 2 + 1, 2)
@@ -483,6 +485,7 @@ def test_host_staging_keeps_persistent_control_words(cuda, native, monkeypatch):
     n = (64, 256, 256)
     h = (n[0], n[1], n[2] // 2 + 1, 2)
     ref = native.PlanR2C(n, "float32")
+    ref.set_pass_order(0)
     monkeypatch.setenv("ACCFFT_GB300_ZY", "persistent")
     plan = native.PlanR2C(n, "float32")
     u = torch.randn(n, device="cuda")

@@ -37,6 +37,7 @@ def test_persistent_zy_wait_gives_up(cuda, native, zero_wait_limit):
     assert e.value.code == native.ECUDA and "gave up" in str(e.value)
     native.set_wait_limit(None)
     ref = native.PlanR2C(n, "float32")
+    ref.set_pass_order(0)                 # the reference's order, as the persistent schedule
     a = torch.empty(half(n), device="cuda")
     ref.r2c(u, a)
     plan.r2c(u, out)                      # the error word was cleared by the report
