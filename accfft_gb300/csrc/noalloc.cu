@@ -140,9 +140,19 @@ extern "C" int accfft_c_laplace_gpuf_noalloc(const int n[3], float* LA, const fl
     return err(ACCFFT_C_EINVAL, msg);
   }
 
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  // the working array is the current device's: a stream of another device
+  // would run the kernels against the wrong array
+  if (s) {
+    int cur = 0, sdev = 0;
+    cudaError_t de = cudaGetDevice(&cur);
+    if (de == cudaSuccess) de = cudaStreamGetDevice(s, &sdev);
+    if (de != cudaSuccess) return err(ACCFFT_C_ECUDA, cudaGetErrorString(de));
+    if (sdev != cur)
+      return err(ACCFFT_C_EINVAL, "laplace_gpuf_noalloc: the stream belongs to another device than the current one");
+  }
   unsigned char* base = nullptr;
   if (int rc = scratch_address(&base)) return rc;
-  cudaStream_t s = static_cast<cudaStream_t>(stream);
   float2* spec = reinterpret_cast<float2*>(base);
   float2* tw = reinterpret_cast<float2*>(base + spec_bytes);
   // the spectrum is fully written by the first pass; only the tables are

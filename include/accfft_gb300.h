@@ -63,7 +63,9 @@ extern "C" {
  * 1e-16; magnitudes must stay within float's exponent range (results below
  * 2^128, inputs above 2^-126 or flushed to zero).  Such plans run the r2c,
  * c2r and c2c transforms (any xyz); the single-axis transforms and the
- * operators stay with plain double plans. */
+ * operators stay with plain double plans.  Every transform of such a plan
+ * rescales by the exponent its input scan leaves in one word of the plan,
+ * so two transforms of one plan must not overlap on the GPU. */
 #define ACCFFT_C_F64_DF 0x400u
 
 typedef struct accfft_c_plan accfft_c_plan; /* opaque */
@@ -164,7 +166,10 @@ int accfft_c_set_pass_order(accfft_c_plan* plan, int order);
 int accfft_c_set_profiling(accfft_c_plan* plan, int on);
 int accfft_c_profile_read(accfft_c_plan* plan, int max_entries, char* labels, long long* counts, double* total_ms);
 /* extension: enqueue on `stream` (a cudaStream_t); blocking = 0 returns
- * without waiting (timer slots are then not updated) */
+ * without waiting (timer slots are then not updated).  A plan's calls share
+ * its scratch spectrum (and a double-float plan's exponent word): calls of
+ * one plan must not overlap on the GPU, so run concurrent transforms with
+ * one plan each. */
 int accfft_c_set_stream(accfft_c_plan* plan, void* stream, int blocking);
 
 /* --- transforms -------------------------------------------------------
@@ -286,8 +291,9 @@ int accfft_c_batch_info(const accfft_c_batch* batch, int* instances, int* levels
  * allocated on the device and nothing is freed.
  * The first call on a device performs a one-time set-up; make it before any
  * stream capture.  Every call reuses the same array, so calls that overlap on
- * the GPU race.  `stream` is a cudaStream_t (NULL: the default stream); the
- * call returns when the result is complete. */
+ * the GPU race.  `stream` is a cudaStream_t of the current device (NULL: the
+ * default stream; a stream of another device is refused with
+ * ACCFFT_C_EINVAL); the call returns when the result is complete. */
 int accfft_c_laplace_gpuf_noalloc(const int n[3], float* LA, const float* A, void* stream);
 
 #ifdef __cplusplus

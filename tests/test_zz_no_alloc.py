@@ -8,7 +8,10 @@ file checks, through the C ABI, that two calls in a row give the same result
 as the plan-based accfft_c_laplace, and that a grid too large for the array
 is refused.  It is named so that pytest collects it last."""
 import ctypes
+import os
+import sys
 
+import numpy as np
 import pytest
 
 pytestmark = pytest.mark.gpu
@@ -46,3 +49,23 @@ def test_noalloc_rejects_grids_beyond_its_array(cuda, native):
     rc = _noalloc(native, n, out, a)
     assert rc == native.EINVAL
     assert "working memory" in native.last_error()
+
+
+def test_noalloc_laplace_matches_oracle(cuda, native):
+    """The same two-call check against the oracle directly (the CPU
+    restatement of the reference's laplace, pinned to the reference's own
+    results), not only through the plan-based entry point."""
+    torch = cuda
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "oracle"))
+    import accfft_oracle as orc
+
+    n = (40, 36, 48)
+    r = np.random.default_rng(6)
+    for call in range(2):
+        a = r.standard_normal(n).astype(np.float32)
+        got = torch.full(n, float("nan"), device="cuda")
+        rc = _noalloc(native, n, got, torch.from_numpy(a).cuda())
+        assert rc == 0, native.last_error()
+        torch.cuda.synchronize()
+        ref = orc.spectral_op(a.astype(np.float64), "laplace")
+        assert orc.rel_l2(got.cpu().numpy().astype(np.float64), ref) < TOL, call
