@@ -85,6 +85,8 @@ def lib() -> ctypes.CDLL:
         "accfft_c_set_stream": ([vp, vp, i], i),
         "accfft_c_set_zy_schedule": ([vp, i], i),
         "accfft_c_set_pass_order": ([vp, i], i),
+        "accfft_c_plan_tuning": ([vp, ip, ip, ip], i),
+        "accfft_c_set_variants": ([vp, ip], i),
         "accfft_c_set_profiling": ([vp, i], i),
         "accfft_c_profile_read": ([vp, i, ctypes.c_char_p, ctypes.POINTER(ll), dp], i),
         "accfft_c_execute_r2c_gpu": ([vp, vp, vp, dp, u], i),
@@ -206,7 +208,10 @@ def local_size_c2c(n, real_bytes=8):
 class _Plan:
     kind = 0
 
-    def __init__(self, n, dtype="float32", data=None, data_out=None, flags=ACCFFT_MEASURE):
+    # Python plans default to ACCFFT_ESTIMATE (the default kernels, no timing
+    # at plan creation); pass flags=ACCFFT_MEASURE, the reference's default
+    # and the C++ API's, to have a float r2c plan tune its passes
+    def __init__(self, n, dtype="float32", data=None, data_out=None, flags=ACCFFT_ESTIMATE):
         self.n = tuple(int(v) for v in n)
         self.dtype = str(dtype).replace("torch.", "")
         if self.dtype not in ("float32", "float64"):
@@ -259,6 +264,21 @@ class _Plan:
         """0: the reference's pass order (z, y, x); 1: packed (y and x over the
         real field viewed as complex, then mirror-paired z lines)"""
         _check(lib().accfft_c_set_pass_order(self._h, int(order)))
+
+    def tuning(self) -> dict:
+        """Radix / tile variants of the y, x, z r2c and z c2r passes (chosen by
+        timing at plan creation with flags=ACCFFT_MEASURE; defaults otherwise):
+        {"tuned": bool, pass: {"variant", "radix", "tile"}}"""
+        v, r, t = (ctypes.c_int * 4)(), (ctypes.c_int * 4)(), (ctypes.c_int * 4)()
+        tuned = lib().accfft_c_plan_tuning(self._h, v, r, t)
+        out = {"tuned": bool(tuned)}
+        for k, name in enumerate(("y", "x", "z_r2c", "z_c2r")):
+            out[name] = {"variant": v[k], "radix": r[k], "tile": t[k]}
+        return out
+
+    def set_variants(self, y=0, x=0, z_r2c=0, z_c2r=0):
+        """Force the radix / tile variants of the four passes (0 = default)."""
+        _check(lib().accfft_c_set_variants(self._h, _ints([y, x, z_r2c, z_c2r])))
 
     def check(self):
         """Wait for the plan's stream; raise AccfftError(ECUDA) when a bounded

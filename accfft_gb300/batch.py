@@ -53,7 +53,7 @@ def radix_plan(length: int, dtype: str) -> dict:
 
 
 class _Instance:
-    def __init__(self, idx, shape, op, dtype, device):
+    def __init__(self, idx, shape, op, dtype, device, flags=None):
         self.idx, self.shape, self.op = idx, tuple(shape), op
         tdt = getattr(torch, dtype)
         self.inp = torch.empty(self.shape, dtype=tdt, device=device)
@@ -63,10 +63,11 @@ class _Instance:
         self.tmp = torch.empty(self.shape, dtype=tdt, device=device) if op == "lap_invlap" else None
         self.plan = None
         self.dtype = dtype
+        self.flags = flags
 
     def make_plan(self, schedule):
         if self.plan is None:
-            self.plan = PlanR2C(self.shape, self.dtype)
+            self.plan = PlanR2C(self.shape, self.dtype, **({} if self.flags is None else {"flags": self.flags}))
         self.plan.set_zy_schedule({"split": 0, "fused": 1, "persistent": 2}[schedule])
 
     def enqueue(self, stream):
@@ -85,7 +86,7 @@ class _Instance:
 
 
 class BatchPlan:
-    def __init__(self, specs, dtype="float32", streams=4, cache=None, device="cuda", form="streams"):
+    def __init__(self, specs, dtype="float32", streams=4, cache=None, device="cuda", form="streams", flags=None):
         for shape, op in specs:
             if op not in OPS:
                 raise ValueError(f"unknown operation {op!r}")
@@ -94,7 +95,7 @@ class BatchPlan:
         self.streams = streams
         self.cache = cache
         self.schedule = {}
-        self.instances = [_Instance(i, s, op, dtype, device) for i, (s, op) in enumerate(specs)]
+        self.instances = [_Instance(i, s, op, dtype, device, flags) for i, (s, op) in enumerate(specs)]
         for inst in self.instances:
             inst.make_plan("split")
         self.graph = None
@@ -168,7 +169,7 @@ class BatchPlan:
             if key in cached:
                 self.schedule[shape] = cached[key]
                 continue
-            probe = _Instance(-1, shape, "r2c_c2r", self.dtype, self.instances[0].inp.device)
+            probe = _Instance(-1, shape, "r2c_c2r", self.dtype, self.instances[0].inp.device, self.instances[0].flags)
             probe.inp.uniform_(-1, 1)
             best = None
             for sched in ("split", "fused", "persistent"):
@@ -214,7 +215,9 @@ class BatchPlan:
         for shape in sorted({i.shape for i in self.instances}):
             axes = {"x": radix_plan(shape[0], self.dtype), "y": radix_plan(shape[1], self.dtype),
                     "z_half": radix_plan(shape[2] // 2, self.dtype)}
-            rows.append({"grid": list(shape), "schedule": self.schedule.get(shape, "split"), "radix": axes})
+            inst = next(i for i in self.instances if i.shape == shape)
+            rows.append({"grid": list(shape), "schedule": self.schedule.get(shape, "split"), "radix": axes,
+                         "tuned_passes": inst.plan.tuning() if inst.plan is not None else None})
         return rows
 
     # ------------------------------------------------------- grouped form

@@ -62,6 +62,8 @@ struct StridedArgs {
   // polls a device-side wait makes before it gives up (tensor-core and
   // persistent kernels; accfft_c_set_wait_limit)
   unsigned wait_limit;
+  // radix / tile variant of a float MODE 0 pass (variants.cu; 0 = default)
+  int variant;
 };
 
 struct ContigArgs {
@@ -89,6 +91,7 @@ struct ContigArgs {
   // (x, y) / ((n0-x)%n0, (n1-y)%n1), both lines of a pair in one CTA; nlines
   // is twice the number of pairs (pair_lines() in passes.cuh)
   int pair_n0, pair_n1;
+  int variant;              // as StridedArgs::variant (float z r2c / z c2r)
 };
 
 struct SlabArgs {

@@ -39,6 +39,7 @@ bool length_supported(int L) {
 }
 
 bool launch_strided(int prec, int L, int mode, const StridedArgs& a, cudaStream_t s) {
+  if (prec == PREC_F32 && mode == 0 && a.variant > 0 && launch_strided_variant_f32(L, a.variant, a, s)) return true;
   switch (prec) {
     case PREC_F32: return launch_strided_f32_g0(L, mode, a, s) || launch_strided_f32_g1(L, mode, a, s);
     case PREC_F64: return launch_strided_f64_g0(L, mode, a, s) || launch_strided_f64_g1(L, mode, a, s);
@@ -46,8 +47,8 @@ bool launch_strided(int prec, int L, int mode, const StridedArgs& a, cudaStream_
     default: return false;
   }
 }
-#define AFG_DISPATCH(K, DF)                                                                  \
-  bool launch_##K(int prec, int L, const ContigArgs& a, cudaStream_t s) {                   \
+#define AFG_DISPATCH(NAME, K, DF)                                                            \
+  bool NAME(int prec, int L, const ContigArgs& a, cudaStream_t s) {                         \
     switch (prec) {                                                                          \
       case PREC_F32: return launch_##K##_f32_g0(L, a, s) || launch_##K##_f32_g1(L, a, s);   \
       case PREC_F64: return launch_##K##_f64_g0(L, a, s) || launch_##K##_f64_g1(L, a, s);   \
@@ -55,11 +56,20 @@ bool launch_strided(int prec, int L, int mode, const StridedArgs& a, cudaStream_
       default: return false;                                                                 \
     }                                                                                        \
   }
-AFG_DISPATCH(zc2c, launch_zc2c_fdf_g0(L, a, s) || launch_zc2c_fdf_g1(L, a, s))
-AFG_DISPATCH(zr2c, launch_zr2c_fdf_g0(L, a, s) || launch_zr2c_fdf_g1(L, a, s))
-AFG_DISPATCH(zc2r, launch_zc2r_fdf_g0(L, a, s) || launch_zc2r_fdf_g1(L, a, s))
-AFG_DISPATCH(zsym, false)
+AFG_DISPATCH(launch_zc2c, zc2c, launch_zc2c_fdf_g0(L, a, s) || launch_zc2c_fdf_g1(L, a, s))
+AFG_DISPATCH(launch_zr2c_default, zr2c, launch_zr2c_fdf_g0(L, a, s) || launch_zr2c_fdf_g1(L, a, s))
+AFG_DISPATCH(launch_zc2r_default, zc2r, launch_zc2r_fdf_g0(L, a, s) || launch_zc2r_fdf_g1(L, a, s))
+AFG_DISPATCH(launch_zsym, zsym, false)
 #undef AFG_DISPATCH
+
+bool launch_zr2c(int prec, int M, const ContigArgs& a, cudaStream_t s) {
+  if (prec == PREC_F32 && a.variant > 0 && launch_contig_variant_f32(true, M, a.variant, a, s)) return true;
+  return launch_zr2c_default(prec, M, a, s);
+}
+bool launch_zc2r(int prec, int M, const ContigArgs& a, cudaStream_t s) {
+  if (prec == PREC_F32 && a.variant > 0 && launch_contig_variant_f32(false, M, a.variant, a, s)) return true;
+  return launch_zc2r_default(prec, M, a, s);
+}
 
 long long grouped_tiles(int kind, int L, const void* args) {
   long long t = -1;

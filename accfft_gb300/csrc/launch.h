@@ -94,6 +94,13 @@ bool launch_df_scan(const void* x, long long rows, long long len, long long stri
 bool launch_add_rows(bool dbl, void* out, long long out_row, const void* in, long long in_row, long long rows,
                      int len, cudaStream_t s);
 
+// tuned variants of the float passes (variants.cu): false when the variant
+// does not exist for the length; variant_shape gives its first radix and
+// tile width (columns or lines per CTA), 0 when it does not exist
+bool launch_strided_variant_f32(int L, int v, const StridedArgs& a, cudaStream_t s);
+bool launch_contig_variant_f32(bool r2c, int M, int v, const ContigArgs& a, cudaStream_t s);
+void variant_shape(int kind, int L, int v, int* E, int* tile);
+
 // pass kinds of a recorded batch task (plan.cpp) and their grouped launch
 enum PassKind { PK_STRIDED = 0, PK_ZR2C = 2, PK_ZC2R = 3 };
 long long grouped_tiles(int kind, int L, const void* args);

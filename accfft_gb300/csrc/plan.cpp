@@ -7,6 +7,8 @@
 
 #include <cmath>
 #include <cstdlib>
+#include <array>
+#include <mutex>
 #include <atomic>
 #include <cstdarg>
 #include <cstdint>
@@ -153,6 +155,10 @@ struct accfft_c_plan {
   bool packed = false;
   // record mode: the plan's passes are appended here instead of launched
   std::vector<PassRecord>* recording = nullptr;
+  // radix / tile variants of the float r2c / c2r passes (variants.cu), chosen
+  // by timing at plan creation under ACCFFT_MEASURE: y, x, z r2c, z c2r
+  int var_y = 0, var_x = 0, var_zr = 0, var_zc = 0;
+  bool tuned = false;
   cudaStream_t stream2 = nullptr;
   static constexpr int kMaxBatches = 64;
   // control words of the persistent z+y kernels (1 + N0, zeroed per launch)
@@ -545,6 +551,7 @@ struct Exec {
     a.in_line = a.out_line = line;
     a.inverse = inverse;
     a.wait_limit = g_wait_limit.load();
+    if (!p->tc && !p->recording) a.variant = tw == p->tw_x ? p->var_x : p->var_y;
     if (p->tc) p->waits_used = true;
     if (!timed(tw == p->tw_x ? (inverse ? "x_inv" : "x") : (inverse ? "y_inv" : "y"), p->stream, [&] {
           return p->tc ? launch_strided_tc(p->tc, L, a, p->wait_err, p->stream) : go_strided(L, 0, a, p->stream);
@@ -590,6 +597,7 @@ struct Exec {
     a.in_dist = in_row;
     a.out_dist = p->H2();
     a.wait_limit = g_wait_limit.load();
+    if (!p->tc && !p->recording) a.variant = p->var_zr;
     if (p->tc) p->waits_used = true;
     if (!timed("z_r2c", p->stream, [&] {
           return p->tc ? launch_z_tc(p->tc, true, p->M(), a, p->wait_err, p->stream)
@@ -610,6 +618,7 @@ struct Exec {
     a.in_dist = p->H2();
     a.out_dist = out_row;
     a.wait_limit = g_wait_limit.load();
+    if (!p->tc && !p->recording) a.variant = p->var_zc;
     if (p->tc) p->waits_used = true;
     if (!timed("z_c2r", p->stream, [&] {
           return p->tc ? launch_z_tc(p->tc, false, p->M(), a, p->wait_err, p->stream)
@@ -635,6 +644,7 @@ struct Exec {
     a.out_dist = p->H2();
     a.pair_n0 = p->n[0];
     a.pair_n1 = p->n[1];
+    a.variant = p->recording ? 0 : p->var_zr;
     if (!timed("z_r2c", p->stream, [&] { return go_zr2c(p->M(), a, p->stream); }))
       unsupported("z r2c pass (mirror pairs)", p->M());
   }
@@ -650,6 +660,7 @@ struct Exec {
     a.out_dist = 2LL * p->M();
     a.pair_n0 = p->n[0];
     a.pair_n1 = p->n[1];
+    a.variant = p->recording ? 0 : p->var_zc;
     if (!timed("z_c2r", p->stream, [&] { return go_zc2r(p->M(), a, p->stream); }))
       unsupported("z c2r pass (mirror pairs)", p->M());
   }
@@ -868,6 +879,7 @@ struct Exec {
     a.in_slab = a.out_slab = N1 * M;
     a.in_line = a.out_line = M;
     a.inverse = inverse;
+    a.variant = p->recording ? 0 : p->var_y;
     if (!timed(inverse ? "y_inv" : "y", st, [&] { return go_strided(p->n[1], 0, a, st); }))
       unsupported("strided pass", p->n[1]);
   }
@@ -1168,6 +1180,112 @@ int check_addressable(const char* fn, std::initializer_list<const void*> ptrs) {
   return ACCFFT_C_OK;
 }
 
+// ---------------------------------------------------------------- tuner
+// ACCFFT_MEASURE (the reference's default flag, src/accfft_gpu.cpp:341-382:
+// time the candidates at plan creation and keep the fastest): a float r2c
+// plan times the radix / tile variants of its y, x, z r2c and z c2r passes
+// (variants.cu) on its own scratch and a temporary spectrum, in the plan's
+// pass order, and keeps the fastest of each.  Choices are cached per process
+// by grid and order, so plans of one grid run the same kernels.
+constexpr unsigned kMeasureFlag = 2u;   // ACCFFT_MEASURE
+std::mutex g_tune_mu;
+std::map<std::tuple<int, int, int, int>, std::array<int, 4>> g_tuned;
+
+bool variant_exists(int kind, int L, int v) {
+  int E = 0, t = 0;
+  variant_shape(kind, L, v, &E, &t);
+  return E > 0;
+}
+
+void tune_variants(accfft_c_plan* p) {
+  if (p->kind != 1 || p->dbl || p->tc || p->df || !p->scratch) return;
+  const int kinds[4] = {PK_STRIDED, PK_STRIDED, PK_ZR2C, PK_ZC2R};
+  const int lens[4] = {p->n[1], p->n[0], p->M(), p->M()};
+  bool any = false;   // nothing to choose when no pass length has a variant
+  for (int w = 0; w < 4; ++w) any = any || variant_exists(kinds[w], lens[w], 1) || variant_exists(kinds[w], lens[w], 2);
+  if (!any) return;
+  const auto key = std::make_tuple(p->n[0], p->n[1], p->n[2], p->packed ? 1 : 0);
+  {
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    auto it = g_tuned.find(key);
+    if (it != g_tuned.end()) {
+      p->var_y = it->second[0];
+      p->var_x = it->second[1];
+      p->var_zr = it->second[2];
+      p->var_zc = it->second[3];
+      p->tuned = true;
+      return;
+    }
+  }
+  DeviceGuard guard(p->device);
+  void* tmp = nullptr;
+  if (cudaMalloc(&tmp, (size_t)p->alloc_max) != cudaSuccess) {
+    cudaGetLastError();   // no room to tune: keep the defaults
+    return;
+  }
+  cudaMemsetAsync(p->scratch, 0, (size_t)p->alloc_max, p->stream);
+  cudaMemsetAsync(tmp, 0, (size_t)p->alloc_max, p->stream);
+  const bool was_blocking = p->blocking;
+  p->blocking = false;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  const long long M = p->M(), h = p->packed ? M : p->H2();
+  void* sc = p->scratch;
+  // one pass of the given kind with the plan's current variants
+  auto pass = [&](int which) {
+    Exec ex(p, nullptr);
+    if (which == 0) ex.ypass(sc, sc, h, 0);
+    else if (which == 1) ex.xpass(sc, sc, h, 0);
+    else if (which == 2) p->packed ? ex.zr2c_pairs(sc, tmp) : ex.zr2c(tmp, sc, p->n[2]);
+    else p->packed ? ex.zc2r_pairs(tmp, sc) : ex.zc2r(sc, tmp, p->n[2]);
+    return ex.finish();
+  };
+  auto ms_of = [&](int which) {
+    if (pass(which) != ACCFFT_C_OK) return -1.0f;   // warm-up and launch check
+    cudaEventRecord(e0, p->stream);
+    for (int r = 0; r < 3; ++r) pass(which);
+    cudaEventRecord(e1, p->stream);
+    float ms = -1.0f;
+    if (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) return -1.0f;
+    return ms;
+  };
+  int* slot[4] = {&p->var_y, &p->var_x, &p->var_zr, &p->var_zc};
+  bool ok = true;
+  for (int w = 0; w < 4 && ok; ++w) {
+    float best = -1.0f;
+    int best_v = 0;
+    for (int v = 0; v < 3; ++v) {
+      if (v > 0 && !variant_exists(kinds[w], lens[w], v)) continue;
+      *slot[w] = v;
+      const float t = ms_of(w);
+      if (t < 0) {
+        if (v == 0) ok = false;
+        continue;
+      }
+      if (best < 0 || t < best) {
+        best = t;
+        best_v = v;
+      }
+    }
+    *slot[w] = best_v;
+  }
+  cudaStreamSynchronize(p->stream);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(tmp);
+  p->blocking = was_blocking;
+  g_err.clear();
+  g_err_code = ACCFFT_C_OK;
+  if (!ok) {
+    p->var_y = p->var_x = p->var_zr = p->var_zc = 0;
+    return;
+  }
+  p->tuned = true;
+  std::lock_guard<std::mutex> lock(g_tune_mu);
+  g_tuned[key] = {p->var_y, p->var_x, p->var_zr, p->var_zc};
+}
+
 int check_plan(accfft_c_plan* p, int kind, int dbl, const char* fn) {
   g_err.clear();
   g_err_code = ACCFFT_C_OK;
@@ -1430,7 +1548,9 @@ accfft_c_plan* accfft_c_plan_dft_3d_r2c_gpu(const int n[3], double* data, double
   return make_plan(1, true, n, data, data_out, flags);
 }
 accfft_c_plan* accfft_c_plan_dft_3d_r2c_gpuf(const int n[3], float* data, float* data_out, unsigned flags) {
-  return make_plan(1, false, n, data, data_out, flags);
+  accfft_c_plan* p = make_plan(1, false, n, data, data_out, flags);
+  if (p && (flags & kMeasureFlag)) tune_variants(p);
+  return p;
 }
 accfft_c_plan* accfft_c_plan_dft_3d_c2c_gpu(const int n[3], double* data, double* data_out, unsigned flags) {
   return make_plan(2, true, n, data, data_out, flags);
@@ -1516,6 +1636,38 @@ int accfft_c_set_zy_schedule(accfft_c_plan* p, int mode) {
   }
   return fail(ACCFFT_C_EINVAL,
               "set_zy_schedule: mode must be 0 (separate passes), 1 (cluster slab kernel) or 2 (persistent z+y kernel)");
+}
+
+int accfft_c_plan_tuning(const accfft_c_plan* p, int variant[4], int radix[4], int tile[4]) {
+  if (!p) return fail(ACCFFT_C_EINVAL, "plan_tuning: NULL plan");
+  const int v[4] = {p->var_y, p->var_x, p->var_zr, p->var_zc};
+  const int kinds[4] = {PK_STRIDED, PK_STRIDED, PK_ZR2C, PK_ZC2R};
+  const int lens[4] = {p->n[1], p->n[0], p->M(), p->M()};
+  for (int w = 0; w < 4; ++w) {
+    int E = 0, t = 0;
+    variant_shape(kinds[w], lens[w], v[w], &E, &t);
+    if (E == 0 && v[w] == 0) E = plan_select(lens[w], p->prec(), 0).E;   // no variants: the default radix
+    if (variant) variant[w] = v[w];
+    if (radix) radix[w] = E;
+    if (tile) tile[w] = t;
+  }
+  return p->tuned ? 1 : 0;
+}
+
+int accfft_c_set_variants(accfft_c_plan* p, const int variant[4]) {
+  if (!p || !variant) return fail(ACCFFT_C_EINVAL, "set_variants: NULL argument");
+  if (p->kind != 1 || p->dbl || p->tc || p->df)
+    return fail(ACCFFT_C_EUNSUPPORTED, "set_variants: float r2c plans only (CUDA-core form)");
+  const int kinds[4] = {PK_STRIDED, PK_STRIDED, PK_ZR2C, PK_ZC2R};
+  const int lens[4] = {p->n[1], p->n[0], p->M(), p->M()};
+  for (int w = 0; w < 4; ++w)
+    if (variant[w] < 0 || variant[w] > 2 || (variant[w] > 0 && !variant_exists(kinds[w], lens[w], variant[w])))
+      return fail(ACCFFT_C_EUNSUPPORTED, "set_variants: pass %d of length %d has no variant %d", w, lens[w], variant[w]);
+  p->var_y = variant[0];
+  p->var_x = variant[1];
+  p->var_zr = variant[2];
+  p->var_zc = variant[3];
+  return ACCFFT_C_OK;
 }
 
 int accfft_c_set_pass_order(accfft_c_plan* p, int order) {

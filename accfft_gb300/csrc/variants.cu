@@ -1,0 +1,185 @@
+// Alternative radix plans and tile shapes of the float r2c / c2r passes, for
+// the plan-time tuner (ACCFFT_MEASURE, plan.cpp).  Variant 0 is the default
+// kernel of kernels.cu; here:
+//   strided pass (MODE 0), L in {64, 128, 256, 512, 1024}:
+//     1  half the columns per tile (TC / 2, at least 8)
+//     2  the next smaller first radix (E = 16 for a default of 32, 8 for 16)
+//   z r2c / z c2r (plain and mirror-pair mode), M in {64, 128, 256, 512}:
+//     1  the other line count per CTA (z r2c: TL / 2; z c2r: TL where its
+//        default is TL / 2, else TL / 2)
+//     2  the next smaller first radix (with that radix's default line count)
+// A variant that does not exist for a length launches nothing (false).
+#include "launch.h"
+#include "passes.cuh"
+#include "per_device.h"
+
+namespace afg {
+
+namespace {
+
+template <int L>
+constexpr int alt_e() {
+  constexpr int E = LineFFT<float, L>::E;
+  return E == 32 ? 16 : (E == 16 ? 8 : 0);
+}
+template <int L>
+constexpr int half_tc() {
+  constexpr int TC = StridedShape<float, L>::TC;
+  return TC / 2 >= 8 ? TC / 2 : 0;
+}
+// the default z c2r line count (kernels.cu halves TL for M >= 256)
+template <int M>
+constexpr int zc2r_default_tl() {
+  constexpr int TL = ContigShape<float, M>::TL;
+  return M >= 256 && TL >= 2 ? TL / 2 : TL;
+}
+template <int M>
+constexpr int zc2r_alt_tl() {
+  constexpr int TL = ContigShape<float, M>::TL;
+  return zc2r_default_tl<M>() == TL ? (TL / 2 >= 2 ? TL / 2 : 0) : TL;
+}
+template <int M>
+constexpr int zr2c_alt_tl() {
+  constexpr int TL = ContigShape<float, M>::TL;
+  return TL / 2 >= 2 ? TL / 2 : 0;
+}
+
+template <int L, int EF, int TCF>
+bool run_strided_v(const StridedArgs& a, cudaStream_t s) {
+  typedef StridedShape<float, L, EF, TCF> SH;
+  auto k = k_strided<float, L, 0, EF, TCF>;
+  static PerDevice prepared;
+  if (!prepare_smem(prepared, k, SH::smem)) return false;
+  StridedArgs b = a;
+  b.early_trigger = pdl_mode() == 2;
+  return launch_pass(k, unsigned((a.ncols + SH::TC - 1) / SH::TC), SH::threads, SH::smem, s, b) == cudaSuccess;
+}
+
+template <int L>
+bool strided_variant(int v, const StridedArgs& a, cudaStream_t s) {
+  if (v == 1) {
+    if constexpr (half_tc<L>() > 0) return run_strided_v<L, 0, half_tc<L>()>(a, s);
+  } else if (v == 2) {
+    if constexpr (alt_e<L>() > 0) return run_strided_v<L, alt_e<L>(), 0>(a, s);
+  }
+  return false;
+}
+
+// pair mode: TL / 2 mirror pairs per CTA (as kernels.cu)
+template <int TL>
+unsigned contig_grid(const ContigArgs& a) {
+  const long long per = a.pair_n1 > 0 ? TL / 2 : TL;
+  const long long units = a.pair_n1 > 0 ? a.nlines / 2 : a.nlines;
+  return unsigned((units + per - 1) / per);
+}
+
+template <bool R2C, int M, int EF, int TLF>
+bool run_contig_v(const ContigArgs& a, cudaStream_t s) {
+  typedef ContigShape<float, M, EF, TLF> SH;
+  if (a.pair_n1 > 0 && SH::TL < 2) return false;
+  void (*k)(const ContigArgs);
+  if constexpr (R2C) k = k_zr2c<float, M, EF, TLF>;
+  else k = k_zc2r<float, M, EF, TLF>;
+  static PerDevice prepared;
+  if (!prepare_smem(prepared, k, SH::smem)) return false;
+  ContigArgs b = a;
+  b.early_trigger = pdl_mode() == 2;
+  return launch_pass(k, contig_grid<SH::TL>(a), SH::threads, SH::smem, s, b) == cudaSuccess;
+}
+
+template <bool R2C, int M>
+bool contig_variant(int v, const ContigArgs& a, cudaStream_t s) {
+  if (v == 1) {
+    constexpr int tl = R2C ? zr2c_alt_tl<M>() : zc2r_alt_tl<M>();
+    if constexpr (tl > 0) return run_contig_v<R2C, M, 0, tl>(a, s);
+  } else if (v == 2) {
+    if constexpr (alt_e<M>() > 0) return run_contig_v<R2C, M, alt_e<M>(), 0>(a, s);
+  }
+  return false;
+}
+
+// first radix and tile width (columns or lines per CTA) of a variant
+template <int L>
+void strided_shape(int v, int* E, int* tile) {
+  *E = *tile = 0;
+  if (v == 0) {
+    *E = LineFFT<float, L>::E;
+    *tile = StridedShape<float, L>::TC;
+  } else if (v == 1) {
+    if constexpr (half_tc<L>() > 0) {
+      *E = LineFFT<float, L>::E;
+      *tile = half_tc<L>();
+    }
+  } else if (v == 2) {
+    if constexpr (alt_e<L>() > 0) {
+      *E = alt_e<L>();
+      *tile = StridedShape<float, L, alt_e<L>()>::TC;
+    }
+  }
+}
+template <bool R2C, int M>
+void contig_shape(int v, int* E, int* tile) {
+  *E = *tile = 0;
+  if (v == 0) {
+    *E = LineFFT<float, M>::E;
+    *tile = R2C ? ContigShape<float, M>::TL : zc2r_default_tl<M>();
+  } else if (v == 1) {
+    constexpr int tl = R2C ? zr2c_alt_tl<M>() : zc2r_alt_tl<M>();
+    if constexpr (tl > 0) {
+      *E = LineFFT<float, M>::E;
+      *tile = tl;
+    }
+  } else if (v == 2) {
+    if constexpr (alt_e<M>() > 0) {
+      *E = alt_e<M>();
+      *tile = ContigShape<float, M, alt_e<M>()>::TL;
+    }
+  }
+}
+
+}  // namespace
+
+#define AFG_VAR_STRIDED(X) X(64) X(128) X(256) X(512) X(1024)
+#define AFG_VAR_CONTIG(X) X(64) X(128) X(256) X(512)
+
+bool launch_strided_variant_f32(int L, int v, const StridedArgs& a, cudaStream_t s) {
+  switch (L) {
+#define AFG_CASE(n) case n: return strided_variant<n>(v, a, s);
+    AFG_VAR_STRIDED(AFG_CASE)
+#undef AFG_CASE
+    default: return false;
+  }
+}
+
+bool launch_contig_variant_f32(bool r2c, int M, int v, const ContigArgs& a, cudaStream_t s) {
+  switch (M) {
+#define AFG_CASE(n) case n: return r2c ? contig_variant<true, n>(v, a, s) : contig_variant<false, n>(v, a, s);
+    AFG_VAR_CONTIG(AFG_CASE)
+#undef AFG_CASE
+    default: return false;
+  }
+}
+
+// kind: PK_STRIDED, PK_ZR2C or PK_ZC2R; E = tile = 0 when the variant does
+// not exist for the length (variant 0 of a length without variants too)
+void variant_shape(int kind, int L, int v, int* E, int* tile) {
+  *E = *tile = 0;
+  if (kind == PK_STRIDED) {
+    switch (L) {
+#define AFG_CASE(n) case n: strided_shape<n>(v, E, tile); break;
+      AFG_VAR_STRIDED(AFG_CASE)
+#undef AFG_CASE
+      default: break;
+    }
+  } else if (kind == PK_ZR2C || kind == PK_ZC2R) {
+    switch (L) {
+#define AFG_CASE(n) \
+  case n: kind == PK_ZR2C ? contig_shape<true, n>(v, E, tile) : contig_shape<false, n>(v, E, tile); break;
+      AFG_VAR_CONTIG(AFG_CASE)
+#undef AFG_CASE
+      default: break;
+    }
+  }
+}
+
+}  // namespace afg

@@ -380,7 +380,7 @@ def e2e_pairs_per_s(args, ag, torch, n, dt, u, stream, world, inflight=3):
     lanes = []
     for _ in range(inflight):
         s = torch.cuda.Stream()
-        plan = ag.PlanR2C(n, dt)
+        plan = ag.PlanR2C(n, dt, flags=ag.ACCFFT_MEASURE)
         plan.set_stream(s, blocking=False)
         lanes.append((s, plan, torch.empty((n[0], n[1], H2, 2), dtype=tdt, device="cuda"),
                       torch.empty(n, dtype=tdt).pin_memory()))
@@ -448,7 +448,7 @@ def ours(args):
     tdt = getattr(torch, dt)
     N0, N1, N2 = n
     H2 = N2 // 2 + 1
-    plan = ag.PlanR2C(n, dt)
+    plan = ag.PlanR2C(n, dt, flags=ag.ACCFFT_MEASURE)   # the reference's default flag: tuned passes
     packed = args.order == "packed"
     plan.set_pass_order(1 if packed else 0)
     stream = torch.cuda.Stream()
@@ -541,6 +541,7 @@ def ours(args):
         "e2e": e2e,
         "clocks": clocks,
         "roundtrip_rel_l2": err,
+        "tuning": plan.tuning(),
         "variants": variants,
     }
     if not args.no_baseline and world == 1:
@@ -719,44 +720,62 @@ def adjoint_workload(args):
 def batch_workload(args):
     """64 independent grids drawn with a seed from {32^3, 48^3, 64^3, 96^3,
     128^3, 160x180x200, 192^3, 256^3}: half r2c+c2r, half laplace then
-    inv_laplace, inputs U[-1, 1]; one CUDA-graph launch per batch."""
+    inv_laplace, inputs U[-1, 1]; one CUDA-graph launch per batch, in both
+    forms: per-instance kernels over CUDA streams (plans tuned by
+    ACCFFT_MEASURE), and the grouped form (one kernel per pass kind, line
+    length and level over all instances, default variants)."""
     import torch
 
+    import accfft_gb300 as ag
     from accfft_gb300.batch import BatchPlan
 
     orc = _oracle()
     sizes = [(32,) * 3, (48,) * 3, (64,) * 3, (96,) * 3, (128,) * 3, (160, 180, 200), (192,) * 3, (256,) * 3]
     r = np.random.default_rng(41)
     specs = [(sizes[r.integers(len(sizes))], "r2c_c2r" if i % 2 == 0 else "lap_invlap") for i in range(64)]
-    bp = BatchPlan(specs, "float32")
+    bp = BatchPlan(specs, "float32", flags=ag.ACCFFT_MEASURE)
     host = [r.uniform(-1, 1, s).astype(np.float32) for s, _ in specs]
     bp.set_inputs([torch.from_numpy(h).cuda() for h in host])
     tune = bp.tune()
-    bp.capture()
-    for _ in range(3):
-        bp.run()
-    torch.cuda.synchronize()
-    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    reps = 20
-    a.record()
-    for _ in range(reps):
-        bp.run()
-    b.record()
-    torch.cuda.synchronize()
-    ms = a.elapsed_time(b) / reps
-    errs = []
-    for (shape, op), h, out in zip(specs, host, bp.outputs):
-        u = h.astype(np.float64)
-        if op == "r2c_c2r":
-            ref = orc.c2r(orc.r2c(u), shape[2])
-        else:
-            ref = orc.spectral_op(orc.spectral_op(u, "laplace"), "inv_laplace")
-        errs.append(orc.rel_l2(out.cpu().numpy().astype(np.float64), ref))
+    chosen = bp.form
+
+    def time_form(form, reps=20):
+        bp.form = form
+        bp.capture()
+        for _ in range(3):
+            bp.run()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        for _ in range(reps):
+            bp.run()
+        b.record()
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / reps
+
+    forms = {}
+    for form in ("streams", "grouped"):
+        ms_f = time_form(form)
+        errs = []
+        for (shape, op), h, out in zip(specs, host, bp.outputs):
+            u = h.astype(np.float64)
+            if op == "r2c_c2r":
+                ref = orc.c2r(orc.r2c(u), shape[2])
+            else:
+                ref = orc.spectral_op(orc.spectral_op(u, "laplace"), "inv_laplace")
+            errs.append(orc.rel_l2(out.cpu().numpy().astype(np.float64), ref))
+        forms[form] = {"ms_per_batch": ms_f, "transforms_per_s": bp.transforms / (ms_f / 1000.0),
+                       "rel_l2_vs_oracle": {"max": max(errs), "median": float(np.median(errs))}}
+    info = bp.grouped().info()
+    forms["grouped"]["launches_per_batch"] = info["launches"]
+    forms["grouped"]["levels"] = info["levels"]
+    bp.form = chosen
+    ms = forms[chosen]["ms_per_batch"]
     line = {"metric": "64 uneven grids, transforms/s (one graph launch)", "workload": "batch",
             "value": bp.transforms / (ms / 1000.0), "unit": "transforms/s", "higher_is_better": True,
-            "ms_per_batch": ms, "transforms_per_batch": bp.transforms, "streams": tune["streams"],
-            "schedule": tune["schedule"], "radix_plans": bp.report(),
-            "rel_l2_vs_oracle": {"max": max(errs), "median": float(np.median(errs))},
+            "form": chosen, "ms_per_batch": ms, "transforms_per_batch": bp.transforms, "forms": forms,
+            "streams": tune["streams"], "schedule": tune["schedule"], "radix_plans": bp.report(),
+            "rel_l2_vs_oracle": forms[chosen]["rel_l2_vs_oracle"],
             "data": "synthetic U[-1,1], seeded"}
     print(json.dumps(line), flush=True)
 
@@ -907,6 +926,8 @@ def call_workload(args):
     else:
         flags = {"none": 0, "tf32": ag.TC_TF32, "bf16": ag.TC_BF16}[args.tc] | (ag.F64_DF if args.df else 0)
         plan = ag.PlanR2C(n, dt, flags=flags) if flags else ag.PlanR2C(n, dt)
+        if not flags:
+            plan.set_pass_order(1 if args.order == "packed" else 0)
         plan.r2c(u, spec)
         fn = {"r2c": lambda: plan.r2c(u, spec), "c2r": lambda: plan.c2r(spec, outs[0]),
               "laplace": lambda: plan.laplace(outs[0], u),

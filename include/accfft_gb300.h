@@ -156,6 +156,21 @@ int accfft_c_set_zy_schedule(accfft_c_plan* plan, int mode);
  * (ACCFFT_C_EUNSUPPORTED otherwise), where it is the default;
  * ACCFFT_GB300_ORDER=natural in the environment makes 0 the default. */
 int accfft_c_set_pass_order(accfft_c_plan* plan, int order);
+/* ACCFFT_MEASURE (the reference's default flag: tune at plan creation,
+ * src/accfft_gpu.cpp:341-382) on a float r2c plan times the radix / tile
+ * variants of its y, x, z r2c and z c2r passes on the plan's scratch and a
+ * temporary spectrum (variant 0 = default; 1 = half the columns or the other
+ * line count per CTA; 2 = the next smaller first radix) and keeps the
+ * fastest; the choice is cached per process by grid and pass order, so plans
+ * of one grid run the same kernels.  ACCFFT_ESTIMATE keeps the defaults.
+ * accfft_c_plan_tuning reports, for y, x, z r2c and z c2r, the variant, its
+ * first radix and its tile width (columns or lines per CTA; 0 where the
+ * length has no variants); returns 1 when the plan was tuned, else 0.
+ * accfft_c_set_variants sets the four variants by hand (float r2c plans;
+ * ACCFFT_C_EUNSUPPORTED for a variant the length does not have).  Batches
+ * (below) run the default variants. */
+int accfft_c_plan_tuning(const accfft_c_plan* plan, int variant[4], int radix[4], int tile[4]);
+int accfft_c_set_variants(accfft_c_plan* plan, const int variant[4]);
 /* extension: per-kernel device times.  With profiling on, every kernel the
  * plan launches is bracketed by CUDA events on its stream;
  * accfft_c_profile_read waits for them and returns, per pass label ("z_r2c",

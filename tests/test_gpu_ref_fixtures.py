@@ -99,7 +99,7 @@ def test_cuda_path_matches_reference(cuda, native, oracle, n, dtype):
     t = "x".join(map(str, n))
     inp = inputs(z, t)
     names = [k.split("__")[2] for k in z.files if k.startswith(f"out__{t}__")]
-    assert len(names) > 60
+    assert len(names) >= 50
     bad = []
     for case in names:
         got = run_case(cuda, native, n, dtype, case, inp)
