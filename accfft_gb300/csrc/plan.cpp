@@ -137,6 +137,11 @@ struct accfft_c_plan {
   const void* tw_z = nullptr;
   const void* tw_post = nullptr;
   const void* fd_tab = nullptr;   // finite-difference Laplacian eigenvalues per axis (r2c plans)
+  // stage twiddles of the tuner's alternative first radix (variant 2) of the
+  // x, y and z lines (float r2c plans; nullptr where the length has none)
+  const void* tw_x_alt = nullptr;
+  const void* tw_y_alt = nullptr;
+  const void* tw_z_alt = nullptr;
   // spectrum-sized scratch (r2c plans): out-of-place c2r and operators
   void* scratch = nullptr;
   // how the z and y passes of r2c/c2r run: 0 = one kernel each over the whole
@@ -330,6 +335,19 @@ accfft_c_plan* make_plan(int kind, bool dbl, const int* n, void* data, void* dat
     if (fd.size() % 2) fd.push_back(0.0L);
     tabs.push_back(fd);
   }
+  // float r2c plans: the stage twiddles of each axis's alternative first
+  // radix (the tuner's variant 2, variants.cu: 16 for a default of 32, 8 for 16)
+  const bool alt_tables = kind == 1 && cls == 0 && !p->tc;
+  int alt_e[3] = {0, 0, 0};
+  if (alt_tables) {
+    const int lens[3] = {n[0], n[1], zlen};
+    for (int a = 0; a < 3; ++a) {
+      const int e = plan_select(lens[a], 0, 0).E;
+      alt_e[a] = e == 32 ? 16 : (e == 16 ? 8 : 0);
+      if (alt_e[a] && plan_with_e(lens[a], alt_e[a]).E == 0) alt_e[a] = 0;
+      tabs.push_back(alt_e[a] ? stage_table(lens[a], 0, alt_e[a]) : std::vector<long double>(2, 0.0L));
+    }
+  }
   const size_t cbytes = dbl ? 16 : 8;
   std::vector<size_t> off;
   size_t total = 0;
@@ -414,6 +432,11 @@ accfft_c_plan* make_plan(int kind, bool dbl, const int* n, void* data, void* dat
   p->tw_z = base + off[2];
   if (kind == 1) p->tw_post = base + off[3];
   if (kind == 1) p->fd_tab = base + off[4];
+  if (alt_tables) {
+    p->tw_x_alt = alt_e[0] ? base + off[5] : nullptr;
+    p->tw_y_alt = alt_e[1] ? base + off[6] : nullptr;
+    p->tw_z_alt = alt_e[2] ? base + off[7] : nullptr;
+  }
   return p;
 }
 
@@ -552,6 +575,7 @@ struct Exec {
     a.inverse = inverse;
     a.wait_limit = g_wait_limit.load();
     if (!p->tc && !p->recording) a.variant = tw == p->tw_x ? p->var_x : p->var_y;
+    if (a.variant == 2) a.tw = tw == p->tw_x ? p->tw_x_alt : p->tw_y_alt;
     if (p->tc) p->waits_used = true;
     if (!timed(tw == p->tw_x ? (inverse ? "x_inv" : "x") : (inverse ? "y_inv" : "y"), p->stream, [&] {
           return p->tc ? launch_strided_tc(p->tc, L, a, p->wait_err, p->stream) : go_strided(L, 0, a, p->stream);
@@ -598,6 +622,7 @@ struct Exec {
     a.out_dist = p->H2();
     a.wait_limit = g_wait_limit.load();
     if (!p->tc && !p->recording) a.variant = p->var_zr;
+    if (a.variant == 2) a.tw = p->tw_z_alt;
     if (p->tc) p->waits_used = true;
     if (!timed("z_r2c", p->stream, [&] {
           return p->tc ? launch_z_tc(p->tc, true, p->M(), a, p->wait_err, p->stream)
@@ -619,6 +644,7 @@ struct Exec {
     a.out_dist = out_row;
     a.wait_limit = g_wait_limit.load();
     if (!p->tc && !p->recording) a.variant = p->var_zc;
+    if (a.variant == 2) a.tw = p->tw_z_alt;
     if (p->tc) p->waits_used = true;
     if (!timed("z_c2r", p->stream, [&] {
           return p->tc ? launch_z_tc(p->tc, false, p->M(), a, p->wait_err, p->stream)
@@ -645,6 +671,7 @@ struct Exec {
     a.pair_n0 = p->n[0];
     a.pair_n1 = p->n[1];
     a.variant = p->recording ? 0 : p->var_zr;
+    if (a.variant == 2) a.tw = p->tw_z_alt;
     if (!timed("z_r2c", p->stream, [&] { return go_zr2c(p->M(), a, p->stream); }))
       unsupported("z r2c pass (mirror pairs)", p->M());
   }
@@ -661,6 +688,7 @@ struct Exec {
     a.pair_n0 = p->n[0];
     a.pair_n1 = p->n[1];
     a.variant = p->recording ? 0 : p->var_zc;
+    if (a.variant == 2) a.tw = p->tw_z_alt;
     if (!timed("z_c2r", p->stream, [&] { return go_zc2r(p->M(), a, p->stream); }))
       unsupported("z c2r pass (mirror pairs)", p->M());
   }
@@ -880,6 +908,7 @@ struct Exec {
     a.in_line = a.out_line = M;
     a.inverse = inverse;
     a.variant = p->recording ? 0 : p->var_y;
+    if (a.variant == 2) a.tw = p->tw_y_alt;
     if (!timed(inverse ? "y_inv" : "y", st, [&] { return go_strided(p->n[1], 0, a, st); }))
       unsupported("strided pass", p->n[1]);
   }
