@@ -187,8 +187,12 @@ struct accfft_c_plan {
   // main [N0][N1][M] (rows of M = N2/2 complex, 128-byte aligned) and the
   // Nyquist plane [N0][N1] (kz = N2/2) after it
   bool split = false;
-  // tensor-core form (ACCFFT_C_TC_*): 0 none, 1 3xTF32, 2 split BF16
+  // tensor-core form (ACCFFT_C_TC_*): 0 none, 1 3xTF32, 2 split BF16;
+  // tc_narrow: its kernels run as four 128-thread CTAs per SM instead of two
+  // 256-thread CTAs (ACCFFT_GB300_TC_CTA = 128 | 256)
   int tc = 0;
+  bool tc_narrow = false;
+  int tc_form() const { return tc | (tc_narrow ? kTcNarrow : 0); }
   // device word set by a kernel whose bounded wait gave up (tensor-core
   // completion waits, the persistent z+y kernel's waits between items).  It
   // stays set until a blocking or timed call (or accfft_c_check) reads and
@@ -298,6 +302,7 @@ accfft_c_plan* make_plan(int kind, bool dbl, const int* n, void* data, void* dat
   auto* p = new accfft_c_plan;
   p->kind = kind;
   p->tc = tcf == ACCFFT_C_TC_TF32 ? 1 : tcf == ACCFFT_C_TC_BF16 ? 2 : 0;
+  if (const char* w = getenv("ACCFFT_GB300_TC_CTA")) p->tc_narrow = atoi(w) == 128;
   p->df = (flags & ACCFFT_C_F64_DF) != 0;
   p->dbl = dbl;
   for (int i = 0; i < 3; ++i) p->n[i] = n[i];
@@ -578,7 +583,7 @@ struct Exec {
     if (a.variant == 2) a.tw = tw == p->tw_x ? p->tw_x_alt : p->tw_y_alt;
     if (p->tc) p->waits_used = true;
     if (!timed(tw == p->tw_x ? (inverse ? "x_inv" : "x") : (inverse ? "y_inv" : "y"), p->stream, [&] {
-          return p->tc ? launch_strided_tc(p->tc, L, a, p->wait_err, p->stream) : go_strided(L, 0, a, p->stream);
+          return p->tc ? launch_strided_tc(p->tc_form(), L, a, p->wait_err, p->stream) : go_strided(L, 0, a, p->stream);
         }))
       unsupported("strided pass", L);
   }
@@ -625,7 +630,7 @@ struct Exec {
     if (a.variant == 2) a.tw = p->tw_z_alt;
     if (p->tc) p->waits_used = true;
     if (!timed("z_r2c", p->stream, [&] {
-          return p->tc ? launch_z_tc(p->tc, true, p->M(), a, p->wait_err, p->stream)
+          return p->tc ? launch_z_tc(p->tc_form(), true, p->M(), a, p->wait_err, p->stream)
                        : go_zr2c(p->M(), a, p->stream);
         }))
       unsupported("z r2c pass", p->M());
@@ -647,7 +652,7 @@ struct Exec {
     if (a.variant == 2) a.tw = p->tw_z_alt;
     if (p->tc) p->waits_used = true;
     if (!timed("z_c2r", p->stream, [&] {
-          return p->tc ? launch_z_tc(p->tc, false, p->M(), a, p->wait_err, p->stream)
+          return p->tc ? launch_z_tc(p->tc_form(), false, p->M(), a, p->wait_err, p->stream)
                        : go_zc2r(p->M(), a, p->stream);
         }))
       unsupported("z c2r pass", p->M());
