@@ -67,6 +67,8 @@ def parse():
                     help="non-cubic grid N0 N1 N2 (smaller cases of the same kernels for profiling)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--inflight", type=int, default=3, help="e2e: pairs in flight (plans on their own streams)")
+    ap.add_argument("--e2e-order", default="free", choices=["free", "ordered"],
+                    help="e2e: ordered makes each step's r2c (c2r) wait for the previous step's r2c (c2r)")
     ap.add_argument("--dtype", default="float32", choices=["float32", "float64"])
     ap.add_argument("--order", default="packed", choices=["packed", "natural"],
                     help="pass order of the r2c/c2r plan (accfft_c_set_pass_order)")
@@ -131,13 +133,22 @@ def algorithmic_bytes(n, esz, packed=False):
     }
 
 
-# dram__bytes_read.sum + dram__bytes_write.sum per launch, from one ncu
-# capture of this bench's own launches (the gpu__time_duration launch list
-# plus the two DRAM counters, one pass each, on the full-size workload),
-# keyed by (grid, dtype, pass order); writes still in L2 at the end of a
-# launch reach DRAM during the next one.  Re-captured whenever the kernels of
-# that configuration change.
+# dram__bytes_read.sum + dram__bytes_write.sum per launch from ncu captures
+# of this bench's own pair, keyed by (grid, dtype, pass order); writes still
+# in L2 at the end of a launch reach DRAM during the next one.
+#  packed:  captured on the 256x512x512 pair (bench.py --grid 256 512 512
+#           --steps 2 --warmup 3 --no-baseline --no-e2e --no-variants
+#           --passes 0 0 1 0; ncu -k regex:^k_ -s <launches before the timed
+#           region> -c 6 --metrics dram__bytes_read.sum,dram__bytes_write.sum)
+#           and doubled: the y, y_inv, z r2c and z c2r kernels are the 512^3
+#           ones with half the lines (the 256-point x kernel is not, so x has
+#           no entry)
+#  natural: captured on the 512^3 pair itself
 TRAFFIC = {
+    ((512, 512, 512), "float32", "packed"): {
+        "y": 2 * (268477440 + 214541568), "z_r2c": 2 * (268498432 + 211163648),
+        "z_c2r": 2 * (269526016 + 213707008), "y_inv": 2 * (268482048 + 212558848),
+    },
     ((512, 512, 512), "float32", "natural"): {
         "z_r2c": 537037056 + 479984384, "y": 539036672 + 480273664, "x": 539024384 + 475256320,
         "x_inv": 539027712 + 484878080, "y_inv": 539026176 + 480036096, "z_c2r": 539017728 + 481038080,
@@ -436,14 +447,19 @@ def link_probe(torch, hu, hb, reps=4):
     return {"h2d_GBps": rates[0], "d2h_GBps": rates[1], "both_directions": True, "floor_ms_per_pair": floor_ms}
 
 
-def e2e_pairs_per_s(args, ag, torch, n, dt, u, stream, world, inflight=3):
+def e2e_pairs_per_s(args, ag, torch, n, dt, u, stream, world, inflight=3, ordered=None):
     """pairs/s through the public r2c / c2r calls with the real field in pinned
     host memory: every step the r2c reads the field from the host and the c2r
     writes the result back to the host (copy-engine slab batches staged
     through each plan's device ring, overlapped with the z and y kernels).
     Steps alternate over `inflight` plans on their own streams, so one
     step's host-to-device copies overlap an earlier step's device-to-host
-    copies (the link is full duplex)."""
+    copies (the link is full duplex).  ordered: each r2c also waits for the
+    previous step's r2c, and each c2r for the previous step's c2r (events
+    between the streams), so the host-to-device copies of consecutive steps
+    take turns on the link instead of sharing it, and likewise the
+    device-to-host copies."""
+    ordered = args.e2e_order == "ordered" if ordered is None else ordered
     tdt = getattr(torch, dt)
     H2 = n[2] // 2 + 1
     hu = torch.empty(n, dtype=tdt).pin_memory()
@@ -461,10 +477,21 @@ def e2e_pairs_per_s(args, ag, torch, n, dt, u, stream, world, inflight=3):
         start.record(stream)
         for s, *_ in lanes:
             s.wait_event(start)
+        prev_r2c = prev_c2r = None
         for k in range(ksteps):
             s, plan, spec, hb = lanes[k % inflight]
+            if ordered and prev_r2c is not None:
+                s.wait_event(prev_r2c)
             plan.r2c(hu, spec)
+            if ordered:
+                prev_r2c = torch.cuda.Event()
+                prev_r2c.record(s)
+                if prev_c2r is not None:
+                    s.wait_event(prev_c2r)
             plan.c2r(spec, hb)
+            if ordered:
+                prev_c2r = torch.cuda.Event()
+                prev_c2r.record(s)
         for s, *_ in lanes:
             done = torch.cuda.Event()
             done.record(s)
@@ -498,7 +525,8 @@ def e2e_pairs_per_s(args, ag, torch, n, dt, u, stream, world, inflight=3):
             "d2h_bytes_per_step": int(hu.numel() * esz), "ms_per_step": e2e_ms, "link": link,
             "host_enqueue_ms_per_step": enqueue_ms,
             "path": f"pinned host field copied in 4 slab batches each way through a device staging ring; "
-                    f"{inflight} pairs in flight on {inflight} streams"}
+                    f"{inflight} pairs in flight on {inflight} streams"
+                    + ("; r2c calls and c2r calls each in step order across the streams" if ordered else "")}
 
 
 def ours(args):
