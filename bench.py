@@ -143,15 +143,10 @@ def algorithmic_bytes(n, esz, packed=False):
 #           and doubled: the y, y_inv, z r2c and z c2r kernels are the 512^3
 #           ones with half the lines (the 256-point x kernel is not, so x has
 #           no entry)
-#  natural: captured on the 512^3 pair itself
 TRAFFIC = {
     ((512, 512, 512), "float32", "packed"): {
         "y": 2 * (268477440 + 214541568), "z_r2c": 2 * (268498432 + 211163648),
         "z_c2r": 2 * (269526016 + 213707008), "y_inv": 2 * (268482048 + 212558848),
-    },
-    ((512, 512, 512), "float32", "natural"): {
-        "z_r2c": 537037056 + 479984384, "y": 539036672 + 480273664, "x": 539024384 + 475256320,
-        "x_inv": 539027712 + 484878080, "y_inv": 539026176 + 480036096, "z_c2r": 539017728 + 481038080,
     },
 }
 
