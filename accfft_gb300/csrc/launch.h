@@ -75,9 +75,6 @@ bool launch_slab(bool dbl, int N1, int N2, bool forward, const SlabArgs& a, cuda
 // length); err is a device word set when a completion wait gave up (after
 // a.wait_limit polls)
 bool tc_length_supported(int len, bool contig);
-// form: 1 3xTF32, 2 split BF16, | kTcNarrow for four 128-thread CTAs per SM
-// (instead of two 256-thread CTAs)
-constexpr int kTcNarrow = 16;
 bool launch_strided_tc(int form, int L, const StridedArgs& a, int* err, cudaStream_t s);
 bool launch_z_tc(int form, bool r2c, int M, const ContigArgs& a, int* err, cudaStream_t s);
 

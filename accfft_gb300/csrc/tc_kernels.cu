@@ -13,49 +13,42 @@
 namespace afg {
 
 // Shared memory of a tensor-core CTA: the exchange buffer of the line engine
-// plus the engine's B operands; at least tc_smem_floor() so that no more CTAs
-// share an SM than its 512 tensor-memory columns hold (each 128-row block
-// takes 128 columns: four 128-thread CTAs, two 256-thread CTAs, one
-// 512-thread CTA; 228 KB of shared memory per SM)
+// plus the engine's B operands; at least kTcSmemFloor per 256 threads so that
+// no more CTAs share an SM than its 512 tensor-memory columns hold (each
+// 128-row block takes 128 columns: two 256-thread CTAs, one 512-thread CTA)
 template <int THREADS>
 constexpr size_t tc_smem_floor() {
-  return THREADS <= 128 ? size_t(52) * 1024 : THREADS <= 256 ? size_t(80) * 1024 : size_t(120) * 1024;
+  return THREADS <= 256 ? size_t(80) * 1024 : size_t(120) * 1024;
 }
 
 // CTAs per SM the register budget aims at (as many as tensor memory holds)
 template <int THREADS>
 constexpr int tc_min_blocks() {
-  return THREADS <= 128 ? 4 : THREADS <= 256 ? 2 : 1;
+  return THREADS <= 256 ? 2 : 1;
 }
 
-// Two CTA widths W: 256 threads (two CTAs per SM, each issuing the products
-// of two 128-row blocks at once) and 128 threads (four CTAs per SM, one block
-// each: twice the independent round trips per SM to hide the latency of a
-// stage's store - product - load).  Lines of 1024 keep 512 threads.
-// strided tiles: TC columns x L
-template <int L, TcForm F, int W = 256> struct TcStridedShape {
+// strided tiles: TC columns x L, 256 threads for L <= 512 (512 for 1024)
+template <int L, TcForm F> struct TcStridedShape {
   static constexpr int P = L / 16;
-  static constexpr int TC = L >= 1024 ? 8 : W == 256 ? (P >= 32 ? 8 : 16) : W / P;
+  static constexpr int TC = P >= 32 ? 8 : 16;
   static constexpr int threads = P * TC;
-  static_assert(threads % 128 == 0, "tensor-core CTAs hold whole 128-row blocks");
   static constexpr size_t exch = size_t(L) * TC * sizeof(float2);
   static constexpr size_t need = exch + tc_extra_smem<F>(threads);
   static constexpr size_t smem = need > tc_smem_floor<threads>() ? need : tc_smem_floor<threads>();
 };
 
-template <int M, TcForm F, int W = 256> struct TcContigShape {
-  typedef ContigShape<float, M, 16, W / LineFFT<float, M, 16>::P> CS;
+template <int M, TcForm F> struct TcContigShape {
+  typedef ContigShape<float, M, 16> CS;
   static constexpr int threads = CS::threads;
-  static_assert(threads == W, "one 16-point butterfly per thread per line position");
   static constexpr size_t exch = (CS::smem + 15) / 16 * 16;
   static constexpr size_t need = exch + tc_extra_smem<F>(threads);
   static constexpr size_t smem = need > tc_smem_floor<threads>() ? need : tc_smem_floor<threads>();
 };
 
-template <int L, TcForm F, int W>
-__global__ void __launch_bounds__(TcStridedShape<L, F, W>::threads, tc_min_blocks<TcStridedShape<L, F, W>::threads>())
+template <int L, TcForm F>
+__global__ void __launch_bounds__(TcStridedShape<L, F>::threads, tc_min_blocks<TcStridedShape<L, F>::threads>())
 k_strided_tc(const StridedArgs a, int* err) {
-  typedef TcStridedShape<L, F, W> SH;
+  typedef TcStridedShape<L, F> SH;
   typedef LineFFTTC<L, F, SH::threads> LN;
   typedef float2 V;
   constexpr int TC = SH::TC;
@@ -86,10 +79,10 @@ k_strided_tc(const StridedArgs a, int* err) {
   tc_end<SH::threads>(ctx);
 }
 
-template <int M, TcForm F, int W>
-__global__ void __launch_bounds__(TcContigShape<M, F, W>::threads, tc_min_blocks<TcContigShape<M, F, W>::threads>())
+template <int M, TcForm F>
+__global__ void __launch_bounds__(TcContigShape<M, F>::threads, tc_min_blocks<TcContigShape<M, F>::threads>())
 k_zr2c_tc(const ContigArgs a, int* err) {
-  typedef TcContigShape<M, F, W> TS;
+  typedef TcContigShape<M, F> TS;
   typedef LineFFTTC<M, F, TS::threads> LN;
   typedef typename TS::CS SH;
   typedef float2 V;
@@ -126,10 +119,10 @@ k_zr2c_tc(const ContigArgs a, int* err) {
   tc_end<TS::threads>(ctx);
 }
 
-template <int M, TcForm F, int W>
-__global__ void __launch_bounds__(TcContigShape<M, F, W>::threads, tc_min_blocks<TcContigShape<M, F, W>::threads>())
+template <int M, TcForm F>
+__global__ void __launch_bounds__(TcContigShape<M, F>::threads, tc_min_blocks<TcContigShape<M, F>::threads>())
 k_zc2r_tc(const ContigArgs a, int* err) {
-  typedef TcContigShape<M, F, W> TS;
+  typedef TcContigShape<M, F> TS;
   typedef LineFFTTC<M, F, TS::threads> LN;
   typedef typename TS::CS SH;
   typedef float2 V;
@@ -177,10 +170,10 @@ k_zc2r_tc(const ContigArgs a, int* err) {
 
 // ------------------------------------------------------------------ launches
 
-template <int L, TcForm F, int W>
+template <int L, TcForm F>
 static bool run_strided_tc(const StridedArgs& a, int* err, cudaStream_t s) {
-  typedef TcStridedShape<L, F, W> SH;
-  auto k = k_strided_tc<L, F, W>;
+  typedef TcStridedShape<L, F> SH;
+  auto k = k_strided_tc<L, F>;
   static PerDevice prepared;
   if (!prepare_smem(prepared, k, SH::smem)) return false;
   k<<<unsigned((a.ncols + SH::TC - 1) / SH::TC), SH::threads, SH::smem, s>>>(a, err);
@@ -188,10 +181,10 @@ static bool run_strided_tc(const StridedArgs& a, int* err, cudaStream_t s) {
   return true;
 }
 
-template <int M, TcForm F, bool R2C, int W>
+template <int M, TcForm F, bool R2C>
 static bool run_contig_tc(const ContigArgs& a, int* err, cudaStream_t s) {
-  typedef TcContigShape<M, F, W> SH;
-  auto k = R2C ? k_zr2c_tc<M, F, W> : k_zc2r_tc<M, F, W>;
+  typedef TcContigShape<M, F> SH;
+  auto k = R2C ? k_zr2c_tc<M, F> : k_zc2r_tc<M, F>;
   static PerDevice prepared;
   if (!prepare_smem(prepared, k, SH::smem)) return false;
   k<<<unsigned((a.nlines + SH::CS::TL - 1) / SH::CS::TL), SH::threads, SH::smem, s>>>(a, err);
@@ -199,42 +192,32 @@ static bool run_contig_tc(const ContigArgs& a, int* err, cudaStream_t s) {
   return true;
 }
 
-template <int L, int W>
-static bool strided_tc_form(int form, const StridedArgs& a, int* err, cudaStream_t s) {
-  return (form & 3) == 1 ? run_strided_tc<L, TcForm::TF32x3, W>(a, err, s)
-                         : run_strided_tc<L, TcForm::BF16x6, W>(a, err, s);
-}
-template <int M, int W>
-static bool z_tc_form(int form, bool r2c, const ContigArgs& a, int* err, cudaStream_t s) {
-  if ((form & 3) == 1)
-    return r2c ? run_contig_tc<M, TcForm::TF32x3, true, W>(a, err, s) : run_contig_tc<M, TcForm::TF32x3, false, W>(a, err, s);
-  return r2c ? run_contig_tc<M, TcForm::BF16x6, true, W>(a, err, s) : run_contig_tc<M, TcForm::BF16x6, false, W>(a, err, s);
-}
-
 bool tc_length_supported(int len, bool contig) {
   return len == 128 || len == 256 || len == 512 || (!contig && len == 1024);
 }
 
-// form: 1 3xTF32, 2 split BF16; plus kTcNarrow for 128-thread CTAs
 bool launch_strided_tc(int form, int L, const StridedArgs& a, int* err, cudaStream_t s) {
-  const bool narrow = (form & kTcNarrow) != 0;
+#define AFG_TC_S(n)                                                                          \
+  case n:                                                                                    \
+    return form == 1 ? run_strided_tc<n, TcForm::TF32x3>(a, err, s) : run_strided_tc<n, TcForm::BF16x6>(a, err, s);
   switch (L) {
-    case 128: return narrow ? strided_tc_form<128, 128>(form, a, err, s) : strided_tc_form<128, 256>(form, a, err, s);
-    case 256: return narrow ? strided_tc_form<256, 128>(form, a, err, s) : strided_tc_form<256, 256>(form, a, err, s);
-    case 512: return narrow ? strided_tc_form<512, 128>(form, a, err, s) : strided_tc_form<512, 256>(form, a, err, s);
-    case 1024: return strided_tc_form<1024, 256>(form, a, err, s);
+    AFG_TC_S(128) AFG_TC_S(256) AFG_TC_S(512) AFG_TC_S(1024)
     default: return false;
   }
+#undef AFG_TC_S
 }
 
 bool launch_z_tc(int form, bool r2c, int M, const ContigArgs& a, int* err, cudaStream_t s) {
-  const bool narrow = (form & kTcNarrow) != 0;
+#define AFG_TC_Z(n)                                                                                \
+  case n:                                                                                          \
+    if (form == 1) return r2c ? run_contig_tc<n, TcForm::TF32x3, true>(a, err, s)                  \
+                              : run_contig_tc<n, TcForm::TF32x3, false>(a, err, s);                \
+    return r2c ? run_contig_tc<n, TcForm::BF16x6, true>(a, err, s) : run_contig_tc<n, TcForm::BF16x6, false>(a, err, s);
   switch (M) {
-    case 128: return narrow ? z_tc_form<128, 128>(form, r2c, a, err, s) : z_tc_form<128, 256>(form, r2c, a, err, s);
-    case 256: return narrow ? z_tc_form<256, 128>(form, r2c, a, err, s) : z_tc_form<256, 256>(form, r2c, a, err, s);
-    case 512: return narrow ? z_tc_form<512, 128>(form, r2c, a, err, s) : z_tc_form<512, 256>(form, r2c, a, err, s);
+    AFG_TC_Z(128) AFG_TC_Z(256) AFG_TC_Z(512)
     default: return false;
   }
+#undef AFG_TC_Z
 }
 
 }  // namespace afg

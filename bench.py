@@ -307,25 +307,15 @@ def precision_variants(ag, torch, n, u, stream, reps=10):
     u64 = u.double()
     out = {}
     spec64 = None
-    tc = ag.TC_TF32 | ag.TC_BF16
-    forms = []
     for name, dt, flags in (("fp64_drop_in", "float64", 0), ("fp64_double_float", "float64", ag.F64_DF),
                             ("fp32_cuda_core", "float32", 0),
                             ("fp32_tensor_core_3xtf32", "float32", ag.TC_TF32),
                             ("fp32_tensor_core_split_bf16", "float32", ag.TC_BF16)):
-        # tensor-core forms at both CTA widths (ACCFFT_GB300_TC_CTA)
-        for cta in (("256", "128") if flags & tc else (None,)):
-            forms.append((name if cta in (None, "256") else f"{name}_cta{cta}", dt, flags, cta))
-    for name, dt, flags, cta in forms:
-        if cta:
-            os.environ["ACCFFT_GB300_TC_CTA"] = cta
         try:
             plan = ag.PlanR2C(n, dt, flags=flags) if flags else ag.PlanR2C(n, dt)
         except ag.AccfftError as e:
             out[name] = f"unavailable for this grid: {e}"
             continue
-        finally:
-            os.environ.pop("ACCFFT_GB300_TC_CTA", None)
         plan.set_stream(stream, blocking=False)
         x = u64 if dt == "float64" else u
         spec = torch.empty((N0, N1, N2 // 2 + 1, 2), dtype=x.dtype, device="cuda")

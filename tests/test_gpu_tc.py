@@ -20,15 +20,11 @@ def flag(native, form):
     return native.TC_TF32 if form == "tf32" else native.TC_BF16
 
 
-@pytest.mark.parametrize("cta", ["256", "128"])
 @pytest.mark.parametrize("form", ["tf32", "bf16"])
 @pytest.mark.parametrize("n", [(128, 128, 256), (256, 128, 512), (128, 512, 1024), (1024, 128, 256)])
-def test_tc_r2c_c2r_vs_oracle(cuda, native, oracle, monkeypatch, n, form, cta):
-    """Both CTA widths of the tensor-core kernels (ACCFFT_GB300_TC_CTA, read
-    at plan creation)."""
+def test_tc_r2c_c2r_vs_oracle(cuda, native, oracle, n, form):
     torch = cuda
     u = rng(70).standard_normal(n)
-    monkeypatch.setenv("ACCFFT_GB300_TC_CTA", cta)
     plan = native.PlanR2C(n, "float32", flags=flag(native, form))
     du = to_dev(torch, u, "float32")
     spec = empty(torch, (n[0], n[1], n[2] // 2 + 1, 2), "float32")
