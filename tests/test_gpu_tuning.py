@@ -44,7 +44,7 @@ def test_every_variant_matches_oracle(cuda, native, oracle, n, order):
             plan.c2r(spec, back)
             rt = ((back.double() / np.prod(n) - du.double()).norm() / du.double().norm()).item()
             assert rt < TOL, (w, v)
-    assert tried >= 4
+    assert tried >= 3
 
 
 def test_measure_tunes_and_caches(cuda, native, oracle):
