@@ -342,57 +342,6 @@ struct LineFFT {
     }
   }
 
-  // stages() with each shared-memory exchange done in XG rounds: in round h
-  // only the threads of group `grp` == h write and read, so the exchange
-  // buffer holds 1/XG of the tile (the caller maps its lines onto it).  The
-  // exchange buffer must be free on entry (no reads of it still pending).
-  template <int XG, class XW, class XR>
-  __device__ __forceinline__ static void stages_rounds(int t, int grp, const V* __restrict__ tw, XW&& xw, XR&& xr,
-                                                       V (&v)[E]) {
-    if constexpr (NS >= 1) Dft<E, 1>::run(v);
-    if constexpr (NS >= 2) {
-      static_for<1, NS>([&](auto s_) {
-        constexpr int s = decltype(s_)::value;
-        constexpr int Rp = pl.radix[s - 1];
-        constexpr int R = pl.radix[s];
-        constexpr int Nsp = plan_ns_before(pl, s - 1);
-        constexpr int Ns = plan_ns_before(pl, s);
-        constexpr int two = plan_tw_offset(pl, s);
-#pragma unroll
-        for (int h = 0; h < XG; ++h) {
-          if (h > 0) __syncthreads();   // the previous round's reads are done
-          if (grp == h) {
-#pragma unroll
-            for (int b = 0; b < E / Rp; ++b) {
-              const int j = t + b * P;
-              const int base = (j / Nsp) * Nsp * Rp + (j % Nsp);
-#pragma unroll
-              for (int r = 0; r < Rp; ++r) xw(base + r * Nsp, v[b * Rp + r]);
-            }
-          }
-          __syncthreads();
-          if (grp == h) {
-#pragma unroll
-            for (int b = 0; b < E / R; ++b) {
-              const int j = t + b * P;
-#pragma unroll
-              for (int r = 0; r < R; ++r) v[b * R + r] = xr(j + r * (L / R));
-            }
-          }
-        }
-        if constexpr (s < NS - 1) __syncthreads();
-#pragma unroll
-        for (int b = 0; b < E / R; ++b) {
-          const int j = t + b * P;
-          const int k = j % Ns;
-#pragma unroll
-          for (int r = 1; r < R; ++r) v[b * R + r] = c_mul(v[b * R + r], ld_tw(tw + two + (r - 1) * Ns + k));
-          Dft<R, 1>::run(v + b * R);
-        }
-      });
-    }
-  }
-
   // visit the outputs of compute() in place: f(p, value&), p = frequency index
   template <class F>
   __device__ __forceinline__ static void for_outputs(int t, V (&v)[E], F&& f) {
