@@ -433,7 +433,6 @@ __device__ __forceinline__ void pair_lines(long long q, int n0, int n1, long lon
 template <int TL>
 struct ContigSlot {
   long long row;
-  long long prow;   // the mirror line's row (this row in plain mode)
   bool valid, wr;
   int partner;   // slot holding the mirror line (the slot itself in plain mode)
   __device__ __forceinline__ ContigSlot(const ContigArgs& a, long long tile, int li) {
@@ -444,14 +443,13 @@ struct ContigSlot {
       long long i = 0, j = 0;
       pair_lines(valid ? q : 0, a.pair_n0, a.pair_n1, i, j);
       row = (li & 1) ? j : i;
-      prow = (li & 1) ? i : j;
       wr = valid && !((li & 1) && i == j);
       // the idle last slot of an odd TL has no partner slot in the CTA
       partner = li < 2 * PP ? (li ^ 1) : li;
     } else {
       const long long line = tile * TL + li;
       valid = wr = line < a.nlines;
-      row = prow = valid ? line : 0;
+      row = valid ? line : 0;
       partner = li;
     }
   }
@@ -506,33 +504,6 @@ __device__ __forceinline__ void zc2r_tile(const ContigArgs& a, long long tile) {
   const V* sp = sm + slot.partner * SH::LP;   // the mirror line's entries (pair mode), else this line's
   const MC* in = static_cast<const MC*>(a.in) + ls2 * a.in_dist;
   MC* out = reinterpret_cast<MC*>(static_cast<MR*>(a.out) + ls2 * a.out_dist);
-  const V* twp = static_cast<const V*>(a.tw_post);
-  const T wint = a.weight == 1 ? T(0.5) : T(1);
-  auto st = [&](int p, V x) { x.y = -x.y; if (slot.wr) out[p] = to_mem<T>(sh, x); };
-  if constexpr (!CG) {
-    if (a.pair_n1 > 0) {
-      // Mirror pairs: each thread reads X[p] of its line and X[M-p] of the
-      // mirror line straight from global memory for the stage-0 positions p
-      // it transforms (the mirror line's entries come through L1, where the
-      // partner's own loads brought them), so the merge needs no staging
-      // round trip through shared memory.  Same arithmetic as below.
-      const MC* inp = static_cast<const MC*>(a.in) + slot.prow * a.in_dist;
-      auto ldg = [&](int p) {
-        V xk = to_reg<T>(sh, in[p]), xm = to_reg<T>(sh, inp[M - p]);
-        if (p == 0) {
-          const V xp = to_reg<T>(sh, inp[0]), xn = to_reg<T>(sh, in[M]);
-          xk = c_make<V>(T(0.5) * (xk.x + xp.x), T(0.5) * (xk.y - xp.y));
-          xm = c_make<V>(T(0.5) * (xn.x + xm.x), T(0.5) * (xm.y - xn.y));
-        } else {
-          xk = c_scale(xk, wint);
-          xm = c_scale(xm, wint);
-        }
-        return c_conj(c2r_merge(xk, xm, c_conj(ld_tw(twp + p))));
-      };
-      LN::template run<false, false>(t, static_cast<const V*>(a.tw), ldg, st, xw, xr);
-      return;
-    }
-  }
   {
     // stage the M+1 input entries: E independent loads per thread, then the
     // Nyquist entry by thread 0
@@ -552,6 +523,8 @@ __device__ __forceinline__ void zc2r_tile(const ContigArgs& a, long long tile) {
     if (t == 0) xw(M, nyq);
   }
   __syncthreads();
+  const V* twp = static_cast<const V*>(a.tw_post);
+  const T wint = a.weight == 1 ? T(0.5) : T(1);
   // X[k] of this line with X[M-k] of the mirror line (this line in plain
   // mode).  k = 0 and k = M enter as the Hermitian parts over the pair,
   // H[k] = (X[k] + conj Xmirror[k]) / 2 (the merge takes conj H[M] as its
@@ -570,6 +543,7 @@ __device__ __forceinline__ void zc2r_tile(const ContigArgs& a, long long tile) {
     }
     return c_conj(c2r_merge(xk, xm, c_conj(ld_tw(twp + p))));
   };
+  auto st = [&](int p, V x) { x.y = -x.y; if (slot.wr) out[p] = to_mem<T>(sh, x); };
   LN::template run<false, true>(t, static_cast<const V*>(a.tw), ld, st, xw, xr);
 }
 
