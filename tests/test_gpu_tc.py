@@ -10,10 +10,11 @@ from test_gpu_transforms import empty, from_dev, to_dev
 
 pytestmark = pytest.mark.gpu
 
-# rel-L2 bounds vs the FP64 oracle: the three-way BF16 split (six products)
-# is exact for float data and drops only products below 2^-16 relative, so it
-# is held to the benchmark spec's bound 1e-6; 3xTF32 keeps about 22 bits per operand
-TOL = {"tf32": 5e-6, "bf16": 1e-6}
+# rel-L2 bounds vs the FP64 oracle, both the benchmark spec's bound 1e-6: the
+# three-way BF16 split (six products) is exact for float data and drops only
+# products below 2^-16 relative; 3xTF32 keeps about 22 bits per operand and
+# drops the lo*lo product (measured 4.5e-7 at 512^3, 4.4e-7 at 1024^3)
+TOL = {"tf32": 1e-6, "bf16": 1e-6}
 
 
 def flag(native, form):
