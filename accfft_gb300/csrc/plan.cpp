@@ -142,11 +142,6 @@ struct accfft_c_plan {
   const void* tw_x_alt = nullptr;
   const void* tw_y_alt = nullptr;
   const void* tw_z_alt = nullptr;
-  // twiddles of the two-CTA cluster form of 1024-point x and y lines (the
-  // tuner's variant 3, strided_c2.cu): w_L^k for k < L/2, then the stage
-  // table of the L/2-point plan; nullptr where the length is not 1024
-  const void* tw_x_c2 = nullptr;
-  const void* tw_y_c2 = nullptr;
   // spectrum-sized scratch (r2c plans): out-of-place c2r and operators
   void* scratch = nullptr;
   // how the z and y passes of r2c/c2r run: 0 = one kernel each over the whole
@@ -352,17 +347,6 @@ accfft_c_plan* make_plan(int kind, bool dbl, const int* n, void* data, void* dat
       if (alt_e[a] && plan_with_e(lens[a], alt_e[a]).E == 0) alt_e[a] = 0;
       tabs.push_back(alt_e[a] ? stage_table(lens[a], 0, alt_e[a]) : std::vector<long double>(2, 0.0L));
     }
-    for (int a = 0; a < 2; ++a) {
-      std::vector<long double> t(2, 0.0L);
-      if (n[a] == 1024) {
-        const int L = n[a];
-        t.assign(size_t(L), 0.0L);
-        for (int k = 0; k < L / 2; ++k) twiddle(k, L, &t[2 * k], &t[2 * k + 1]);
-        const std::vector<long double> st = stage_table(L / 2, 0);
-        t.insert(t.end(), st.begin(), st.end());
-      }
-      tabs.push_back(t);
-    }
   }
   const size_t cbytes = dbl ? 16 : 8;
   std::vector<size_t> off;
@@ -452,8 +436,6 @@ accfft_c_plan* make_plan(int kind, bool dbl, const int* n, void* data, void* dat
     p->tw_x_alt = alt_e[0] ? base + off[5] : nullptr;
     p->tw_y_alt = alt_e[1] ? base + off[6] : nullptr;
     p->tw_z_alt = alt_e[2] ? base + off[7] : nullptr;
-    p->tw_x_c2 = n[0] == 1024 ? base + off[8] : nullptr;
-    p->tw_y_c2 = n[1] == 1024 ? base + off[9] : nullptr;
   }
   return p;
 }
@@ -620,7 +602,6 @@ struct Exec {
     a.wait_limit = g_wait_limit.load();
     if (!p->tc && !p->recording) a.variant = tw == p->tw_x ? p->var_x : p->var_y;
     if (a.variant == 2) a.tw = tw == p->tw_x ? p->tw_x_alt : p->tw_y_alt;
-    if (a.variant == 3) a.tw = tw == p->tw_x ? p->tw_x_c2 : p->tw_y_c2;
     if (p->tc) p->waits_used = true;
     if (!timed(tw == p->tw_x ? (inverse ? "x_inv" : "x") : (inverse ? "y_inv" : "y"), p->stream, [&] {
           return p->tc ? launch_strided_tc(p->tc, L, a, p->wait_err, p->stream) : go_strided(L, 0, a, p->stream);
@@ -955,7 +936,6 @@ struct Exec {
     a.inverse = inverse;
     a.variant = p->recording ? 0 : p->var_y;
     if (a.variant == 2) a.tw = p->tw_y_alt;
-    if (a.variant == 3) a.tw = p->tw_y_c2;
     if (!timed(inverse ? "y_inv" : "y", st, [&] { return go_strided(p->n[1], 0, a, st); }))
       unsupported("strided pass", p->n[1]);
   }
@@ -1279,8 +1259,7 @@ void tune_variants(accfft_c_plan* p) {
   const int kinds[4] = {PK_STRIDED, PK_STRIDED, PK_ZR2C, PK_ZC2R};
   const int lens[4] = {p->n[1], p->n[0], p->M(), p->M()};
   bool any = false;   // nothing to choose when no pass length has a variant
-  for (int w = 0; w < 4; ++w)
-    for (int v = 1; v <= kMaxVariant; ++v) any = any || variant_exists(kinds[w], lens[w], v);
+  for (int w = 0; w < 4; ++w) any = any || variant_exists(kinds[w], lens[w], 1) || variant_exists(kinds[w], lens[w], 2);
   if (!any) return;
   const auto key = std::make_tuple(p->n[0], p->n[1], p->n[2], p->packed ? 1 : 0);
   {
@@ -1333,7 +1312,7 @@ void tune_variants(accfft_c_plan* p) {
   for (int w = 0; w < 4 && ok; ++w) {
     float best = -1.0f;
     int best_v = 0;
-    for (int v = 0; v <= kMaxVariant; ++v) {
+    for (int v = 0; v < 3; ++v) {
       if (v > 0 && !variant_exists(kinds[w], lens[w], v)) continue;
       *slot[w] = v;
       const float t = ms_of(w);
@@ -1739,8 +1718,7 @@ int accfft_c_set_variants(accfft_c_plan* p, const int variant[4]) {
   const int kinds[4] = {PK_STRIDED, PK_STRIDED, PK_ZR2C, PK_ZC2R};
   const int lens[4] = {p->n[1], p->n[0], p->M(), p->M()};
   for (int w = 0; w < 4; ++w)
-    if (variant[w] < 0 || variant[w] > kMaxVariant ||
-        (variant[w] > 0 && !variant_exists(kinds[w], lens[w], variant[w])))
+    if (variant[w] < 0 || variant[w] > 2 || (variant[w] > 0 && !variant_exists(kinds[w], lens[w], variant[w])))
       return fail(ACCFFT_C_EUNSUPPORTED, "set_variants: pass %d of length %d has no variant %d", w, lens[w], variant[w]);
   p->var_y = variant[0];
   p->var_x = variant[1];
