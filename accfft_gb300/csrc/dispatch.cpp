@@ -39,7 +39,10 @@ bool length_supported(int L) {
 }
 
 bool launch_strided(int prec, int L, int mode, const StridedArgs& a, cudaStream_t s) {
-  if (prec == PREC_F32 && mode == 0 && a.variant > 0 && launch_strided_variant_f32(L, a.variant, a, s)) return true;
+  if (prec == PREC_F32 && mode == 0 && a.variant > 0) {
+    if (launch_strided_variant_f32(L, a.variant, a, s)) return true;
+    if (a.variant == 2) return false;   // a.tw holds the alternative radix's twiddles
+  }
   switch (prec) {
     case PREC_F32: return launch_strided_f32_g0(L, mode, a, s) || launch_strided_f32_g1(L, mode, a, s);
     case PREC_F64: return launch_strided_f64_g0(L, mode, a, s) || launch_strided_f64_g1(L, mode, a, s);
@@ -63,11 +66,17 @@ AFG_DISPATCH(launch_zsym, zsym, false)
 #undef AFG_DISPATCH
 
 bool launch_zr2c(int prec, int M, const ContigArgs& a, cudaStream_t s) {
-  if (prec == PREC_F32 && a.variant > 0 && launch_contig_variant_f32(true, M, a.variant, a, s)) return true;
+  if (prec == PREC_F32 && a.variant > 0) {
+    if (launch_contig_variant_f32(true, M, a.variant, a, s)) return true;
+    if (a.variant == 2) return false;   // a.tw holds the alternative radix's twiddles
+  }
   return launch_zr2c_default(prec, M, a, s);
 }
 bool launch_zc2r(int prec, int M, const ContigArgs& a, cudaStream_t s) {
-  if (prec == PREC_F32 && a.variant > 0 && launch_contig_variant_f32(false, M, a.variant, a, s)) return true;
+  if (prec == PREC_F32 && a.variant > 0) {
+    if (launch_contig_variant_f32(false, M, a.variant, a, s)) return true;
+    if (a.variant == 2) return false;   // a.tw holds the alternative radix's twiddles
+  }
   return launch_zc2r_default(prec, M, a, s);
 }
 
