@@ -4,9 +4,10 @@ Two forms of the same batch:
   * "streams": every instance's own kernels, forked over `streams` CUDA
     streams inside the graph;
   * "grouped": the instances' calls are recorded into an accfft_gb300.Batch
-    and run level by level, one grouped kernel per (pass kind, line length)
-    and level over the tiles of every instance (about 10 levels x a few
-    lengths instead of one launch per pass per instance).
+    and run level by level, one persistent grouped kernel per (pass kind,
+    line length) and level, whose CTAs walk the tiles of every instance's
+    pass (about 10 levels x a few lengths instead of one launch per pass per
+    instance).
 tune() times both and keeps the faster.
 
     bp = BatchPlan([((32, 32, 32), "r2c_c2r"), ((160, 180, 200), "lap_invlap"), ...])

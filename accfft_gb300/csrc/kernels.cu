@@ -104,10 +104,11 @@ static bool run_strided_grouped(const StridedArgs* tab, const long long* starts,
                                 cudaStream_t s) {
   typedef StridedShape<Real, L> SH;
   auto k = k_strided_grouped<Real, L, MODE>;
-  static PerDevice prepared;
+  static PerDevice prepared, occupancy;
   if (!prepare_smem(prepared, k, SH::smem)) return false;
-  return launch_pass(k, unsigned(grid), SH::threads, SH::smem, s, tab, starts, ntasks, int(pdl_mode() == 2)) ==
-         cudaSuccess;
+  const long long g = persistent_grid(occupancy, k, SH::threads, SH::smem, grid);
+  return g > 0 && launch_pass(k, unsigned(g), SH::threads, SH::smem, s, tab, starts, ntasks, grid,
+                              int(pdl_mode() == 2)) == cudaSuccess;
 }
 // lengths above 256 have no grouped kernel (kept out of the build)
 template <int L>
@@ -212,10 +213,11 @@ static bool run_contig_grouped(const ContigArgs* tab, const long long* starts, i
 #else
   auto k = k_zc2r_grouped<Real, L, contig_tl<L>()>;
 #endif
-  static PerDevice prepared;
+  static PerDevice prepared, occupancy;
   if (!prepare_smem(prepared, k, SH::smem)) return false;
-  return launch_pass(k, unsigned(grid), SH::threads, SH::smem, s, tab, starts, ntasks, int(pdl_mode() == 2)) ==
-         cudaSuccess;
+  const long long g = persistent_grid(occupancy, k, SH::threads, SH::smem, grid);
+  return g > 0 && launch_pass(k, unsigned(g), SH::threads, SH::smem, s, tab, starts, ntasks, grid,
+                              int(pdl_mode() == 2)) == cudaSuccess;
 }
 template <int L>
 static long long tiles_contig_if(const ContigArgs& a) {

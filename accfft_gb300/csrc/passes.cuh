@@ -555,10 +555,12 @@ k_zc2r(const ContigArgs a) {
 }
 
 // ------------------------------------------------------- grouped launches
-// One grid over the tiles of several independent tasks of one line length
-// (the same pass of many transforms of a batch): task k owns the CTAs
-// [starts[k], starts[k+1]) and reads its arguments from tab[k] in global
-// memory.  The tile bodies are the single-task kernels'.
+// One persistent grid over the tiles of several independent tasks of one
+// line length (the same pass of many transforms of a batch): task k owns the
+// tiles [starts[k], starts[k+1]) of the `total` tiles and reads its
+// arguments from tab[k] in global memory; CTA b runs tiles b, b + gridDim.x,
+// ... (a work list walked in order, at most as many CTAs as fit the GPU at
+// once).  The tile bodies are the single-task kernels'.
 __device__ __forceinline__ int group_task(const long long* __restrict__ starts, int ntasks, long long b) {
   int lo = 0, hi = ntasks - 1;
   while (lo < hi) {
@@ -571,26 +573,38 @@ __device__ __forceinline__ int group_task(const long long* __restrict__ starts, 
 
 template <typename T, int L, int MODE>
 __global__ void __launch_bounds__(StridedShape<T, L>::threads, (strided_min_blocks<T, L, 0, 0>()))
-k_strided_grouped(const StridedArgs* __restrict__ tab, const long long* __restrict__ starts, int ntasks, int early) {
+k_strided_grouped(const StridedArgs* __restrict__ tab, const long long* __restrict__ starts, int ntasks, long long total,
+                  int early) {
   PassScope scope(early);
-  const int k = group_task(starts, ntasks, blockIdx.x);
-  strided_tile<T, L, MODE>(tab[k], blockIdx.x - __ldg(starts + k));
+  for (long long b = blockIdx.x; b < total; b += gridDim.x) {
+    if (b != blockIdx.x) __syncthreads();   // the last tile's shared-memory reads are done
+    const int k = group_task(starts, ntasks, b);
+    strided_tile<T, L, MODE>(tab[k], b - __ldg(starts + k));
+  }
 }
 
 template <typename T, int M>
 __global__ void __launch_bounds__(ContigShape<T, M>::threads)
-k_zr2c_grouped(const ContigArgs* __restrict__ tab, const long long* __restrict__ starts, int ntasks, int early) {
+k_zr2c_grouped(const ContigArgs* __restrict__ tab, const long long* __restrict__ starts, int ntasks, long long total,
+               int early) {
   PassScope scope(early);
-  const int k = group_task(starts, ntasks, blockIdx.x);
-  zr2c_tile<T, M>(tab[k], blockIdx.x - __ldg(starts + k));
+  for (long long b = blockIdx.x; b < total; b += gridDim.x) {
+    if (b != blockIdx.x) __syncthreads();   // the last tile's shared-memory reads are done
+    const int k = group_task(starts, ntasks, b);
+    zr2c_tile<T, M>(tab[k], b - __ldg(starts + k));
+  }
 }
 
 template <typename T, int M, int TLF = 0>
 __global__ void __launch_bounds__(ContigShape<T, M, 0, TLF>::threads)
-k_zc2r_grouped(const ContigArgs* __restrict__ tab, const long long* __restrict__ starts, int ntasks, int early) {
+k_zc2r_grouped(const ContigArgs* __restrict__ tab, const long long* __restrict__ starts, int ntasks, long long total,
+               int early) {
   PassScope scope(early);
-  const int k = group_task(starts, ntasks, blockIdx.x);
-  zc2r_tile<T, M, 0, TLF>(tab[k], blockIdx.x - __ldg(starts + k));
+  for (long long b = blockIdx.x; b < total; b += gridDim.x) {
+    if (b != blockIdx.x) __syncthreads();   // the last tile's shared-memory reads are done
+    const int k = group_task(starts, ntasks, b);
+    zc2r_tile<T, M, 0, TLF>(tab[k], b - __ldg(starts + k));
+  }
 }
 
 // real line r2c -> i k / N -> c2r, one pass (z-direction derivative: the

@@ -41,4 +41,21 @@ inline bool prepare_smem(PerDevice& cache, K kernel, size_t smem) {
          }) == 1;
 }
 
+// CTAs of a persistent grid over `tiles` tiles: as many as fit the current
+// device at once (SMs x resident CTAs of the kernel), at most `tiles`; 0 when
+// the occupancy query fails
+template <typename K>
+inline long long persistent_grid(PerDevice& cache, K kernel, int threads, size_t smem, long long tiles) {
+  const int occ = per_device(cache, [&] {
+    int n = 0;
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kernel, threads, smem) == cudaSuccess && n > 0 ? n : -1;
+  });
+  int dev = 0, sms = 0;
+  if (occ < 1 || cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms < 1)
+    return 0;
+  const long long cap = (long long)sms * occ;
+  return tiles < cap ? tiles : cap;
+}
+
 }  // namespace afg
