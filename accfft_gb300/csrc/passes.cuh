@@ -504,6 +504,46 @@ __device__ __forceinline__ void zc2r_tile(const ContigArgs& a, long long tile) {
   const V* sp = sm + slot.partner * SH::LP;   // the mirror line's entries (pair mode), else this line's
   const MC* in = static_cast<const MC*>(a.in) + ls2 * a.in_dist;
   MC* out = reinterpret_cast<MC*>(static_cast<MR*>(a.out) + ls2 * a.out_dist);
+  const V* twp = static_cast<const V*>(a.tw_post);
+  const T wint = a.weight == 1 ? T(0.5) : T(1);
+  auto st = [&](int p, V x) { x.y = -x.y; if (slot.wr) out[p] = to_mem<T>(sh, x); };
+  if constexpr (!CG && std::is_same<T, float>::value && LN::E <= 16 && P <= 16 && 32 % (2 * P) == 0 && TL % 2 == 0) {
+    if (a.pair_n1 > 0) {
+      // Mirror pairs whose two lines share a warp (slot 2m on the lanes below
+      // slot 2m+1's).  X[M-p] of the mirror line, p = t + r*P, is the stage-0
+      // entry r' = E-1-r of the mirror line's thread t' = P-t (t != 0), or
+      // entry (E-r) mod E of its thread 0 (t = 0; r = 0 gives its X[0]), so
+      // each thread loads only its own entries and takes the mirror line's
+      // from a warp shuffle instead of staging both lines in shared memory.
+      // The same merge arithmetic as the staged path below.
+      constexpr int E = LN::E;
+      V x[E];
+#pragma unroll
+      for (int r = 0; r < E; ++r) x[r] = to_reg<T>(sh, in[t + r * P]);
+      const V xn = to_reg<T>(sh, in[M]);   // X[M] of this line (one address per line)
+      const int lane = threadIdx.x & 31;
+      const int src = ((lane ^ P) & ~(P - 1)) | ((P - t) & (P - 1));
+      auto shfl = [&](V y) { return c_make<V>(__shfl_sync(0xffffffffu, y.x, src), __shfl_sync(0xffffffffu, y.y, src)); };
+      const V pn = shfl(xn);               // X[M] of the mirror line
+      V v[E];
+#pragma unroll
+      for (int r = 0; r < E; ++r) {
+        const V xm = shfl(t == 0 ? x[(E - r) % E] : x[E - 1 - r]);
+        V xk = x[r], xq = xm;
+        if (r == 0 && t == 0) {
+          xk = c_make<V>(T(0.5) * (xk.x + xm.x), T(0.5) * (xk.y - xm.y));
+          xq = c_make<V>(T(0.5) * (xn.x + pn.x), T(0.5) * (pn.y - xn.y));
+        } else {
+          xk = c_scale(xk, wint);
+          xq = c_scale(xq, wint);
+        }
+        v[r] = c_conj(c2r_merge(xk, xq, c_conj(ld_tw(twp + t + r * P))));
+      }
+      LN::stages(t, static_cast<const V*>(a.tw), xw, xr, [] {}, v);
+      LN::emit(t, v, st);
+      return;
+    }
+  }
   {
     // stage the M+1 input entries: E independent loads per thread, then the
     // Nyquist entry by thread 0
@@ -523,8 +563,6 @@ __device__ __forceinline__ void zc2r_tile(const ContigArgs& a, long long tile) {
     if (t == 0) xw(M, nyq);
   }
   __syncthreads();
-  const V* twp = static_cast<const V*>(a.tw_post);
-  const T wint = a.weight == 1 ? T(0.5) : T(1);
   // X[k] of this line with X[M-k] of the mirror line (this line in plain
   // mode).  k = 0 and k = M enter as the Hermitian parts over the pair,
   // H[k] = (X[k] + conj Xmirror[k]) / 2 (the merge takes conj H[M] as its
@@ -543,7 +581,6 @@ __device__ __forceinline__ void zc2r_tile(const ContigArgs& a, long long tile) {
     }
     return c_conj(c2r_merge(xk, xm, c_conj(ld_tw(twp + p))));
   };
-  auto st = [&](int p, V x) { x.y = -x.y; if (slot.wr) out[p] = to_mem<T>(sh, x); };
   LN::template run<false, true>(t, static_cast<const V*>(a.tw), ld, st, xw, xr);
 }
 
