@@ -463,10 +463,44 @@ __device__ __forceinline__ void zr2c_tile(const ContigArgs& a, long long tile) {
   const MC* in = reinterpret_cast<const MC*>(static_cast<const MR*>(a.in) + slot.row * a.in_dist);
   MC* out = static_cast<MC*>(a.out) + slot.row * a.out_dist;
   auto ld = [&](int p) { return to_reg<T>(sh, in[p]); };
-  LN::template run<true, false>(t, static_cast<const V*>(a.tw), ld, xw, xw, xr);
-  __syncthreads();
   const V* twp = static_cast<const V*>(a.tw_post);
   const T wint = a.weight == 2 ? T(2) : T(1);
+  if constexpr (std::is_same<T, float>::value && LN::E <= 16 && P <= 16 && 32 % (2 * P) == 0 && TL % 2 == 0) {
+    if (a.pair_n1 > 0) {
+      // Mirror pairs whose two lines share a warp: after the transform
+      // (registers back in stage-0 order, LineFFT::to_load_order) thread t
+      // holds Z[t + r*P], and Z[M-k] of the mirror line is the mirror
+      // thread's entry r' = E-1-r (t != 0) or (E-r) mod E (t = 0), taken by
+      // warp shuffle as in zc2r_tile; the split needs no shared-memory round
+      // trip.  The same split arithmetic as the staged path below.
+      constexpr int E = LN::E;
+      V v[E];
+      LN::compute(t, static_cast<const V*>(a.tw), ld, xw, xr, [] {}, v);
+      LN::to_load_order(v);
+      const int lane = threadIdx.x & 31;
+      const int src = ((lane ^ P) & ~(P - 1)) | ((P - t) & (P - 1));
+      V zp0 = v[0];
+#pragma unroll
+      for (int r = 0; r < E; ++r) {
+        const V y = t == 0 ? v[(E - r) % E] : v[E - 1 - r];
+        const V zm = c_make<V>(__shfl_sync(0xffffffffu, y.x, src), __shfl_sync(0xffffffffu, y.y, src));
+        if (r == 0) zp0 = zm;   // Z[0] of the mirror line on thread 0
+        const int k = t + r * P;
+        V x = r2c_split(v[r], zm, ld_tw(twp + k));
+        if (k != 0) x = c_scale(x, wint);
+        if (slot.wr) out[k] = to_mem<T>(sh, x);
+      }
+      if (t == 0 && slot.wr) {
+        const V z0 = v[0], zp = zp0;
+        const V xn = c_make<V>(T(0.5) * ((z0.x + zp.x) - (z0.y + zp.y)), T(0.5) * ((z0.y - zp.y) + (z0.x - zp.x)));
+        if (a.nyq_out) static_cast<MC*>(a.nyq_out)[slot.row] = to_mem<T>(sh, xn);
+        else out[M] = to_mem<T>(sh, xn);
+      }
+      return;
+    }
+  }
+  LN::template run<true, false>(t, static_cast<const V*>(a.tw), ld, xw, xw, xr);
+  __syncthreads();
   // outputs k = t + r*P (r < E) cover 0..M-1; thread 0 also writes k = M
 #pragma unroll
   for (int r = 0; r < LN::E; ++r) {
