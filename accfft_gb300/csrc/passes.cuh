@@ -479,15 +479,11 @@ __device__ __forceinline__ void zr2c_tile(const ContigArgs& a, long long tile) {
       LN::to_load_order(v);
       const int lane = threadIdx.x & 31;
       const int src = ((lane ^ P) & ~(P - 1)) | ((P - t) & (P - 1));
-      auto shfl = [&](V y) { return c_make<V>(__shfl_sync(0xffffffffu, y.x, src), __shfl_sync(0xffffffffu, y.y, src)); };
       V zp0 = v[0];
-      // r in the order 0, E-1, 1, E-2, ... (as in zc2r_tile: short register
-      // lifetimes)
 #pragma unroll
-      for (int i = 0; i < E; ++i) {
-        const int r = (i & 1) ? E - 1 - (i >> 1) : (i >> 1);
-        const V m1 = shfl(v[E - 1 - r]), m0 = shfl(v[(E - r) % E]);
-        const V zm = t == 0 ? m0 : m1;
+      for (int r = 0; r < E; ++r) {
+        const V y = t == 0 ? v[(E - r) % E] : v[E - 1 - r];
+        const V zm = c_make<V>(__shfl_sync(0xffffffffu, y.x, src), __shfl_sync(0xffffffffu, y.y, src));
         if (r == 0) zp0 = zm;   // Z[0] of the mirror line on thread 0
         const int k = t + r * P;
         V x = r2c_split(v[r], zm, ld_tw(twp + k));
@@ -564,14 +560,9 @@ __device__ __forceinline__ void zc2r_tile(const ContigArgs& a, long long tile) {
       auto shfl = [&](V y) { return c_make<V>(__shfl_sync(0xffffffffu, y.x, src), __shfl_sync(0xffffffffu, y.y, src)); };
       const V pn = shfl(xn);               // X[M] of the mirror line
       V v[E];
-      // r in the order 0, E-1, 1, E-2, ...: entry k is used as r = k, sent
-      // as E-1-k and (E-k) mod E, all within three steps, so each x[k] dies
-      // soon after the loads and the registers peak near one line's worth
 #pragma unroll
-      for (int i = 0; i < E; ++i) {
-        const int r = (i & 1) ? E - 1 - (i >> 1) : (i >> 1);
-        const V m1 = shfl(x[E - 1 - r]), m0 = shfl(x[(E - r) % E]);
-        const V xm = t == 0 ? m0 : m1;
+      for (int r = 0; r < E; ++r) {
+        const V xm = shfl(t == 0 ? x[(E - r) % E] : x[E - 1 - r]);
         V xk = x[r], xq = xm;
         if (r == 0 && t == 0) {
           xk = c_make<V>(T(0.5) * (xk.x + xm.x), T(0.5) * (xk.y - xm.y));
