@@ -138,15 +138,15 @@ def algorithmic_bytes(n, esz, packed=False):
 # in L2 at the end of a launch reach DRAM during the next one.
 #  packed:  captured on the 256x512x512 pair (bench.py --grid 256 512 512
 #           --steps 2 --warmup 3 --no-baseline --no-e2e --no-variants
-#           --passes 0 0 1 0; ncu -k regex:^k_ -s <launches before the timed
+#           --passes 0 0 0 0; ncu -k regex:^k_ -s <launches before the timed
 #           region> -c 6 --metrics dram__bytes_read.sum,dram__bytes_write.sum)
 #           and doubled: the y, y_inv, z r2c and z c2r kernels are the 512^3
 #           ones with half the lines (the 256-point x kernel is not, so x has
 #           no entry)
 TRAFFIC = {
     ((512, 512, 512), "float32", "packed"): {
-        "y": 2 * (268477440 + 214541568), "z_r2c": 2 * (268498432 + 211163648),
-        "z_c2r": 2 * (269526016 + 213707008), "y_inv": 2 * (268482048 + 212558848),
+        "y": 2 * (268476672 + 215201792), "z_r2c": 2 * (268544000 + 212315648),
+        "z_c2r": 2 * (269545472 + 216573696), "y_inv": 2 * (268498944 + 212618752),
     },
 }
 
