@@ -127,7 +127,7 @@ def test_differentiation_workload_256_fd64(cuda, native, ag):
 
 
 def test_fp32_backward_fd_along_smooth_directions(cuda, native, ag):
-    """The benchmark spec's bound for the spectral-gradient backward, in float32:
+    """The 1e-6 bound for the spectral-gradient backward, in float32:
     256^3, the same loss as above, against FP64 central differences along 16
     smooth directions (N(0,1) fields smoothed by a Gaussian of 4 cells, like
     u itself).  Along such directions <g, v> does not cancel, so the float32

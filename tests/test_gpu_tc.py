@@ -10,7 +10,7 @@ from test_gpu_transforms import empty, from_dev, to_dev
 
 pytestmark = pytest.mark.gpu
 
-# rel-L2 bounds vs the FP64 oracle, both the benchmark spec's bound 1e-6: the
+# rel-L2 bounds vs the FP64 oracle, both 1e-6 (the FP32 form's target): the
 # three-way BF16 split (six products) is exact for float data and drops only
 # products below 2^-16 relative; 3xTF32 keeps about 22 bits per operand and
 # drops the lo*lo product (measured 4.5e-7 at 512^3, 4.4e-7 at 1024^3)
