@@ -629,6 +629,9 @@ def ours(args):
         "kernel_frac_of_peak": {lab: nbytes[lab] / (per[lab] / 1000.0) / 1e9 / peak
                                 for lab in per},
         "step_algorithmic_GBps": step_bytes / (ms_step / 1000.0) / 1e9,
+        # compulsory bytes: each transform reads its input and writes its output
+        # once, 2 (esz N + 2 esz H) per pair ("end-to-end effective" bandwidth)
+        "compulsory_GBps": 2 * (esz * N0 * N1 * N2 + 2 * esz * N0 * N1 * H2) / (ms_step / 1000.0) / 1e9,
         "gflops_5nlogn": 5 * N0 * N1 * N2 * np.log2(N0 * N1 * N2) / (ms_step / 1000.0) / 1e9,
         "e2e": e2e,
         "clocks": clocks,
