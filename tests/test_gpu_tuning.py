@@ -13,7 +13,7 @@ TOL = 1e-5
 
 
 @pytest.mark.parametrize("order", [0, 1])
-@pytest.mark.parametrize("n", [(64, 128, 256), (256, 64, 128), (128, 512, 128), (1024, 64, 512)])
+@pytest.mark.parametrize("n", [(64, 128, 256), (256, 64, 128), (128, 512, 128), (1024, 64, 512), (64, 1024, 256)])
 def test_every_variant_matches_oracle(cuda, native, oracle, n, order):
     torch = cuda
     h = (n[0], n[1], n[2] // 2 + 1)
