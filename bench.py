@@ -432,6 +432,30 @@ def link_probe(torch, hu, hb, reps=4):
     return {"h2d_GBps": rates[0], "d2h_GBps": rates[1], "both_directions": True, "floor_ms_per_pair": floor_ms}
 
 
+def buffer_rates(torch, hu, outs, reps=2):
+    """Single-direction copy rates (GB/s) of the e2e step's own pinned buffers:
+    host-to-device from the input field, device-to-host into each output
+    buffer.  A buffer the host side serves slowly shows up here."""
+    d = torch.empty_like(hu, device="cuda")
+    nbytes = hu.numel() * hu.element_size()
+
+    def rate(f):
+        f()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        for _ in range(reps):
+            f()
+        b.record()
+        torch.cuda.synchronize()
+        return reps * nbytes / (a.elapsed_time(b) / 1000.0) / 1e9
+
+    out = {"h2d_GBps": rate(lambda: d.copy_(hu, non_blocking=True)),
+           "d2h_GBps": [rate(lambda h=h: h.copy_(d, non_blocking=True)) for h in outs]}
+    del d
+    return out
+
+
 def e2e_pairs_per_s(args, ag, torch, n, dt, u, stream, world, inflight=3, ordered=None):
     """pairs/s through the public r2c / c2r calls with the real field in pinned
     host memory: every step the r2c reads the field from the host and the c2r
@@ -484,6 +508,7 @@ def e2e_pairs_per_s(args, ag, torch, n, dt, u, stream, world, inflight=3, ordere
 
     run(max(inflight, args.warmup))
     stream.synchronize()
+    buffers_before = buffer_rates(torch, hu, [lane[3] for lane in lanes])
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     ksteps = max(3, min(args.steps, 100))
@@ -506,6 +531,10 @@ def e2e_pairs_per_s(args, ag, torch, n, dt, u, stream, world, inflight=3, ordere
         plan.destroy()
     link = link_probe(torch, hu, lanes[0][3])
     link["frac"] = link["floor_ms_per_pair"] / e2e_ms
+    # the same buffers' single-direction rates just before and just after the
+    # timed region (the spread of e2e from run to run follows these)
+    link["buffers_before"] = buffers_before
+    link["buffers_after"] = buffer_rates(torch, hu, [lane[3] for lane in lanes])
     return {"value": world * 1000.0 / e2e_ms, "unit": "pairs/s", "h2d_bytes_per_step": int(hu.numel() * esz),
             "d2h_bytes_per_step": int(hu.numel() * esz), "ms_per_step": e2e_ms, "link": link,
             "host_enqueue_ms_per_step": enqueue_ms,
