@@ -481,7 +481,7 @@ def e2e_pairs_per_s(args, ag, torch, n, dt, u, stream, world, inflight=3, ordere
         lanes.append((s, plan, torch.empty((n[0], n[1], H2, 2), dtype=tdt, device="cuda"),
                       torch.empty(n, dtype=tdt).pin_memory()))
 
-    def run(ksteps):
+    def run(ksteps, marks=None):
         start = torch.cuda.Event()
         start.record(stream)
         for s, *_ in lanes:
@@ -498,6 +498,10 @@ def e2e_pairs_per_s(args, ag, torch, n, dt, u, stream, world, inflight=3, ordere
                 if prev_c2r is not None:
                     s.wait_event(prev_c2r)
             plan.c2r(spec, hb)
+            if marks is not None:
+                m = torch.cuda.Event(enable_timing=True)
+                m.record(s)
+                marks.append(m)
             if ordered:
                 prev_c2r = torch.cuda.Event()
                 prev_c2r.record(s)
@@ -516,7 +520,8 @@ def e2e_pairs_per_s(args, ag, torch, n, dt, u, stream, world, inflight=3, ordere
         torch.distributed.barrier()
     e0.record(stream)
     t_enq = time.perf_counter()
-    run(ksteps)
+    marks = []
+    run(ksteps, marks)
     enqueue_ms = (time.perf_counter() - t_enq) * 1000.0 / ksteps   # host time to issue one pair
     e1.record(stream)
     stream.synchronize()
@@ -526,6 +531,13 @@ def e2e_pairs_per_s(args, ag, torch, n, dt, u, stream, world, inflight=3, ordere
         err = ((hb / (n[0] * n[1] * n[2]) - hu).norm() / hu.norm()).item()
         assert err < (1e-5 if dt == "float32" else 1e-12), err
     e2e_ms = max_over_ranks(e0.elapsed_time(e1) / ksteps, world)
+    # completion times of the steps (each pair's c2r, on its lane's stream):
+    # the spacing of consecutive completions shows whether a slow run is
+    # slow throughout or in bursts
+    done_ms = sorted(e0.elapsed_time(m) for m in marks)
+    gaps = [b - a for a, b in zip(done_ms, done_ms[1:])]
+    step_spacing = ({"min_ms": min(gaps), "median_ms": statistics.median(gaps), "max_ms": max(gaps)}
+                    if gaps else None)
     esz = hu.element_size()
     for _, plan, *_ in lanes:
         plan.destroy()
@@ -537,7 +549,7 @@ def e2e_pairs_per_s(args, ag, torch, n, dt, u, stream, world, inflight=3, ordere
     link["buffers_after"] = buffer_rates(torch, hu, [lane[3] for lane in lanes])
     return {"value": world * 1000.0 / e2e_ms, "unit": "pairs/s", "h2d_bytes_per_step": int(hu.numel() * esz),
             "d2h_bytes_per_step": int(hu.numel() * esz), "ms_per_step": e2e_ms, "link": link,
-            "host_enqueue_ms_per_step": enqueue_ms,
+            "host_enqueue_ms_per_step": enqueue_ms, "step_spacing": step_spacing,
             "path": f"pinned host field copied in 4 slab batches each way through a device staging ring; "
                     f"{inflight} pairs in flight on {inflight} streams"
                     + ("; r2c calls and c2r calls each in step order across the streams" if ordered else "")}
