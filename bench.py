@@ -536,7 +536,8 @@ def e2e_pairs_per_s(args, ag, torch, n, dt, u, stream, world, inflight=3, ordere
     # slow throughout or in bursts
     done_ms = sorted(e0.elapsed_time(m) for m in marks)
     gaps = [b - a for a, b in zip(done_ms, done_ms[1:])]
-    step_spacing = ({"min_ms": min(gaps), "median_ms": statistics.median(gaps), "max_ms": max(gaps)}
+    step_spacing = ({"min_ms": min(gaps), "median_ms": statistics.median(gaps), "max_ms": max(gaps),
+                     "pairs_per_s_at_median": world * 1000.0 / statistics.median(gaps)}
                     if gaps else None)
     esz = hu.element_size()
     for _, plan, *_ in lanes:
