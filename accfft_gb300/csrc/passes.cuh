@@ -625,14 +625,6 @@ k_zc2r(const ContigArgs a) {
   zc2r_tile<T, M, EF, TLF>(a, blockIdx.x);
 }
 
-// k_zc2r compiled for at least MINB resident CTAs per SM (a register budget
-// of 65536 / (threads * MINB)): the tuner's occupancy variant
-template <typename T, int M, int TLF, int MINB>
-__global__ void __launch_bounds__(ContigShape<T, M, 0, TLF>::threads, MINB) k_zc2r_occ(const ContigArgs a) {
-  PassScope scope(a.early_trigger);
-  zc2r_tile<T, M, 0, TLF>(a, blockIdx.x);
-}
-
 // ------------------------------------------------------- grouped launches
 // One persistent grid over the tiles of several independent tasks of one
 // line length (the same pass of many transforms of a batch): task k owns the

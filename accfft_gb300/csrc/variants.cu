@@ -8,9 +8,6 @@
 //     1  the other line count per CTA (z r2c: TL / 2; z c2r: TL where its
 //        default is TL / 2, else TL / 2)
 //     2  the next smaller first radix (with that radix's default line count)
-//     3  z c2r: the default tile compiled for a 72-register budget (7
-//        128-thread CTAs per SM) instead of the compiler's choice: more warps
-//        to hide the loads
 // A variant that does not exist for a length launches nothing (false).
 #include "launch.h"
 #include "passes.cuh"
@@ -90,24 +87,6 @@ bool run_contig_v(const ContigArgs& a, cudaStream_t s) {
   return launch_pass(k, contig_grid<SH::TL>(a), SH::threads, SH::smem, s, b) == cudaSuccess;
 }
 
-// the default z c2r tile with a register budget of 72 a thread
-template <int M>
-constexpr int zc2r_occ_blocks() {
-  return 65536 / (ContigShape<float, M, 0, zc2r_default_tl<M>()>::threads * 72);
-}
-template <int M>
-bool run_zc2r_occ(const ContigArgs& a, cudaStream_t s) {
-  constexpr int TL = zc2r_default_tl<M>();
-  typedef ContigShape<float, M, 0, TL> SH;
-  if (a.pair_n1 > 0 && SH::TL < 2) return false;
-  auto k = k_zc2r_occ<float, M, TL, zc2r_occ_blocks<M>()>;
-  static PerDevice prepared;
-  if (!prepare_smem(prepared, k, SH::smem)) return false;
-  ContigArgs b = a;
-  b.early_trigger = pdl_mode() == 2;
-  return launch_pass(k, contig_grid<SH::TL>(a), SH::threads, SH::smem, s, b) == cudaSuccess;
-}
-
 template <bool R2C, int M>
 bool contig_variant(int v, const ContigArgs& a, cudaStream_t s) {
   if (v == 1) {
@@ -115,8 +94,6 @@ bool contig_variant(int v, const ContigArgs& a, cudaStream_t s) {
     if constexpr (tl > 0) return run_contig_v<R2C, M, 0, tl>(a, s);
   } else if (v == 2) {
     if constexpr (alt_e<M>() > 0) return run_contig_v<R2C, M, alt_e<M>(), 0>(a, s);
-  } else if (v == 3) {
-    if constexpr (!R2C && zc2r_occ_blocks<M>() >= 2) return run_zc2r_occ<M>(a, s);
   }
   return false;
 }
@@ -156,11 +133,6 @@ void contig_shape(int v, int* E, int* tile) {
     if constexpr (alt_e<M>() > 0) {
       *E = alt_e<M>();
       *tile = ContigShape<float, M, alt_e<M>()>::TL;
-    }
-  } else if (v == 3) {
-    if constexpr (!R2C && zc2r_occ_blocks<M>() >= 2) {
-      *E = LineFFT<float, M>::E;
-      *tile = zc2r_default_tl<M>();
     }
   }
 }
