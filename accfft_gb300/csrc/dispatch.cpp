@@ -41,7 +41,7 @@ bool length_supported(int L) {
 bool launch_strided(int prec, int L, int mode, const StridedArgs& a, cudaStream_t s) {
   if (prec == PREC_F32 && mode == 0 && a.variant > 0) {
     if (launch_strided_variant_f32(L, a.variant, a, s)) return true;
-    if (a.variant >= 2) return false;   // a.tw holds the alternative radix's twiddles
+    if (a.variant == 2) return false;   // a.tw holds the alternative radix's twiddles
   }
   switch (prec) {
     case PREC_F32: return launch_strided_f32_g0(L, mode, a, s) || launch_strided_f32_g1(L, mode, a, s);

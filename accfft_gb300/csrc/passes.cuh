@@ -197,10 +197,7 @@ constexpr int strided_min_blocks() {
              ? ((LineFFT<T, L, EF>::E <= 8 && StridedShape<T, L, EF, TCF>::threads >= 64)
                     ? 1024 / StridedShape<T, L, EF, TCF>::threads
                     : 1)
-             : ((sizeof(T) == 4 && L >= 512 && StridedShape<T, L, EF, TCF>::threads <= 256) ? 2
-                : (sizeof(T) == 4 && L >= 1024 && EF > 0 && EF <= 16 && StridedShape<T, L, EF, TCF>::threads == 512)
-                    ? 2   // radix-16 first stages of long lines in 512-thread tiles: two CTAs at 64 registers
-                    : 1);
+             : ((sizeof(T) == 4 && L >= 512 && StridedShape<T, L, EF, TCF>::threads <= 256) ? 2 : 1);
 }
 // One column tile of the strided pass (the body of k_strided; also run by the
 // persistent z+y kernels).  CG loads the input through L2 only.

@@ -601,8 +601,7 @@ struct Exec {
     a.inverse = inverse;
     a.wait_limit = g_wait_limit.load();
     if (!p->tc && !p->recording) a.variant = tw == p->tw_x ? p->var_x : p->var_y;
-    // variants 2 and 3 start with the alternative radix
-    if (a.variant == 2 || a.variant == 3) a.tw = tw == p->tw_x ? p->tw_x_alt : p->tw_y_alt;
+    if (a.variant == 2) a.tw = tw == p->tw_x ? p->tw_x_alt : p->tw_y_alt;
     if (p->tc) p->waits_used = true;
     if (!timed(tw == p->tw_x ? (inverse ? "x_inv" : "x") : (inverse ? "y_inv" : "y"), p->stream, [&] {
           return p->tc ? launch_strided_tc(p->tc, L, a, p->wait_err, p->stream) : go_strided(L, 0, a, p->stream);
@@ -936,7 +935,7 @@ struct Exec {
     a.in_line = a.out_line = M;
     a.inverse = inverse;
     a.variant = p->recording ? 0 : p->var_y;
-    if (a.variant == 2 || a.variant == 3) a.tw = p->tw_y_alt;
+    if (a.variant == 2) a.tw = p->tw_y_alt;
     if (!timed(inverse ? "y_inv" : "y", st, [&] { return go_strided(p->n[1], 0, a, st); }))
       unsupported("strided pass", p->n[1]);
   }
@@ -1260,8 +1259,7 @@ void tune_variants(accfft_c_plan* p) {
   const int kinds[4] = {PK_STRIDED, PK_STRIDED, PK_ZR2C, PK_ZC2R};
   const int lens[4] = {p->n[1], p->n[0], p->M(), p->M()};
   bool any = false;   // nothing to choose when no pass length has a variant
-  for (int w = 0; w < 4; ++w)
-    for (int v = 1; v <= kMaxVariant; ++v) any = any || variant_exists(kinds[w], lens[w], v);
+  for (int w = 0; w < 4; ++w) any = any || variant_exists(kinds[w], lens[w], 1) || variant_exists(kinds[w], lens[w], 2);
   if (!any) return;
   const auto key = std::make_tuple(p->n[0], p->n[1], p->n[2], p->packed ? 1 : 0);
   {
@@ -1314,7 +1312,7 @@ void tune_variants(accfft_c_plan* p) {
   for (int w = 0; w < 4 && ok; ++w) {
     float best = -1.0f;
     int best_v = 0;
-    for (int v = 0; v <= kMaxVariant; ++v) {
+    for (int v = 0; v < 3; ++v) {
       if (v > 0 && !variant_exists(kinds[w], lens[w], v)) continue;
       *slot[w] = v;
       const float t = ms_of(w);
@@ -1720,8 +1718,7 @@ int accfft_c_set_variants(accfft_c_plan* p, const int variant[4]) {
   const int kinds[4] = {PK_STRIDED, PK_STRIDED, PK_ZR2C, PK_ZC2R};
   const int lens[4] = {p->n[1], p->n[0], p->M(), p->M()};
   for (int w = 0; w < 4; ++w)
-    if (variant[w] < 0 || variant[w] > kMaxVariant ||
-        (variant[w] > 0 && !variant_exists(kinds[w], lens[w], variant[w])))
+    if (variant[w] < 0 || variant[w] > 2 || (variant[w] > 0 && !variant_exists(kinds[w], lens[w], variant[w])))
       return fail(ACCFFT_C_EUNSUPPORTED, "set_variants: pass %d of length %d has no variant %d", w, lens[w], variant[w]);
   p->var_y = variant[0];
   p->var_x = variant[1];

@@ -4,8 +4,6 @@
 //   strided pass (MODE 0), L in {64, 128, 256, 512, 1024}:
 //     1  half the columns per tile (TC / 2, at least 8)
 //     2  the next smaller first radix (E = 16 for a default of 32, 8 for 16)
-//     3  L = 1024: both (radix 16 first, 8 columns: 512 threads at 64
-//        registers, two CTAs per SM)
 //   z r2c / z c2r (plain and mirror-pair mode), M in {64, 128, 256, 512}:
 //     1  the other line count per CTA (z r2c: TL / 2; z c2r: TL where its
 //        default is TL / 2, else TL / 2)
@@ -63,8 +61,6 @@ bool strided_variant(int v, const StridedArgs& a, cudaStream_t s) {
     if constexpr (half_tc<L>() > 0) return run_strided_v<L, 0, half_tc<L>()>(a, s);
   } else if (v == 2) {
     if constexpr (alt_e<L>() > 0) return run_strided_v<L, alt_e<L>(), 0>(a, s);
-  } else if (v == 3) {
-    if constexpr (L == 1024) return run_strided_v<L, 16, 8>(a, s);
   }
   return false;
 }
@@ -118,11 +114,6 @@ void strided_shape(int v, int* E, int* tile) {
     if constexpr (alt_e<L>() > 0) {
       *E = alt_e<L>();
       *tile = StridedShape<float, L, alt_e<L>()>::TC;
-    }
-  } else if (v == 3) {
-    if constexpr (L == 1024) {
-      *E = 16;
-      *tile = 8;
     }
   }
 }
