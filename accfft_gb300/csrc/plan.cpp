@@ -1972,6 +1972,14 @@ struct accfft_c_batch {
   size_t dev_bytes = 0;
   bool final = false;
   int tasks = 0;
+  // the groups of one level are independent: they run on up to kBranches
+  // streams forked from the caller's stream at the level's start and joined
+  // at its end (created by finalize)
+  static constexpr int kBranches = 4;
+  cudaStream_t branch[kBranches] = {};
+  cudaEvent_t fork = nullptr;
+  cudaEvent_t join[kBranches] = {};
+  std::vector<int> branch_of;        // branch of each launch
 };
 
 extern "C" {
@@ -1984,10 +1992,13 @@ accfft_c_batch* accfft_c_batch_create(void) {
 
 void accfft_c_batch_destroy(accfft_c_batch* b) {
   if (!b) return;
-  if (b->dev) {
-    DeviceGuard guard(b->device);
-    cudaFree(b->dev);
+  DeviceGuard guard(b->device);
+  if (b->dev) cudaFree(b->dev);
+  for (int j = 0; j < accfft_c_batch::kBranches; ++j) {
+    if (b->branch[j]) cudaStreamDestroy(b->branch[j]);
+    if (b->join[j]) cudaEventDestroy(b->join[j]);
   }
+  if (b->fork) cudaEventDestroy(b->fork);
   delete b;
 }
 
@@ -2070,7 +2081,29 @@ int accfft_c_batch_finalize(accfft_c_batch* b) {
     }
     b->level_end.push_back((int)b->launches.size());
   }
+  // branches: within a level, the largest grid first onto the branch with the
+  // fewest CTAs so far
+  b->branch_of.assign(b->launches.size(), 0);
+  for (size_t lv = 0, first = 0; lv < b->level_end.size(); first = (size_t)b->level_end[lv++]) {
+    const size_t last = (size_t)b->level_end[lv];
+    std::vector<size_t> order;
+    for (size_t i = first; i < last; ++i) order.push_back(i);
+    std::sort(order.begin(), order.end(), [&](size_t x, size_t y) { return b->launches[x].grid > b->launches[y].grid; });
+    long long load[accfft_c_batch::kBranches] = {};
+    for (size_t i : order) {
+      int j = (int)(std::min_element(load, load + accfft_c_batch::kBranches) - load);
+      b->branch_of[i] = j;
+      load[j] += b->launches[i].grid;
+    }
+  }
   DeviceGuard guard(b->device);
+  for (int j = 0; j < accfft_c_batch::kBranches; ++j) {
+    cudaError_t e = cudaStreamCreateWithFlags(&b->branch[j], cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->join[j], cudaEventDisableTiming);
+    if (e != cudaSuccess) return cuda_fail(e, "batch_finalize: branch streams");
+  }
+  if (cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) != cudaSuccess)
+    return cuda_fail(cudaGetLastError(), "batch_finalize: fork event");
   if (!host.empty()) {
     cudaError_t e = cudaMalloc(&b->dev, host.size());
     if (e == cudaSuccess) e = cudaMemcpy(b->dev, host.data(), host.size(), cudaMemcpyHostToDevice);
@@ -2089,10 +2122,31 @@ int accfft_c_batch_run(accfft_c_batch* b, void* stream) {
   DeviceGuard guard(b->device);
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   auto* base = static_cast<unsigned char*>(b->dev);
-  for (const auto& ln : b->launches) {
-    if (!launch_grouped(ln.kind, ln.L, ln.mode, base + ln.tab_off,
-                        reinterpret_cast<const long long*>(base + ln.starts_off), ln.ntasks, ln.grid, st))
-      return fail(ACCFFT_C_ECUDA, "batch_run: grouped launch of length %d failed", ln.L);
+  auto go = [&](const accfft_c_batch::Launch& ln, cudaStream_t s) {
+    return launch_grouped(ln.kind, ln.L, ln.mode, base + ln.tab_off,
+                          reinterpret_cast<const long long*>(base + ln.starts_off), ln.ntasks, ln.grid, s);
+  };
+  for (size_t lv = 0, first = 0; lv < b->level_end.size(); first = (size_t)b->level_end[lv++]) {
+    const size_t last = (size_t)b->level_end[lv];
+    if (last - first == 1) {   // one group: on the caller's stream
+      if (!go(b->launches[first], st)) return fail(ACCFFT_C_ECUDA, "batch_run: grouped launch of length %d failed", b->launches[first].L);
+      continue;
+    }
+    // fork: every branch this level uses waits for the caller's stream, runs
+    // its groups, and the caller's stream waits for all of them
+    bool used[accfft_c_batch::kBranches] = {};
+    for (size_t i = first; i < last; ++i) used[b->branch_of[i]] = true;
+    cudaEventRecord(b->fork, st);
+    for (int j = 0; j < accfft_c_batch::kBranches; ++j)
+      if (used[j]) cudaStreamWaitEvent(b->branch[j], b->fork, 0);
+    for (size_t i = first; i < last; ++i)
+      if (!go(b->launches[i], b->branch[b->branch_of[i]]))
+        return fail(ACCFFT_C_ECUDA, "batch_run: grouped launch of length %d failed", b->launches[i].L);
+    for (int j = 0; j < accfft_c_batch::kBranches; ++j) {
+      if (!used[j]) continue;
+      cudaEventRecord(b->join[j], b->branch[j]);
+      cudaStreamWaitEvent(st, b->join[j], 0);
+    }
   }
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? ACCFFT_C_OK : cuda_fail(e, "batch_run");
