@@ -1972,14 +1972,18 @@ struct accfft_c_batch {
   size_t dev_bytes = 0;
   bool final = false;
   int tasks = 0;
-  // the groups of one level are independent: they run on up to kBranches
-  // streams forked from the caller's stream at the level's start and joined
-  // at its end (created by finalize)
-  static constexpr int kBranches = 4;
+  // Launch i waits only for the launches of the level before it that hold
+  // one of its instances (deps[i]), so no level waits for the whole of the
+  // level before: an instance's next pass starts once its own pass is done.
+  // The launches run on kBranches streams forked from the caller's stream
+  // and joined at the end (created by finalize; one event per launch).
+  static constexpr int kBranches = 8;
   cudaStream_t branch[kBranches] = {};
   cudaEvent_t fork = nullptr;
   cudaEvent_t join[kBranches] = {};
-  std::vector<int> branch_of;        // branch of each launch
+  std::vector<int> branch_of;             // branch of each launch
+  std::vector<std::vector<int>> deps;     // launches each launch waits for
+  std::vector<cudaEvent_t> done;          // recorded after each launch
 };
 
 extern "C" {
@@ -1999,6 +2003,8 @@ void accfft_c_batch_destroy(accfft_c_batch* b) {
     if (b->join[j]) cudaEventDestroy(b->join[j]);
   }
   if (b->fork) cudaEventDestroy(b->fork);
+  for (cudaEvent_t e : b->done)
+    if (e) cudaEventDestroy(e);
   delete b;
 }
 
@@ -2034,23 +2040,38 @@ int accfft_c_batch_finalize(accfft_c_batch* b) {
   size_t levels = 0;
   for (auto& v : b->instances) levels = std::max(levels, v.size());
   std::vector<unsigned char> host;
+  std::vector<int> prev_launch(b->instances.size(), -1);   // each instance's launch at the level before
   auto align = [&](size_t a) { host.resize((host.size() + a - 1) / a * a); };
   b->tasks = 0;
   for (size_t lv = 0; lv < levels; ++lv) {
     // the level's tasks, grouped by (kind, length, mode) in first-seen order
     std::vector<std::pair<std::tuple<int, int, int>, std::vector<const PassRecord*>>> groups;
+    std::vector<std::vector<int>> members;   // instance indices of each group
+    int inst = 0;
     for (auto& v : b->instances) {
+      const int me = inst++;
       if (lv >= v.size()) continue;
       const PassRecord& r = v[lv];
       auto key = std::make_tuple(r.kind, r.L, r.mode);
       auto it = std::find_if(groups.begin(), groups.end(), [&](auto& g) { return g.first == key; });
       if (it == groups.end()) {
         groups.push_back({key, {}});
+        members.push_back({});
         it = groups.end() - 1;
       }
       it->second.push_back(&r);
+      members[it - groups.begin()].push_back(me);
     }
-    for (auto& g : groups) {
+    std::vector<int> this_launch(b->instances.size(), -1);
+    for (size_t gi = 0; gi < groups.size(); ++gi) {
+      auto& g = groups[gi];
+      std::vector<int> dep;
+      for (int m : members[gi]) {
+        if (prev_launch[m] >= 0 && std::find(dep.begin(), dep.end(), prev_launch[m]) == dep.end())
+          dep.push_back(prev_launch[m]);
+        this_launch[m] = (int)b->launches.size();
+      }
+      b->deps.push_back(dep);
       accfft_c_batch::Launch ln{};
       std::tie(ln.kind, ln.L, ln.mode) = g.first;
       ln.ntasks = (int)g.second.size();
@@ -2079,6 +2100,8 @@ int accfft_c_batch_finalize(accfft_c_batch* b) {
       b->launches.push_back(ln);
       b->tasks += ln.ntasks;
     }
+    for (size_t m = 0; m < this_launch.size(); ++m)
+      if (this_launch[m] >= 0) prev_launch[m] = this_launch[m];
     b->level_end.push_back((int)b->launches.size());
   }
   // branches: within a level, the largest grid first onto the branch with the
@@ -2104,6 +2127,10 @@ int accfft_c_batch_finalize(accfft_c_batch* b) {
   }
   if (cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) != cudaSuccess)
     return cuda_fail(cudaGetLastError(), "batch_finalize: fork event");
+  b->done.assign(b->launches.size(), nullptr);
+  for (auto& e : b->done)
+    if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess)
+      return cuda_fail(cudaGetLastError(), "batch_finalize: launch events");
   if (!host.empty()) {
     cudaError_t e = cudaMalloc(&b->dev, host.size());
     if (e == cudaSuccess) e = cudaMemcpy(b->dev, host.data(), host.size(), cudaMemcpyHostToDevice);
@@ -2126,27 +2153,26 @@ int accfft_c_batch_run(accfft_c_batch* b, void* stream) {
     return launch_grouped(ln.kind, ln.L, ln.mode, base + ln.tab_off,
                           reinterpret_cast<const long long*>(base + ln.starts_off), ln.ntasks, ln.grid, s);
   };
-  for (size_t lv = 0, first = 0; lv < b->level_end.size(); first = (size_t)b->level_end[lv++]) {
-    const size_t last = (size_t)b->level_end[lv];
-    if (last - first == 1) {   // one group: on the caller's stream
-      if (!go(b->launches[first], st)) return fail(ACCFFT_C_ECUDA, "batch_run: grouped launch of length %d failed", b->launches[first].L);
-      continue;
+  // fork every branch from the caller's stream; each launch waits for the
+  // launches holding its instances' previous passes; join at the end
+  cudaEventRecord(b->fork, st);
+  for (int j = 0; j < accfft_c_batch::kBranches; ++j) cudaStreamWaitEvent(b->branch[j], b->fork, 0);
+  for (size_t i = 0; i < b->launches.size(); ++i) {
+    cudaStream_t s = b->branch[b->branch_of[i]];
+    for (int d : b->deps[i])
+      if (b->branch_of[(size_t)d] != b->branch_of[i]) cudaStreamWaitEvent(s, b->done[(size_t)d], 0);
+    if (!go(b->launches[i], s)) {
+      for (int j = 0; j < accfft_c_batch::kBranches; ++j) {
+        cudaEventRecord(b->join[j], b->branch[j]);
+        cudaStreamWaitEvent(st, b->join[j], 0);
+      }
+      return fail(ACCFFT_C_ECUDA, "batch_run: grouped launch of length %d failed", b->launches[i].L);
     }
-    // fork: every branch this level uses waits for the caller's stream, runs
-    // its groups, and the caller's stream waits for all of them
-    bool used[accfft_c_batch::kBranches] = {};
-    for (size_t i = first; i < last; ++i) used[b->branch_of[i]] = true;
-    cudaEventRecord(b->fork, st);
-    for (int j = 0; j < accfft_c_batch::kBranches; ++j)
-      if (used[j]) cudaStreamWaitEvent(b->branch[j], b->fork, 0);
-    for (size_t i = first; i < last; ++i)
-      if (!go(b->launches[i], b->branch[b->branch_of[i]]))
-        return fail(ACCFFT_C_ECUDA, "batch_run: grouped launch of length %d failed", b->launches[i].L);
-    for (int j = 0; j < accfft_c_batch::kBranches; ++j) {
-      if (!used[j]) continue;
-      cudaEventRecord(b->join[j], b->branch[j]);
-      cudaStreamWaitEvent(st, b->join[j], 0);
-    }
+    cudaEventRecord(b->done[i], s);
+  }
+  for (int j = 0; j < accfft_c_batch::kBranches; ++j) {
+    cudaEventRecord(b->join[j], b->branch[j]);
+    cudaStreamWaitEvent(st, b->join[j], 0);
   }
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? ACCFFT_C_OK : cuda_fail(e, "batch_run");

@@ -282,10 +282,10 @@ int accfft_c_divergence_adjoint(accfft_c_plan* plan, void* a_x, void* a_y, void*
  * poisson, grad_slow; other calls return ACCFFT_C_EUNSUPPORTED).
  * accfft_c_batch_finalize groups level k (the k-th pass of every instance)
  * by pass kind and line length and uploads one descriptor table per group;
- * accfft_c_batch_run launches one persistent kernel per group, level after
- * level, on `stream`: the groups of a level are independent and run on up
- * to four streams of the batch forked from `stream` at the level's start
- * and joined before the next level (capturable into a CUDA graph).  Line
+ * accfft_c_batch_run launches one persistent kernel per group on eight
+ * streams of the batch forked from `stream` and joined before it returns;
+ * each group waits only for the groups of the level before that hold its
+ * instances' previous passes (capturable into a CUDA graph).  Line
  * lengths up to 256.  One instance per plan (the plan's scratch belongs to
  * it); the arrays given to the recorded calls must stay valid and distinct
  * between instances; a batch runs one call at a time. */
