@@ -100,6 +100,7 @@ bool launch_add_rows(bool dbl, void* out, long long out_row, const void* in, lon
 bool launch_strided_variant_f32(int L, int v, const StridedArgs& a, cudaStream_t s);
 bool launch_contig_variant_f32(bool r2c, int M, int v, const ContigArgs& a, cudaStream_t s);
 void variant_shape(int kind, int L, int v, int* E, int* tile);
+constexpr int kMaxVariant = 3;
 
 // pass kinds of a recorded batch task (plan.cpp) and their grouped launch
 enum PassKind { PK_STRIDED = 0, PK_ZR2C = 2, PK_ZC2R = 3 };

@@ -1259,7 +1259,8 @@ void tune_variants(accfft_c_plan* p) {
   const int kinds[4] = {PK_STRIDED, PK_STRIDED, PK_ZR2C, PK_ZC2R};
   const int lens[4] = {p->n[1], p->n[0], p->M(), p->M()};
   bool any = false;   // nothing to choose when no pass length has a variant
-  for (int w = 0; w < 4; ++w) any = any || variant_exists(kinds[w], lens[w], 1) || variant_exists(kinds[w], lens[w], 2);
+  for (int w = 0; w < 4; ++w)
+    for (int v = 1; v <= kMaxVariant; ++v) any = any || variant_exists(kinds[w], lens[w], v);
   if (!any) return;
   const auto key = std::make_tuple(p->n[0], p->n[1], p->n[2], p->packed ? 1 : 0);
   {
@@ -1312,7 +1313,7 @@ void tune_variants(accfft_c_plan* p) {
   for (int w = 0; w < 4 && ok; ++w) {
     float best = -1.0f;
     int best_v = 0;
-    for (int v = 0; v < 3; ++v) {
+    for (int v = 0; v <= kMaxVariant; ++v) {
       if (v > 0 && !variant_exists(kinds[w], lens[w], v)) continue;
       *slot[w] = v;
       const float t = ms_of(w);
@@ -1718,7 +1719,8 @@ int accfft_c_set_variants(accfft_c_plan* p, const int variant[4]) {
   const int kinds[4] = {PK_STRIDED, PK_STRIDED, PK_ZR2C, PK_ZC2R};
   const int lens[4] = {p->n[1], p->n[0], p->M(), p->M()};
   for (int w = 0; w < 4; ++w)
-    if (variant[w] < 0 || variant[w] > 2 || (variant[w] > 0 && !variant_exists(kinds[w], lens[w], variant[w])))
+    if (variant[w] < 0 || variant[w] > kMaxVariant ||
+        (variant[w] > 0 && !variant_exists(kinds[w], lens[w], variant[w])))
       return fail(ACCFFT_C_EUNSUPPORTED, "set_variants: pass %d of length %d has no variant %d", w, lens[w], variant[w]);
   p->var_y = variant[0];
   p->var_x = variant[1];

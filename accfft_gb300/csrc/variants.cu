@@ -4,11 +4,17 @@
 //   strided pass (MODE 0), L in {64, 128, 256, 512, 1024}:
 //     1  half the columns per tile (TC / 2, at least 8)
 //     2  the next smaller first radix (E = 16 for a default of 32, 8 for 16)
+//     3  the default shape with 16-byte loads and stores: each pair of
+//        neighbouring columns' threads loads two rows as float4 and swaps
+//        halves by warp shuffle (launches with partial or misaligned tiles
+//        run the default kernel)
 //   z r2c / z c2r (plain and mirror-pair mode), M in {64, 128, 256, 512}:
 //     1  the other line count per CTA (z r2c: TL / 2; z c2r: TL where its
 //        default is TL / 2, else TL / 2)
 //     2  the next smaller first radix (with that radix's default line count)
 // A variant that does not exist for a length launches nothing (false).
+#include <cstdint>
+
 #include "launch.h"
 #include "passes.cuh"
 #include "per_device.h"
@@ -55,12 +61,86 @@ bool run_strided_v(const StridedArgs& a, cudaStream_t s) {
   return launch_pass(k, unsigned((a.ncols + SH::TC - 1) / SH::TC), SH::threads, SH::smem, s, b) == cudaSuccess;
 }
 
+// The default strided tile (MODE 0) with 16-byte global accesses.  Threads c
+// and c+1 (c even) of one line position t own neighbouring columns; for each
+// pair of stage-0 entries (i, i+1) the even thread loads row t+i*P and the
+// odd thread row t+(i+1)*P, both as (column c, column c+1), and one shuffle
+// swaps the halves each needs.  The outputs leave the same way in reverse.
+template <int L>
+__global__ void __launch_bounds__(StridedShape<float, L>::threads, (strided_min_blocks<float, L, 0, 0>()))
+k_strided_vec(const StridedArgs a) {
+  typedef LineFFT<float, L> LN;
+  typedef float2 V;
+  constexpr int TC = StridedShape<float, L>::TC, P = LN::P, E = LN::E;
+  static_assert(E % 2 == 0 && TC % 2 == 0 && LN::NS >= 2, "pairs of entries, columns and stages");
+  PassScope scope(a.early_trigger);
+  extern __shared__ __align__(16) unsigned char smraw[];
+  V* sm = reinterpret_cast<V*>(smraw);
+  const int c = threadIdx.x % TC;
+  const int t = threadIdx.x / TC;
+  const bool odd = (c & 1) != 0;
+  const long long g0 = (long long)blockIdx.x * TC;   // whole tiles inside one slab (launcher)
+  const long long slab = g0 / a.cps;
+  const long long cc0 = g0 - slab * a.cps + (c & ~1);
+  const V* in = static_cast<const V*>(a.in) + slab * a.in_slab + cc0;
+  V* out = static_cast<V*>(a.out) + slab * a.out_slab + cc0;
+  const long long il = a.in_line, ol = a.out_line;
+  const float sg = a.inverse ? -1.f : 1.f;
+  auto swap = [&](V x) { return make_float2(__shfl_xor_sync(0xffffffffu, x.x, 1), __shfl_xor_sync(0xffffffffu, x.y, 1)); };
+  V v[E];
+#pragma unroll
+  for (int i = 0; i < E; i += 2) {
+    const float4 q = *reinterpret_cast<const float4*>(in + (long long)(t + (odd ? i + 1 : i) * P) * il);
+    const V lo = make_float2(q.x, q.y), hi = make_float2(q.z, q.w);
+    const V got = swap(odd ? lo : hi);
+    V x0 = odd ? got : lo;   // row t+i*P, this thread's column
+    V x1 = odd ? hi : got;   // row t+(i+1)*P
+    x0.y *= sg;
+    x1.y *= sg;
+    v[i] = x0;
+    v[i + 1] = x1;
+  }
+  LN::stages(t, static_cast<const V*>(a.tw), [&](int p, V x) { sm[p * TC + c] = x; },
+             [&](int p) { return sm[p * TC + c]; }, [] {}, v);
+  // outputs: entry i = b*R + r of the last stage is frequency t + b*P + r*Ns
+  constexpr int R = LN::pl.radix[LN::NS - 1];
+  constexpr int Ns = plan_ns_before(LN::pl, LN::NS - 1);
+#pragma unroll
+  for (int i = 0; i < E; i += 2) {
+    const int p0 = t + (i / R) * P + (i % R) * Ns;
+    const int p1 = t + ((i + 1) / R) * P + ((i + 1) % R) * Ns;
+    V y0 = v[i], y1 = v[i + 1];
+    y0.y *= sg;
+    y1.y *= sg;
+    const V got = swap(odd ? y0 : y1);
+    const float4 q = odd ? make_float4(got.x, got.y, y1.x, y1.y) : make_float4(y0.x, y0.y, got.x, got.y);
+    *reinterpret_cast<float4*>(out + (long long)(odd ? p1 : p0) * ol) = q;
+  }
+}
+
+template <int L>
+bool run_strided_vec(const StridedArgs& a, cudaStream_t s) {
+  typedef StridedShape<float, L> SH;
+  constexpr int TC = SH::TC;
+  const bool aligned = reinterpret_cast<uintptr_t>(a.in) % 16 == 0 && reinterpret_cast<uintptr_t>(a.out) % 16 == 0 &&
+                       a.in_line % 2 == 0 && a.out_line % 2 == 0 && a.in_slab % 2 == 0 && a.out_slab % 2 == 0;
+  if (!aligned || a.ncols_main > 0 || a.ncols <= 0 || a.cps % TC != 0 || a.ncols % TC != 0) return false;
+  auto k = k_strided_vec<L>;
+  static PerDevice prepared;
+  if (!prepare_smem(prepared, k, SH::smem)) return false;
+  StridedArgs b = a;
+  b.early_trigger = pdl_mode() == 2;
+  return launch_pass(k, unsigned(a.ncols / TC), SH::threads, SH::smem, s, b) == cudaSuccess;
+}
+
 template <int L>
 bool strided_variant(int v, const StridedArgs& a, cudaStream_t s) {
   if (v == 1) {
     if constexpr (half_tc<L>() > 0) return run_strided_v<L, 0, half_tc<L>()>(a, s);
   } else if (v == 2) {
     if constexpr (alt_e<L>() > 0) return run_strided_v<L, alt_e<L>(), 0>(a, s);
+  } else if (v == 3) {
+    return run_strided_vec<L>(a, s);
   }
   return false;
 }
@@ -115,6 +195,9 @@ void strided_shape(int v, int* E, int* tile) {
       *E = alt_e<L>();
       *tile = StridedShape<float, L, alt_e<L>()>::TC;
     }
+  } else if (v == 3) {
+    *E = LineFFT<float, L>::E;
+    *tile = StridedShape<float, L>::TC;
   }
 }
 template <bool R2C, int M>

@@ -160,7 +160,8 @@ int accfft_c_set_pass_order(accfft_c_plan* plan, int order);
  * src/accfft_gpu.cpp:341-382) on a float r2c plan times the radix / tile
  * variants of its y, x, z r2c and z c2r passes on the plan's scratch and a
  * temporary spectrum (variant 0 = default; 1 = half the columns or the other
- * line count per CTA; 2 = the next smaller first radix) and keeps the
+ * line count per CTA; 2 = the next smaller first radix; 3 = for y and x,
+ * the default tile with 16-byte loads and stores) and keeps the
  * fastest; the choice is cached per process by grid and pass order, so plans
  * of one grid run the same kernels.  ACCFFT_ESTIMATE keeps the defaults.
  * accfft_c_plan_tuning reports, for y, x, z r2c and z c2r, the variant, its
