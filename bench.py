@@ -649,6 +649,7 @@ def ours(args):
     e2e = None if args.no_e2e else e2e_pairs_per_s(args, ag, torch, n, dt, u, stream, world, args.inflight)
     variants = None if args.no_variants or dt != "float32" else precision_variants(ag, torch, n, u, stream)
     prec1024 = precision_1024(ag, torch) if variants is not None and n == (512, 512, 512) else None
+    adjoint = adjoint_timing(ag, torch) if variants is not None and n == (512, 512, 512) else None
 
     if rank != 0:
         return
@@ -681,6 +682,7 @@ def ours(args):
         "tuning": plan.tuning(),
         "variants": variants,
         "precision_1024": prec1024,
+        "adjoint": adjoint,
     }
     if not args.no_baseline and world == 1:
         v, sample, th = cpu_pairs_per_s(n)
@@ -758,6 +760,54 @@ def precision_workload(args):
             "speedup_fp32_over_fp64": res["fp64_drop_in"]["ms_per_pair"] / res["fp32_cuda_core"]["ms_per_pair"],
             "data": "synthetic turbulence-like spectrum, seeded"}
     print(json.dumps(line), flush=True)
+
+
+def adjoint_timing(ag, torch, n=(256, 256, 256)):
+    """ms of one float32 forward + backward of L(u) = 0.5|grad u|^2 +
+    <f, inv_laplace u> through the adjoint kernels, eager and replayed as one
+    CUDA graph (the 'adjoint ms' of the headline metric)."""
+    import accfft_gb300.autograd as ad
+
+    g = torch.Generator(device="cuda").manual_seed(11)
+    u = torch.randn(n, device="cuda", generator=g)
+    f = torch.randn(n, device="cuda", generator=g)
+    plan = ag.PlanR2C(n, "float32")
+
+    def step(x):
+        gx, gy, gz = ad.grad(x, plan)
+        loss = 0.5 * ((gx * gx).sum() + (gy * gy).sum() + (gz * gz).sum()) + (f * ad.inv_laplace(x, plan)).sum()
+        return torch.autograd.grad(loss, x)[0]
+
+    x = u.clone().requires_grad_(True)
+    for _ in range(3):
+        step(x)
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(10):
+        step(x)
+    b.record()
+    torch.cuda.synchronize()
+    eager = a.elapsed_time(b) / 10
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(side):
+        for _ in range(3):
+            step(x)
+    torch.cuda.current_stream().wait_stream(side)
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph, capture_error_mode="relaxed"):
+        step(x)
+    graph.replay()
+    torch.cuda.synchronize()
+    a.record()
+    for _ in range(10):
+        graph.replay()
+    b.record()
+    torch.cuda.synchronize()
+    plan.destroy()
+    return {"grid": list(n), "dtype": "float32", "eager_ms": eager, "graph_replay_ms": a.elapsed_time(b) / 10,
+            "loss": "0.5|grad u|^2 + <f, inv_laplace u>, forward + backward"}
 
 
 def adjoint_workload(args):
