@@ -67,6 +67,9 @@ def parse():
                     help="non-cubic grid N0 N1 N2 (smaller cases of the same kernels for profiling)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--inflight", type=int, default=3, help="e2e: pairs in flight (plans on their own streams)")
+    ap.add_argument("--host-pages", default="pinned", choices=["pinned", "huge"],
+                    help="e2e host buffers: pinned = torch pin_memory (cudaHostAlloc); huge = anonymous memory "
+                         "advised to transparent huge pages, then registered (cudaHostRegister)")
     ap.add_argument("--e2e-order", default="free", choices=["free", "ordered"],
                     help="e2e: ordered makes each step's r2c (c2r) wait for the previous step's r2c (c2r)")
     ap.add_argument("--dtype", default="float32", choices=["float32", "float64"])
@@ -432,6 +435,32 @@ def link_probe(torch, hu, hb, reps=4):
     return {"h2d_GBps": rates[0], "d2h_GBps": rates[1], "both_directions": True, "floor_ms_per_pair": floor_ms}
 
 
+_HOST_KEEP = []   # mappings behind registered host buffers
+
+
+def host_buffer(torch, shape, tdt, pages):
+    """A page-locked host array for the e2e step: torch's pinned allocation,
+    or anonymous memory advised to transparent huge pages, touched, and
+    registered with the CUDA driver."""
+    if pages == "pinned":
+        return torch.empty(shape, dtype=tdt).pin_memory()
+    import mmap
+
+    esz = torch.empty((), dtype=tdt).element_size()
+    nbytes = int(np.prod(shape)) * esz
+    mm = mmap.mmap(-1, nbytes, flags=mmap.MAP_PRIVATE | mmap.MAP_ANONYMOUS)
+    if hasattr(mmap, "MADV_HUGEPAGE"):
+        mm.madvise(mmap.MADV_HUGEPAGE)
+    arr = np.frombuffer(mm, dtype=np.uint8)
+    arr[::4096] = 0   # fault every page in before registering
+    t = torch.from_numpy(arr).view(tdt).view(shape)
+    rc = torch.cuda.cudart().cudaHostRegister(t.data_ptr(), nbytes, 0)
+    if int(rc) != 0:
+        raise RuntimeError(f"cudaHostRegister failed ({int(rc)})")
+    _HOST_KEEP.append((mm, arr, t))
+    return t
+
+
 def buffer_rates(torch, hu, outs, reps=2):
     """Single-direction copy rates (GB/s) of the e2e step's own pinned buffers:
     host-to-device from the input field, device-to-host into each output
@@ -471,7 +500,7 @@ def e2e_pairs_per_s(args, ag, torch, n, dt, u, stream, world, inflight=3, ordere
     ordered = args.e2e_order == "ordered" if ordered is None else ordered
     tdt = getattr(torch, dt)
     H2 = n[2] // 2 + 1
-    hu = torch.empty(n, dtype=tdt).pin_memory()
+    hu = host_buffer(torch, n, tdt, args.host_pages)
     hu.copy_(u.cpu())
     lanes = []
     for _ in range(inflight):
@@ -479,7 +508,7 @@ def e2e_pairs_per_s(args, ag, torch, n, dt, u, stream, world, inflight=3, ordere
         plan = ag.PlanR2C(n, dt, flags=ag.ACCFFT_MEASURE)
         plan.set_stream(s, blocking=False)
         lanes.append((s, plan, torch.empty((n[0], n[1], H2, 2), dtype=tdt, device="cuda"),
-                      torch.empty(n, dtype=tdt).pin_memory()))
+                      host_buffer(torch, n, tdt, args.host_pages)))
 
     def run(ksteps, marks=None):
         start = torch.cuda.Event()
@@ -564,6 +593,7 @@ def e2e_pairs_per_s(args, ag, torch, n, dt, u, stream, world, inflight=3, ordere
             "host_enqueue_ms_per_step": enqueue_ms, "step_spacing": step_spacing,
             "regions": {"steps_each": ksteps, "ms_per_step": [t[0] for t in trials],
                         "pairs_per_s": [world * 1000.0 / t[0] for t in trials], "value": "median"},
+            "host_pages": args.host_pages,
             "path": f"pinned host field copied in 4 slab batches each way through a device staging ring; "
                     f"{inflight} pairs in flight on {inflight} streams"
                     + ("; r2c calls and c2r calls each in step order across the streams" if ordered else "")}
