@@ -101,6 +101,9 @@ bool launch_strided_variant_f32(int L, int v, const StridedArgs& a, cudaStream_t
 bool launch_contig_variant_f32(bool r2c, int M, int v, const ContigArgs& a, cudaStream_t s);
 void variant_shape(int kind, int L, int v, int* E, int* tile);
 constexpr int kMaxVariant = 3;
+// spec[n0][cols] (double complex) *= the symbol of s at (x, column), for the
+// operators of double-float plans (df_sym.cu)
+bool launch_sym_spectrum_f64(void* spec, long long n0, long long cols, const SymArgs& s, cudaStream_t st);
 
 // pass kinds of a recorded batch task (plan.cpp) and their grouped launch
 enum PassKind { PK_STRIDED = 0, PK_ZR2C = 2, PK_ZC2R = 3 };

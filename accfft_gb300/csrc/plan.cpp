@@ -627,6 +627,14 @@ struct Exec {
       unsupported("symbol pass", L);
   }
   // y pass over an [N0][N1][h] complex array, x pass over [N0][N1*h]
+  // the symbol multiply of a double-float plan's operator over the natural
+  // spectrum in the plan scratch
+  void sym_spectrum(void* spec, const SymArgs& s) {
+    if (!ok()) return;
+    const long long cols = (long long)p->n[1] * p->H2();
+    if (!timed("sym", p->stream, [&] { return launch_sym_spectrum_f64(spec, p->n[0], cols, s, p->stream); }))
+      rc = fail(ACCFFT_C_ECUDA, "operator: symbol pass launch failed");
+  }
   void ypass(const void* in, void* out, long long h, int inverse) {
     strided(in, out, p->tw_y, p->n[1], (long long)p->n[0] * h, h, (long long)p->n[1] * h, h, inverse);
   }
@@ -1354,9 +1362,16 @@ int check_plan(accfft_c_plan* p, int kind, int dbl, const char* fn) {
     return fail(ACCFFT_C_EINVAL, "%s: precision mismatch (plan is %s)", fn, p->dbl ? "double" : "float");
   if (p->tc && strcmp(fn, "execute_r2c") && strcmp(fn, "execute_c2r") && strcmp(fn, "execute"))
     return fail(ACCFFT_C_EUNSUPPORTED, "%s: tensor-core plans run full r2c / c2r transforms only", fn);
-  if (p->df && strcmp(fn, "execute_r2c") && strcmp(fn, "execute_c2r") && strcmp(fn, "execute") &&
-      strcmp(fn, "execute_c2c"))
-    return fail(ACCFFT_C_EUNSUPPORTED, "%s: double-float plans run r2c, c2r and c2c transforms only", fn);
+  if (p->df) {
+    static const char* const df_ok[] = {"execute_r2c", "execute_c2r", "execute", "execute_c2c", "laplace",
+                                        "biharmonic", "inv_laplace", "inv_biharmonic", "heat", "helmholtz",
+                                        "poisson"};
+    bool ok = false;
+    for (const char* f : df_ok) ok = ok || !strcmp(fn, f);
+    if (!ok)
+      return fail(ACCFFT_C_EUNSUPPORTED,
+                  "%s: double-float plans run r2c, c2r and c2c transforms and the 3-D spectral operators only", fn);
+  }
   return ACCFFT_C_OK;
 }
 
@@ -1508,6 +1523,25 @@ int op3d(accfft_c_plan* p, int sym_kind, void* outr, const void* inr, double* ti
   Exec ex(p, timer);
   SymArgs sym = make_sym(p, sym_kind, 1.0 / N);
   sym.param = param;
+  if (p->df) {
+    // double-float plans: the plan's r2c, the symbol multiply in double over
+    // the spectrum, the plan's c2r (each transform scans its own input for
+    // the exponent its passes scale by)
+    if (sym_kind == SYM_POISSON_FD)
+      return fail(ACCFFT_C_EUNSUPPORTED, "poisson: double-float plans take the spectral method (1) only");
+    void* s = p->scratch;
+    const long long spec_doubles = 2LL * p->n[0] * p->n[1] * h;
+    ex.df_scan(inr, (long long)p->n[0] * p->n[1], p->n[2], p->rrow());
+    ex.zr2c(inr, s, p->rrow());
+    ex.ypass(s, s, h, 0);
+    ex.xpass(s, s, h, 0);
+    ex.sym_spectrum(s, sym);
+    ex.df_scan(s, 1, spec_doubles, spec_doubles);
+    ex.xpass(s, s, h, 1);
+    ex.ypass(s, s, h, 1);
+    ex.zc2r(s, outr, p->rrow());
+    return ex.finish();
+  }
   if (p->split) {
     ex.zr2c_split(inr, p->rrow());
     ex.y_split(0);

@@ -168,3 +168,35 @@ def test_df_plans_reject_host_arrays(cuda, native):
         plan.r2c(hu, torch.empty((8, 8, 5, 2), dtype=torch.float64, device="cuda"))
     assert e.value.code == native.EUNSUPPORTED
     plan.destroy()
+
+
+OPS_DF = ("laplace", "biharmonic", "inv_laplace", "inv_biharmonic")
+
+
+@pytest.mark.parametrize("n", [(8, 8, 8), (5, 9, 4), (16, 12, 10), (48, 96, 64), (90, 100, 180), (128, 128, 128)])
+def test_df_operators_vs_oracle(cuda, native, oracle, n):
+    """The 3-D operators of double-float plans (the plan's r2c, the symbol in
+    double, the plan's c2r) against the oracle, and the spectral Poisson
+    solve, heat and Helmholtz against the plain double plan (itself pinned to
+    the oracle); odd and even axes."""
+    torch = cuda
+    u = rng(33).standard_normal(n)
+    du = to_dev(torch, u, "float64")
+    df = native.PlanR2C(n, "float64", flags=native.F64_DF)
+    dp = native.PlanR2C(n, "float64")
+    out = empty(torch, n, "float64")
+    for op in OPS_DF:
+        getattr(df, op)(out, du)
+        assert oracle.rel_l2(from_dev(out), oracle.spectral_op(u, op)) < 1e-12, op
+    ref = empty(torch, n, "float64")
+    for name, call in (("poisson", lambda p, o: p.poisson(o, du, method=1)),
+                       ("heat", lambda p, o: p.heat(o, du, 0.01)),
+                       ("helmholtz", lambda p, o: p.helmholtz(o, du, 2.5))):
+        call(df, out)
+        call(dp, ref)
+        assert ((out - ref).norm() / ref.norm()).item() < 1e-12, name
+    with pytest.raises(native.AccfftError) as e:
+        df.poisson(out, du, method=0)   # the finite-difference eigenvalues stay with plain double plans
+    assert e.value.code == native.EUNSUPPORTED
+    df.destroy()
+    dp.destroy()
