@@ -76,13 +76,16 @@ def test_df_partial_axes(cuda, native, oracle, xyz):
     plan.destroy()
 
 
-def test_df_plans_reject_operators_and_float(cuda, native):
+def test_df_plans_reject_derivatives_and_float(cuda, native):
+    """Double-float plans run the transforms and the 3-D spectral operators;
+    the derivative operators (grad, divergence, single-axis transforms) stay
+    with plain double plans."""
     torch = cuda
     n = (16, 16, 16)
     p = native.PlanR2C(n, "float64", flags=native.F64_DF)
     u = torch.zeros(n, dtype=torch.float64, device="cuda")
     with pytest.raises(native.AccfftError) as e:
-        p.laplace(torch.empty_like(u), u)
+        p.grad(torch.empty_like(u), torch.empty_like(u), torch.empty_like(u), u)
     assert e.value.code == native.EUNSUPPORTED
     p.destroy()
     with pytest.raises(native.AccfftError) as e:
