@@ -1030,7 +1030,10 @@ def operators_workload(args):
     exact["divergence"] = gx + gy + gz
     u = u64.to(tdt)
     del u64
-    plan = ag.PlanR2C(n, dt)
+    # --df with --dtype float64: a double-float plan (transforms and the 3-D
+    # operators; the derivative operators stay with plain double plans)
+    df = args.df and dt == "float64"
+    plan = ag.PlanR2C(n, dt, flags=ag.F64_DF) if df else ag.PlanR2C(n, dt)
     stream = torch.cuda.Stream()
     plan.set_stream(stream, blocking=False)
     outs = [torch.empty_like(u) for _ in range(3)]
@@ -1052,6 +1055,11 @@ def operators_workload(args):
         "divergence": (lambda: plan.divergence(back, u, u, u), 8 * esz * N,
                        3 * (2 * transform + 4 * esz * H) + 2 * 3 * esz * N),
     }
+    if df:
+        # r2c, the symbol pass over the half spectrum, c2r
+        for name in ("laplace", "biharmonic", "inv_laplace"):
+            calls[name] = (calls[name][0], ref_op, ref_op)
+        del calls["grad"], calls["divergence"]
     K = max(5, min(args.steps, 50))
     res = {}
     for name, (fn, nbytes, ref_bytes) in calls.items():
@@ -1085,7 +1093,7 @@ def operators_workload(args):
                                                                generator=torch.Generator(device="cuda").manual_seed(5))
                                         )).to(tdt)
     cs, cb = torch.empty_like(cu), torch.empty_like(cu)
-    pc = ag.PlanC2C(n, dt)
+    pc = ag.PlanC2C(n, dt, flags=ag.F64_DF) if df else ag.PlanC2C(n, dt)
     pc.set_stream(stream, blocking=False)
     with torch.cuda.stream(stream):
         for _ in range(3):
@@ -1109,7 +1117,8 @@ def operators_workload(args):
     label = "x".join(map(str, n))
     line = {"metric": f"{label} {dt} spectral operators ms per call", "workload": "operators",
             "value": res["laplace"]["ms"], "unit": "ms (laplace)", "higher_is_better": False,
-            "dtype": "f32" if dt == "float32" else "f64", "peak_GBps": peak, "peak_kind": peak_kind,
+            "dtype": "f32" if dt == "float32" else ("f64 (double-float arithmetic)" if df else "f64"),
+            "peak_GBps": peak, "peak_kind": peak_kind,
             "calls": res, "steps": K,
             "error_note": ("rel_l2_vs_exact of the symbol operators is the transform's rounding noise times "
                            "the symbol: |k|^2 (laplace, up to 2e5 at 512^3) and |k|^4 (biharmonic, up to 3.8e10) "
