@@ -60,12 +60,16 @@ extern "C" {
  * of floats (hi + lo, 48-bit significand) on the FP32 pipes, which on GB300
  * issue about 70x the operations per cycle of the FP64 pipe.  Arrays stay
  * IEEE double.  rel-L2 against an exact transform is about 1e-14 instead of
- * 1e-16; magnitudes must stay within float's exponent range (results below
- * 2^128, inputs above 2^-126 or flushed to zero).  Such plans run the r2c,
- * c2r and c2c transforms (any xyz); the single-axis transforms and the
- * operators stay with plain double plans.  Every transform of such a plan
- * rescales by the exponent its input scan leaves in one word of the plan,
- * so two transforms of one plan must not overlap on the GPU. */
+ * 1e-16; every transform first scans its input for the largest exponent and
+ * scales its passes by that power of two, so any finite input keeps
+ * normwise accuracy (entries below 2^-126 of the largest flush to zero).
+ * Such plans run the r2c, c2r and c2c transforms (any xyz) and the 3-D
+ * spectral operators (laplace, biharmonic, inv_laplace, inv_biharmonic,
+ * heat, helmholtz, poisson with method 1: r2c, the symbol in double, c2r);
+ * the single-axis transforms, grad, divergence and the finite-difference
+ * Poisson method stay with plain double plans.  The exponent lives in one
+ * word of the plan, so two transforms of one plan must not overlap on the
+ * GPU. */
 #define ACCFFT_C_F64_DF 0x400u
 
 typedef struct accfft_c_plan accfft_c_plan; /* opaque */
