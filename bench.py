@@ -78,7 +78,7 @@ def parse():
     ap.add_argument("--no-baseline", action="store_true")
     ap.add_argument("--no-variants", action="store_true", help="skip the tensor-core and FP64 forms of the pair")
     ap.add_argument("--passes", type=int, nargs=4, default=None, metavar=("Y", "X", "ZR2C", "ZC2R"),
-                    help="pairs workload: fix the radix / tile variants of the y, x, z r2c and z c2r passes "
+                    help="pairs and call workloads: fix the radix / tile variants of the y, x, z r2c and z c2r passes "
                          "instead of timing them at plan creation (ACCFFT_MEASURE); profiler captures use "
                          "this so the captured kernels do not depend on timings taken under the profiler")
     return ap.parse_args()
@@ -1152,6 +1152,8 @@ def call_workload(args):
         plan = ag.PlanR2C(n, dt, flags=flags) if flags else ag.PlanR2C(n, dt)
         if not flags:
             plan.set_pass_order(1 if args.order == "packed" else 0)
+            if args.passes:
+                plan.set_variants(*args.passes)
         plan.r2c(u, spec)
         fn = {"r2c": lambda: plan.r2c(u, spec), "c2r": lambda: plan.c2r(spec, outs[0]),
               "laplace": lambda: plan.laplace(outs[0], u),
