@@ -68,6 +68,7 @@ def lib() -> ctypes.CDLL:
         "accfft_c_last_error_code": ([], i),
         "accfft_c_version": ([], i),
         "accfft_c_length_supported": ([i], i),
+        "accfft_c_length_generic": ([i], i),
         "accfft_c_line_plan": ([i, i, ip, ip, ip], i),
         "accfft_c_kernel_launches": ([], ctypes.c_ulonglong),
         "accfft_c_set_pdl": ([ctypes.c_int], ctypes.c_int),

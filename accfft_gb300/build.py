@@ -96,7 +96,7 @@ def build(verbose: bool = False, jobs: int | None = None) -> str:
         cmd = ["g++", *CXX_FLAGS, "-I", cuda_inc, "-c", src, "-o", obj]
         work.append((src, obj, cmd, _digest([src] + hdrs, cmd[1:])))
     for name in ("noalloc.cu", "slab.cu", "tc_kernels.cu", "zy_fused.cu", "df_scale.cu", "accum.cu", "variants.cu",
-                 "df_sym.cu"):
+                 "sym_spectrum.cu", "gen.cu"):
         src = os.path.join(CSRC, name)
         obj = os.path.join(OBJ, name.replace(".cu", ".o"))
         cmd = [nvcc, *NVCC_FLAGS, "-c", src, "-o", obj]

@@ -94,6 +94,33 @@ struct ContigArgs {
   int variant;              // as StridedArgs::variant (float z r2c / z c2r)
 };
 
+// Lines of a length without compiled kernels (gen.cu): a runtime radix plan
+// (radix[s], stage twiddles at tw + off[s]: entry (r-1)*Ns + k is
+// w_{Ns*R}^{r*k}), run over the lines of one pass.
+constexpr int kGenMaxStages = 16;
+struct GenPlan {
+  int L;                    // line length (the full real length N2 for r2c / c2r)
+  int nst;
+  int radix[kGenMaxStages];
+  int off[kGenMaxStages];   // complex entries into tw
+  const void* tw;           // in the plan's precision
+};
+struct GenArgs {
+  GenPlan g;
+  const void* in;
+  void* out;
+  long long nlines;         // lines (columns of a strided pass)
+  // strided lines (y and x passes): line c starts at slab * slab + cc, c =
+  // slab * cps + cc, element p at p * line (complex elements)
+  long long cps, in_slab, out_slab, in_line, out_line;
+  // contiguous lines (z passes): line l starts at l * dist (elements of the
+  // array's own type: reals for the real side of r2c / c2r)
+  long long in_dist, out_dist;
+  int inverse;
+  int tc;                   // lines per CTA (a power of two up to 16)
+  int early_trigger;
+};
+
 struct SlabArgs {
   const void* in;           // forward: real [N0][N1][row]; inverse: spectrum [N0][N1][N2/2+1]
   void* out;                // forward: spectrum; inverse: real

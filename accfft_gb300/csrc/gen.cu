@@ -1,0 +1,222 @@
+// Line FFTs of lengths without compiled kernels (float and double plans).
+//
+// The compiled passes (kernels.cu) fix the line length, radix plan and tile
+// shape at compile time for the lengths of AFG_LENGTHS_*; any other length
+// whose prime factors are at most 31 runs here, from a radix plan chosen at
+// plan creation (gen_factor: radices up to 16, primes 17..31 alone), with
+// TC lines per CTA held in shared memory and the Stockham stages run
+// between two shared-memory buffers (stage s of radix R reads x[j + r*L/R],
+// multiplies by w_{Ns*R}^{(j%Ns)*r} and writes y[(j/Ns)*Ns*R + j%Ns + r*Ns],
+// the R-point DFT in registers from the same codelets as the compiled
+// engine).  These kernels make every such grid run; they are not tuned.
+//
+// Four kernels:
+//   k_gen_strided  c2c along strided lines (y and x passes)
+//   k_gen_c2c      c2c along contiguous lines (z pass of c2c plans)
+//   k_gen_r2c      real lines of L -> L/2+1 complex (z pass of r2c plans,
+//                  odd L included: the real line as a complex line)
+//   k_gen_c2r      L/2+1 complex -> real lines of L (the Hermitian
+//                  completion, imaginary parts of kz = 0 and L/2 dropped)
+// Inverse transforms conjugate on the way in and out.
+#include "launch.h"
+#include "passes.cuh"
+#include "per_device.h"
+
+namespace afg {
+
+namespace {
+
+constexpr int kGenThreads = 256;
+
+template <typename T, int R>
+__device__ __forceinline__ void gen_stage(const typename CT<T>::V* __restrict__ in, typename CT<T>::V* __restrict__ out,
+                                          const typename CT<T>::V* __restrict__ tw, int L, int Ns, int tc, int c,
+                                          int j0, int jstep) {
+  typedef typename CT<T>::V V;
+  const int nb = L / R;
+  for (int j = j0; j < nb; j += jstep) {
+    const int k = j % Ns;
+    V v[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) v[r] = in[(j + r * nb) * tc + c];
+#pragma unroll
+    for (int r = 1; r < R; ++r) v[r] = c_mul(v[r], ld_tw(tw + (r - 1) * Ns + k));
+    Dft<R, 1>::run(v);
+    const int base = (j / Ns) * Ns * R + k;
+#pragma unroll
+    for (int q = 0; q < R; ++q) out[(base + q * Ns) * tc + c] = v[q];
+  }
+}
+
+// every stage over the CTA's tc lines, buffer a holding entry p of line c at
+// p*tc + c; returns the buffer holding the result
+template <typename T>
+__device__ typename CT<T>::V* gen_fft(typename CT<T>::V* a, typename CT<T>::V* b, const GenPlan& g, int tc) {
+  typedef typename CT<T>::V V;
+  const int c = threadIdx.x % tc, j0 = threadIdx.x / tc, jstep = kGenThreads / tc;
+  const V* tw = static_cast<const V*>(g.tw);
+  int Ns = 1;
+  for (int s = 0; s < g.nst; ++s) {
+    const V* t = tw + g.off[s];
+    switch (g.radix[s]) {
+#define AFG_GEN_R(R) \
+  case R: gen_stage<T, R>(a, b, t, g.L, Ns, tc, c, j0, jstep); break;
+      AFG_GEN_R(2) AFG_GEN_R(3) AFG_GEN_R(4) AFG_GEN_R(5) AFG_GEN_R(6) AFG_GEN_R(7) AFG_GEN_R(8) AFG_GEN_R(9)
+      AFG_GEN_R(10) AFG_GEN_R(11) AFG_GEN_R(12) AFG_GEN_R(13) AFG_GEN_R(14) AFG_GEN_R(15) AFG_GEN_R(16)
+      AFG_GEN_R(17) AFG_GEN_R(19) AFG_GEN_R(23) AFG_GEN_R(29) AFG_GEN_R(31)
+#undef AFG_GEN_R
+      default: break;   // gen_factor produces no other radix
+    }
+    __syncthreads();
+    V* x = a;
+    a = b;
+    b = x;
+    Ns *= g.radix[s];
+  }
+  return a;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kGenThreads) k_gen_strided(const GenArgs ga) {
+  typedef typename CT<T>::V V;
+  PassScope scope(ga.early_trigger);
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int L = ga.g.L, tc = ga.tc;
+  V* a = reinterpret_cast<V*>(smraw);
+  V* b = a + (size_t)L * tc;
+  const long long g0 = (long long)blockIdx.x * tc;
+  const T sg = ga.inverse ? T(-1) : T(1);
+  const V* in = static_cast<const V*>(ga.in);
+  for (int e = threadIdx.x; e < L * tc; e += kGenThreads) {
+    const int p = e / tc, c = e % tc;
+    const long long col = g0 + c;
+    V x = c_make<V>(T(0), T(0));
+    if (col < ga.nlines) {
+      const long long slab = col / ga.cps;
+      x = in[slab * ga.in_slab + (col - slab * ga.cps) + (long long)p * ga.in_line];
+      x.y *= sg;
+    }
+    a[e] = x;
+  }
+  __syncthreads();
+  const V* res = gen_fft<T>(a, b, ga.g, tc);
+  V* out = static_cast<V*>(ga.out);
+  for (int e = threadIdx.x; e < L * tc; e += kGenThreads) {
+    const int p = e / tc, c = e % tc;
+    const long long col = g0 + c;
+    if (col < ga.nlines) {
+      const long long slab = col / ga.cps;
+      V x = res[e];
+      x.y *= sg;
+      out[slab * ga.out_slab + (col - slab * ga.cps) + (long long)p * ga.out_line] = x;
+    }
+  }
+}
+
+// contiguous lines: MODE 0 c2c, 1 r2c, 2 c2r
+template <typename T, int MODE>
+__global__ void __launch_bounds__(kGenThreads) k_gen_contig(const GenArgs ga) {
+  typedef typename CT<T>::V V;
+  PassScope scope(ga.early_trigger);
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int L = ga.g.L, tc = ga.tc, H = L / 2 + 1;
+  V* a = reinterpret_cast<V*>(smraw);
+  V* b = a + (size_t)L * tc;
+  const long long l0 = (long long)blockIdx.x * tc;
+  const T sg = ga.inverse ? T(-1) : T(1);
+  // load: entry p of line c (consecutive threads along p)
+  for (int e = threadIdx.x; e < L * tc; e += kGenThreads) {
+    const int c = e / L, p = e % L;
+    const long long l = l0 + c;
+    V x = c_make<V>(T(0), T(0));
+    if (l < ga.nlines) {
+      if constexpr (MODE == 0) {
+        x = static_cast<const V*>(ga.in)[l * ga.in_dist + p];
+        x.y *= sg;
+      } else if constexpr (MODE == 1) {
+        x.x = static_cast<const T*>(ga.in)[l * ga.in_dist + p];
+      } else {
+        // the full spectrum from the half one (Hermitian completion), then
+        // conjugated for the forward engine
+        const V* h = static_cast<const V*>(ga.in) + l * ga.in_dist;
+        if (p < H) {
+          x = h[p];
+          if (p == 0 || 2 * p == L) x.y = T(0);
+        } else {
+          x = h[L - p];
+          x.y = -x.y;
+        }
+        x.y = -x.y;
+      }
+    }
+    a[p * tc + c] = x;
+  }
+  __syncthreads();
+  const V* res = gen_fft<T>(a, b, ga.g, tc);
+  for (int e = threadIdx.x; e < L * tc; e += kGenThreads) {
+    const int c = e / L, p = e % L;
+    const long long l = l0 + c;
+    if (l >= ga.nlines) continue;
+    V x = res[p * tc + c];
+    if constexpr (MODE == 0) {
+      x.y *= sg;
+      static_cast<V*>(ga.out)[l * ga.out_dist + p] = x;
+    } else if constexpr (MODE == 1) {
+      if (p < H) static_cast<V*>(ga.out)[l * ga.out_dist + p] = x;
+    } else {
+      static_cast<T*>(ga.out)[l * ga.out_dist + p] = x.x;   // real part of the conjugated result
+    }
+  }
+}
+
+template <typename T, typename K>
+bool gen_launch(K kernel, const GenArgs& g, cudaStream_t s) {
+  typedef typename CT<T>::V V;
+  const size_t smem = 2 * (size_t)g.g.L * g.tc * sizeof(V);
+  static PerDevice prepared;
+  int dev = 0;
+  // the shared-memory opt-in is per kernel and size: set it on every launch
+  // above the default (cheap, and the sizes differ between lengths)
+  if (smem > 48 * 1024 && (cudaGetDevice(&dev) != cudaSuccess ||
+                           cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)) !=
+                               cudaSuccess))
+    return false;
+  (void)prepared;
+  GenArgs b = g;
+  b.early_trigger = pdl_mode() == 2;
+  const long long grid = (g.nlines + g.tc - 1) / g.tc;
+  return launch_pass(kernel, unsigned(grid), kGenThreads, smem, s, b) == cudaSuccess;
+}
+
+}  // namespace
+
+// lines of L per CTA for the generic kernels: as many as fit 96 KB of
+// shared memory (two buffers), at most 16, at least 1
+int gen_lines_per_cta(int L, bool dbl) {
+  const size_t per = 2 * (size_t)L * (dbl ? 16 : 8);
+  int tc = 16;
+  while (tc > 1 && per * tc > 96 * 1024) tc /= 2;
+  return tc;
+}
+
+bool launch_gen(int prec, int mode, const GenArgs& g, cudaStream_t s) {
+  // mode: 0 strided c2c, 1 contiguous c2c, 2 r2c, 3 c2r
+  if (prec == PREC_F32) {
+    switch (mode) {
+      case 0: return gen_launch<float>(k_gen_strided<float>, g, s);
+      case 1: return gen_launch<float>(k_gen_contig<float, 0>, g, s);
+      case 2: return gen_launch<float>(k_gen_contig<float, 1>, g, s);
+      case 3: return gen_launch<float>(k_gen_contig<float, 2>, g, s);
+    }
+  } else if (prec == PREC_F64) {
+    switch (mode) {
+      case 0: return gen_launch<double>(k_gen_strided<double>, g, s);
+      case 1: return gen_launch<double>(k_gen_contig<double, 0>, g, s);
+      case 2: return gen_launch<double>(k_gen_contig<double, 1>, g, s);
+      case 3: return gen_launch<double>(k_gen_contig<double, 2>, g, s);
+    }
+  }
+  return false;
+}
+
+}  // namespace afg

@@ -101,9 +101,14 @@ bool launch_strided_variant_f32(int L, int v, const StridedArgs& a, cudaStream_t
 bool launch_contig_variant_f32(bool r2c, int M, int v, const ContigArgs& a, cudaStream_t s);
 void variant_shape(int kind, int L, int v, int* E, int* tile);
 constexpr int kMaxVariant = 3;
-// spec[n0][cols] (double complex) *= the symbol of s at (x, column), for the
-// operators of double-float plans (df_sym.cu)
-bool launch_sym_spectrum_f64(void* spec, long long n0, long long cols, const SymArgs& s, cudaStream_t st);
+// spec[n0][cols] (complex, float or double) *= the symbol of s at
+// (x, column), for the operators that run as r2c, symbol, c2r
+// (sym_spectrum.cu)
+bool launch_sym_spectrum(bool dbl, void* spec, long long n0, long long cols, const SymArgs& s, cudaStream_t st);
+// lines of lengths without compiled kernels (gen.cu): mode 0 strided c2c,
+// 1 contiguous c2c, 2 r2c, 3 c2r; float and double plans
+bool launch_gen(int prec, int mode, const GenArgs& g, cudaStream_t s);
+int gen_lines_per_cta(int L, bool dbl);
 
 // pass kinds of a recorded batch task (plan.cpp) and their grouped launch
 enum PassKind { PK_STRIDED = 0, PK_ZR2C = 2, PK_ZC2R = 3 };

@@ -16,6 +16,7 @@
 #include <cstdio>
 #include <cstring>
 #include <algorithm>
+#include <functional>
 #include <map>
 #include <string>
 #include <deque>
@@ -98,6 +99,69 @@ std::vector<long double> stage_table(int L, int cls, int first_radix = 0) {
         t[2 * i + 1] = si;
       }
   }
+  return t;
+}
+
+// Radix plan of the generic kernels (gen.cu) for a line of L: the prime
+// factors (at most 31) combined greedily into radices of at most 16, primes
+// above 16 alone; false when L has a larger prime factor, exceeds 4096 or
+// needs more than kGenMaxStages stages.  Lengths of one or no stage are fine.
+bool gen_factor(int L, GenPlan* g) {
+  if (L < 1 || L > 4096) return false;
+  std::vector<int> pf;
+  int m = L;
+  for (int q = 2; q * q <= m; ++q)
+    while (m % q == 0) {
+      pf.push_back(q);
+      m /= q;
+    }
+  if (m > 1) pf.push_back(m);
+  for (int q : pf)
+    if (q > 31) return false;
+  std::sort(pf.begin(), pf.end(), std::greater<int>());
+  std::vector<int> rad;
+  for (int q : pf) {
+    bool merged = false;
+    if (q <= 16)
+      for (int& r : rad)
+        if (r <= 16 && r * q <= 16) {
+          r *= q;
+          merged = true;
+          break;
+        }
+    if (!merged) rad.push_back(q);
+  }
+  if ((int)rad.size() > kGenMaxStages) return false;
+  if (g) {
+    g->L = L;
+    g->nst = (int)rad.size();
+    int off = 0, Ns = 1;
+    for (int s = 0; s < g->nst; ++s) {
+      g->radix[s] = rad[s];
+      g->off[s] = off;
+      off += (rad[s] - 1) * Ns;
+      Ns *= rad[s];
+    }
+  }
+  return true;
+}
+// stage twiddles of a generic radix plan: entry (r-1)*Ns + k of stage s is
+// w_{Ns*R}^{r*k}
+std::vector<long double> gen_table(const GenPlan& g) {
+  std::vector<long double> t;
+  int Ns = 1;
+  for (int s = 0; s < g.nst; ++s) {
+    const int R = g.radix[s];
+    for (int r = 1; r < R; ++r)
+      for (int k = 0; k < Ns; ++k) {
+        long double c, sn;
+        twiddle((long long)r * k, (long long)Ns * R, &c, &sn);
+        t.push_back(c);
+        t.push_back(sn);
+      }
+    Ns *= R;
+  }
+  if (t.empty()) t.assign(2, 0.0L);
   return t;
 }
 
@@ -187,6 +251,11 @@ struct accfft_c_plan {
   // main [N0][N1][M] (rows of M = N2/2 complex, 128-byte aligned) and the
   // Nyquist plane [N0][N1] (kz = N2/2) after it
   bool split = false;
+  // axes (x, y, z) whose lines have no compiled kernels run the generic
+  // kernels (gen.cu) with a radix plan made here; gen_any: at least one
+  bool gen[3] = {false, false, false};
+  bool gen_any = false;
+  afg::GenPlan gp[3] = {};
   // tensor-core form (ACCFFT_C_TC_*): 0 none, 1 3xTF32, 2 split BF16
   int tc = 0;
   // device word set by a kernel whose bounded wait gave up (tensor-core
@@ -267,25 +336,32 @@ accfft_c_plan* make_plan(int kind, bool dbl, const int* n, void* data, void* dat
       fail(ACCFFT_C_EINVAL, "plan: size n[%d]=%d must be positive", i, n[i]);
       return nullptr;
     }
-  if (kind == 1 && n[2] % 2) {
-    fail(ACCFFT_C_EUNSUPPORTED, "plan: r2c needs an even N2 (got %d)", n[2]);
-    return nullptr;
-  }
   int zlen = kind == 1 ? n[2] / 2 : n[2];
-  int lens[3] = {n[0], n[1], zlen};
+  // axes without compiled kernels take the generic kernels when their length
+  // factors into primes up to 31 (the real z axis of r2c plans then as a
+  // whole line of N2, odd N2 included)
+  bool gen[3] = {!length_supported(n[0]), !length_supported(n[1]),
+                 kind == 1 ? (n[2] % 2 != 0 || !length_supported(n[2] / 2)) : !length_supported(n[2])};
+  const int glen[3] = {n[0], n[1], n[2]};
   for (int i = 0; i < 3; ++i)
-    if (!length_supported(lens[i])) {
-      fail(ACCFFT_C_EUNSUPPORTED, "plan: no kernels for %s length %d (sizes %dx%dx%d)",
-           i == 0 ? "x" : i == 1 ? "y" : "z", lens[i], n[0], n[1], n[2]);
+    if (gen[i] && !gen_factor(glen[i], nullptr)) {
+      fail(ACCFFT_C_EUNSUPPORTED, "plan: no kernels for %s length %d (sizes %dx%dx%d): lengths up to 4096 whose "
+           "prime factors are at most 31", i == 0 ? "x" : i == 1 ? "y" : "z", glen[i], n[0], n[1], n[2]);
       return nullptr;
     }
+  const bool gen_any = gen[0] || gen[1] || gen[2];
+  if (gen_any && (dbl && (flags & ACCFFT_C_F64_DF))) {
+    fail(ACCFFT_C_EUNSUPPORTED, "plan: double-float plans need compiled lengths (sizes %dx%dx%d)", n[0], n[1], n[2]);
+    return nullptr;
+  }
   const unsigned tcf = flags & (ACCFFT_C_TC_TF32 | ACCFFT_C_TC_BF16);
   if (tcf) {
     if (tcf == (ACCFFT_C_TC_TF32 | ACCFFT_C_TC_BF16) || kind != 1 || dbl) {
       fail(ACCFFT_C_EUNSUPPORTED, "plan: tensor-core forms are float r2c plans with one of the two flags");
       return nullptr;
     }
-    if (!tc_length_supported(n[0], false) || !tc_length_supported(n[1], false) || !tc_length_supported(zlen, true)) {
+    if (gen_any || !tc_length_supported(n[0], false) || !tc_length_supported(n[1], false) ||
+        !tc_length_supported(zlen, true)) {
       fail(ACCFFT_C_EUNSUPPORTED, "plan: no tensor-core kernels for %dx%dx%d (x, y in 128..1024, N2/2 in 128..512, "
            "powers of two)", n[0], n[1], n[2]);
       return nullptr;
@@ -298,6 +374,11 @@ accfft_c_plan* make_plan(int kind, bool dbl, const int* n, void* data, void* dat
   auto* p = new accfft_c_plan;
   p->kind = kind;
   p->tc = tcf == ACCFFT_C_TC_TF32 ? 1 : tcf == ACCFFT_C_TC_BF16 ? 2 : 0;
+  for (int i = 0; i < 3; ++i) {
+    p->gen[i] = gen[i];
+    if (gen[i]) gen_factor(glen[i], &p->gp[i]);
+  }
+  p->gen_any = gen_any;
   p->df = (flags & ACCFFT_C_F64_DF) != 0;
   p->dbl = dbl;
   for (int i = 0; i < 3; ++i) p->n[i] = n[i];
@@ -348,6 +429,12 @@ accfft_c_plan* make_plan(int kind, bool dbl, const int* n, void* data, void* dat
       tabs.push_back(alt_e[a] ? stage_table(lens[a], 0, alt_e[a]) : std::vector<long double>(2, 0.0L));
     }
   }
+  int gen_tab[3] = {-1, -1, -1};
+  for (int i = 0; i < 3; ++i)
+    if (p->gen[i]) {
+      gen_tab[i] = (int)tabs.size();
+      tabs.push_back(gen_table(p->gp[i]));
+    }
   const size_t cbytes = dbl ? 16 : 8;
   std::vector<size_t> off;
   size_t total = 0;
@@ -402,7 +489,7 @@ accfft_c_plan* make_plan(int kind, bool dbl, const int* n, void* data, void* dat
     // operators keep their spectrum in the split layout when its rows of M
     // complex are 128-byte aligned (M a multiple of 16 for float, 8 for double)
     const int M = n[2] / 2;
-    p->split = M >= 8 && M % (dbl ? 8 : 16) == 0;
+    p->split = M >= 8 && M % (dbl ? 8 : 16) == 0 && !p->gen_any;
     if (const char* hb = getenv("ACCFFT_GB300_HOST_BATCHES")) {
       const int v = atoi(hb);
       p->host_batches = v < 1 ? 1 : (v > accfft_c_plan::kHostBatches ? accfft_c_plan::kHostBatches : v);
@@ -414,7 +501,7 @@ accfft_c_plan* make_plan(int kind, bool dbl, const int* n, void* data, void* dat
     const char* ord = getenv("ACCFFT_GB300_ORDER");
     p->packed = packed_eligible(p) && !(ord && std::string(ord) == "natural");
     const char* env = getenv("ACCFFT_GB300_ZY");
-    std::string zy = env ? env : "";
+    std::string zy = env && !p->gen_any ? env : "";
     if (zy == "fused" && slab_available(dbl, n[1], n[2])) {
       p->zy_mode = 1;
     } else if (zy == "persistent") {
@@ -432,6 +519,8 @@ accfft_c_plan* make_plan(int kind, bool dbl, const int* n, void* data, void* dat
   p->tw_z = base + off[2];
   if (kind == 1) p->tw_post = base + off[3];
   if (kind == 1) p->fd_tab = base + off[4];
+  for (int i = 0; i < 3; ++i)
+    if (gen_tab[i] >= 0) p->gp[i].tw = base + off[(size_t)gen_tab[i]];
   if (alt_tables) {
     p->tw_x_alt = alt_e[0] ? base + off[5] : nullptr;
     p->tw_y_alt = alt_e[1] ? base + off[6] : nullptr;
@@ -589,6 +678,12 @@ struct Exec {
   void strided(const void* in, void* out, const void* tw, int L, long long ncols, long long cps, long long slab,
                long long line, int inverse) {
     if (!ok()) return;
+    const int axis = tw == p->tw_x ? 0 : 1;
+    if (p->gen[axis]) {
+      gen_strided(axis, in, out, ncols, cps, slab, line, inverse,
+                  axis == 0 ? (inverse ? "x_inv" : "x") : (inverse ? "y_inv" : "y"));
+      return;
+    }
     StridedArgs a{};
     a.dfx = p->df_exp;
     a.in = in;
@@ -627,13 +722,51 @@ struct Exec {
       unsupported("symbol pass", L);
   }
   // y pass over an [N0][N1][h] complex array, x pass over [N0][N1*h]
-  // the symbol multiply of a double-float plan's operator over the natural
+  // the symbol multiply of an operator that runs as r2c, symbol, c2r
+  // (double-float plans, plans with generic-length axes) over the natural
   // spectrum in the plan scratch
   void sym_spectrum(void* spec, const SymArgs& s) {
     if (!ok()) return;
     const long long cols = (long long)p->n[1] * p->H2();
-    if (!timed("sym", p->stream, [&] { return launch_sym_spectrum_f64(spec, p->n[0], cols, s, p->stream); }))
+    if (!timed("sym", p->stream, [&] { return launch_sym_spectrum(p->dbl, spec, p->n[0], cols, s, p->stream); }))
       rc = fail(ACCFFT_C_ECUDA, "operator: symbol pass launch failed");
+  }
+  // lines of an axis without compiled kernels (gen.cu)
+  void gen_strided(int axis, const void* in, void* out, long long ncols, long long cps, long long slab,
+                   long long line, int inverse, const char* label) {
+    if (!ok() || not_recordable("a pass of a length without compiled kernels")) return;
+    GenArgs g{};
+    g.g = p->gp[axis];
+    g.in = in;
+    g.out = out;
+    g.nlines = ncols;
+    g.cps = cps;
+    g.in_slab = g.out_slab = slab;
+    g.in_line = g.out_line = line;
+    g.inverse = inverse;
+    g.tc = gen_lines_per_cta(g.g.L, p->dbl);
+    if (!timed(label, p->stream, [&] { return launch_gen(p->prec(), 0, g, p->stream); }))
+      rc = fail(ACCFFT_C_ECUDA, "%s: generic pass launch failed (length %d)", label, g.g.L);
+  }
+  // z lines of an axis without compiled kernels: mode 1 c2c, 2 r2c, 3 c2r
+  void gen_z(int mode, const void* in, void* out, long long in_dist, long long out_dist, int inverse,
+             const char* label) {
+    if (!ok() || not_recordable("a pass of a length without compiled kernels")) return;
+    if (weight) {
+      rc = fail(ACCFFT_C_EUNSUPPORTED, "%s: adjoint weighting needs compiled z lengths", label);
+      return;
+    }
+    GenArgs g{};
+    g.g = p->gp[2];
+    g.in = in;
+    g.out = out;
+    g.nlines = (long long)p->n[0] * p->n[1];
+    g.in_dist = in_dist;
+    g.out_dist = out_dist;
+    g.inverse = inverse;
+    g.tc = gen_lines_per_cta(g.g.L, p->dbl);
+    if (!timed(label, p->stream, [&] { return launch_gen(p->prec(), mode, g, p->stream); }))
+      rc = fail(ACCFFT_C_ECUDA, "%s: generic pass launch failed (length %d)", label, g.g.L);
   }
   void ypass(const void* in, void* out, long long h, int inverse) {
     strided(in, out, p->tw_y, p->n[1], (long long)p->n[0] * h, h, (long long)p->n[1] * h, h, inverse);
@@ -644,6 +777,10 @@ struct Exec {
   }
   void zr2c(const void* in, void* out, long long in_row) {
     if (!ok()) return;
+    if (p->gen[2]) {
+      gen_z(2, in, out, in_row, p->H2(), 0, "z_r2c");
+      return;
+    }
     ContigArgs a{};
     a.dfx = p->df_exp;
     a.weight = weight;
@@ -666,6 +803,10 @@ struct Exec {
   }
   void zc2r(const void* in, void* out, long long out_row) {
     if (!ok()) return;
+    if (p->gen[2]) {
+      gen_z(3, in, out, p->H2(), out_row, 0, "z_c2r");
+      return;
+    }
     ContigArgs a{};
     a.dfx = p->df_exp;
     a.weight = weight;
@@ -1030,6 +1171,10 @@ struct Exec {
   }
   void zc2c(const void* in, void* out, int inverse) {
     if (!ok() || not_recordable("a z c2c pass")) return;
+    if (p->gen[2]) {
+      gen_z(1, in, out, p->n[2], p->n[2], inverse, "z_c2c");
+      return;
+    }
     ContigArgs a{};
     a.dfx = p->df_exp;
     a.in = in;
@@ -1211,7 +1356,7 @@ struct Exec {
 
 // plans that can run the packed pass order (exec_r2c_plan)
 bool packed_eligible(const accfft_c_plan* p) {
-  return p->kind == 1 && !p->inplace && !p->tc && !p->df && p->scratch != nullptr;
+  return p->kind == 1 && !p->inplace && !p->tc && !p->df && !p->gen_any && p->scratch != nullptr;
 }
 
 // every array is accessed as whole complex elements (8 or 16 bytes)
@@ -1362,6 +1507,19 @@ int check_plan(accfft_c_plan* p, int kind, int dbl, const char* fn) {
     return fail(ACCFFT_C_EINVAL, "%s: precision mismatch (plan is %s)", fn, p->dbl ? "double" : "float");
   if (p->tc && strcmp(fn, "execute_r2c") && strcmp(fn, "execute_c2r") && strcmp(fn, "execute"))
     return fail(ACCFFT_C_EUNSUPPORTED, "%s: tensor-core plans run full r2c / c2r transforms only", fn);
+  if (p->gen_any) {
+    // axes without compiled kernels: the transforms (any xyz) and the 3-D
+    // operators, which run as r2c, symbol, c2r
+    static const char* const gen_ok[] = {"execute_r2c", "execute_c2r", "execute", "execute_c2c", "laplace",
+                                         "biharmonic", "inv_laplace", "inv_biharmonic", "heat", "helmholtz",
+                                         "poisson"};
+    bool ok = false;
+    for (const char* f : gen_ok) ok = ok || !strcmp(fn, f);
+    if (!ok)
+      return fail(ACCFFT_C_EUNSUPPORTED,
+                  "%s: the plan has an axis length without compiled kernels (%dx%dx%d); such plans run the "
+                  "transforms and the 3-D spectral operators only", fn, p->n[0], p->n[1], p->n[2]);
+  }
   if (p->df) {
     static const char* const df_ok[] = {"execute_r2c", "execute_c2r", "execute", "execute_c2c", "laplace",
                                         "biharmonic", "inv_laplace", "inv_biharmonic", "heat", "helmholtz",
@@ -1405,6 +1563,8 @@ int exec_r2c_plan(accfft_c_plan* p, int direction, void* in, void* out, double* 
   }
   if (p->df && (host_in || host_out))
     return fail(ACCFFT_C_EUNSUPPORTED, "execute: double-float plans take device arrays");
+  if (p->gen_any && (host_in || host_out))
+    return fail(ACCFFT_C_EUNSUPPORTED, "execute: plans with an axis length without compiled kernels take device arrays");
   if (p->packed && (xyz & 7) == 7 && weight == 0 && p->zy_mode == 0 && (direction == -1 || direction == 1)) {
     // packed order: r2c = y, x over the packed real field (in -> scratch),
     // then the mirror-pair z pass (scratch -> natural spectrum); c2r the
@@ -1434,7 +1594,7 @@ int exec_r2c_plan(accfft_c_plan* p, int direction, void* in, void* out, double* 
   else ex.df_scan(in, 1, spec_doubles, spec_doubles);
   if (direction == -1) {
     void* work = in;   // with z skipped the reference transforms the input in place
-    if ((xyz & ZB) && (xyz & YB)) {
+    if ((xyz & ZB) && (xyz & YB) && !p->gen_any) {
       if (host_in) ex.zy_host(true, in, nullptr, out, p->rrow());
       else ex.zy(true, in, nullptr, out, p->rrow());
       work = out;
@@ -1455,7 +1615,7 @@ int exec_r2c_plan(accfft_c_plan* p, int direction, void* in, void* out, double* 
       ex.xpass(src, buf, h, 1);
       src = buf;
     }
-    if ((xyz & YB) && (xyz & ZB)) {
+    if ((xyz & YB) && (xyz & ZB) && !p->gen_any) {
       if (host_out) ex.zy_host(false, src, buf, out, p->rrow());
       else ex.zy(false, src, buf, out, p->rrow());
     } else {
@@ -1523,11 +1683,12 @@ int op3d(accfft_c_plan* p, int sym_kind, void* outr, const void* inr, double* ti
   Exec ex(p, timer);
   SymArgs sym = make_sym(p, sym_kind, 1.0 / N);
   sym.param = param;
-  if (p->df) {
-    // double-float plans: the plan's r2c, the symbol multiply in double over
-    // the spectrum, the plan's c2r (each transform scans its own input for
-    // the exponent its passes scale by)
-    if (sym_kind == SYM_POISSON_FD)
+  if (p->df || p->gen_any) {
+    // double-float plans and plans with a generic-length axis: the plan's
+    // r2c, the symbol multiply over the spectrum, the plan's c2r (in
+    // double-float each transform scans its own input for the exponent its
+    // passes scale by)
+    if (sym_kind == SYM_POISSON_FD && p->df)
       return fail(ACCFFT_C_EUNSUPPORTED, "poisson: double-float plans take the spectral method (1) only");
     void* s = p->scratch;
     const long long spec_doubles = 2LL * p->n[0] * p->n[1] * h;
@@ -1597,6 +1758,7 @@ const char* accfft_c_last_error(void) { return g_err.c_str(); }
 int accfft_c_last_error_code(void) { return g_err_code; }
 int accfft_c_version(void) { return 1; }
 int accfft_c_length_supported(int len) { return length_supported(len) ? 1 : 0; }
+int accfft_c_length_generic(int len) { return gen_factor(len, nullptr) ? 1 : 0; }
 int accfft_c_line_plan(int len, int precision, int* E, int* P, int* radices) {
   if (len < 1 || precision < 0 || precision > 2 || !E || !P || !radices) return -1;
   const LinePlan pl = plan_select(len, precision, 0);

@@ -83,6 +83,14 @@ int accfft_c_version(void);
 /* 1 if an axis of this length has compiled kernels (complex length for
  * c2c axes; for the real z axis of an r2c plan the check is on N2/2) */
 int accfft_c_length_supported(int len);
+/* 1 if a line of this length runs on the generic kernels (lengths up to
+ * 4096 whose prime factors are at most 31; the real z axis of an r2c plan
+ * as its full length N2, odd N2 included).  Plans whose axes are all either
+ * compiled or generic are accepted; an axis on the generic kernels limits
+ * the plan to the transforms (any xyz, device arrays) and the 3-D spectral
+ * operators, which then run as r2c, a symbol pass and c2r; such plans are
+ * float or double (not double-float or tensor-core) and are not tuned. */
+int accfft_c_length_generic(int len);
 /* the compiled radix plan of a line length for the arithmetic `precision`
  * (0 float, 1 double, 2 double-float): first radix *E, threads per line *P
  * and the stage radices in radices[0..] (at most 16); returns the number of

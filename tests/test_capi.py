@@ -58,16 +58,26 @@ def test_supported_lengths(native):
         assert L.accfft_c_length_supported(n) == 1, n
     for n in (7, 11, 13, 17, 1000003):
         assert L.accfft_c_length_supported(n) == 0, n
+    # lengths without compiled kernels that the generic kernels take: prime
+    # factors up to 31, at most 4096
+    for n in (7, 11, 13, 14, 18, 27, 31, 36, 62, 121, 2048, 4096):
+        assert L.accfft_c_length_generic(n) == 1, n
+    for n in (37, 74, 97, 4100, 1000003):
+        assert L.accfft_c_length_generic(n) == 0, n
 
 
 def test_plan_rejects_bad_sizes(native):
     L = native.lib()
-    n = (ctypes.c_int * 3)(8, 8, 7)
+    n = (ctypes.c_int * 3)(8, 8, 74)
     assert not L.accfft_c_plan_dft_3d_r2c_gpuf(n, None, None, 2)
-    assert "even N2" in native.last_error()
-    n = (ctypes.c_int * 3)(8, 13, 8)
+    assert "length 74" in native.last_error()
+    n = (ctypes.c_int * 3)(8, 37, 8)
     assert not L.accfft_c_plan_dft_3d_c2c_gpu(n, None, None, 2)
-    assert "length 13" in native.last_error()
+    assert "length 37" in native.last_error()
+    assert L.accfft_c_last_error_code() == native.EUNSUPPORTED
+    # double-float plans need compiled lengths (rejected before any device call)
+    n = (ctypes.c_int * 3)(8, 13, 8)
+    assert not L.accfft_c_plan_dft_3d_r2c_gpu(n, None, None, native.F64_DF)
     assert L.accfft_c_last_error_code() == native.EUNSUPPORTED
     n = (ctypes.c_int * 3)(0, 8, 8)
     assert not L.accfft_c_plan_dft_3d_r2c_gpu(n, None, None, 2)
@@ -83,7 +93,7 @@ def test_plan_rejects_bad_sizes(native):
 
 def test_python_plan_errors_carry_the_code(native):
     with pytest.raises(native.AccfftError) as e:
-        native.PlanR2C((8, 13, 8), "float32")
+        native.PlanR2C((8, 37, 8), "float32")
     assert e.value.code == native.EUNSUPPORTED
     with pytest.raises(native.AccfftError) as e:
         native.PlanC2C((0, 8, 8), "float64")
