@@ -1933,7 +1933,7 @@ int accfft_c_set_pass_order(accfft_c_plan* p, int order) {
   }
   if (order != 1) return fail(ACCFFT_C_EINVAL, "set_pass_order: order must be 0 (natural) or 1 (packed)");
   if (!packed_eligible(p))
-    return fail(ACCFFT_C_EUNSUPPORTED, "set_pass_order: the packed order needs an out-of-place float or double r2c plan");
+    return fail(ACCFFT_C_EUNSUPPORTED, "set_pass_order: the packed order needs an out-of-place float or double r2c plan with compiled lengths");
   p->packed = true;
   return ACCFFT_C_OK;
 }

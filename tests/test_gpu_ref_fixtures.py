@@ -100,13 +100,8 @@ def test_cuda_path_matches_reference(cuda, native, oracle, n, dtype):
     inp = inputs(z, t)
     names = [k.split("__")[2] for k in z.files if k.startswith(f"out__{t}__")]
     assert len(names) >= 50
-    # c2c needs complex-line kernels of every axis length (a z length of 18
-    # exists only as the 9-point half line of an r2c plan)
-    c2c_ok = all(native.lib().accfft_c_length_supported(m) for m in n)
     bad = []
     for case in names:
-        if case.startswith("c2c") and not c2c_ok:
-            continue
         got = run_case(cuda, native, n, dtype, case, inp)
         e = oracle.rel_l2(got, fixture(z, t, case))
         if not e <= TOL[dtype]:
@@ -124,3 +119,29 @@ def test_packed_order_matches_reference(cuda, native, oracle, n, dtype):
     for case in ("r2c_u_7", "r2c_nyq_7", "c2r_7"):
         got = run_case(cuda, native, n, dtype, case, inp, order=1)
         assert oracle.rel_l2(got, fixture(z, t, case)) <= TOL[dtype], case
+
+
+# grids the reference's CPU path runs with an odd N2: every axis of the
+# CUDA path then goes through the generic kernels (z as the full real line)
+ODD_N2_SHAPES = [(7, 5, 9), (3, 11, 7)]
+GENERIC_CASES = ("r2c_", "c2r_", "c2c", "laplace_", "biharmonic_", "inv_laplace_", "inv_biharmonic_")
+
+
+@pytest.mark.parametrize("dtype", ["float64", "float32"])
+@pytest.mark.parametrize("n", ODD_N2_SHAPES)
+def test_odd_n2_grids_match_reference(cuda, native, oracle, n, dtype):
+    """The reference's own results on its odd-N2 grids: the transforms and
+    the 3-D operators (the calls plans with generic-length axes take)."""
+    z = np.load(FIX)
+    t = "x".join(map(str, n))
+    inp = inputs(z, t)
+    names = [k.split("__")[2] for k in z.files if k.startswith(f"out__{t}__")]
+    names = [c for c in names if c.startswith(GENERIC_CASES)]
+    assert len(names) >= 12
+    bad = []
+    for case in names:
+        got = run_case(cuda, native, n, dtype, case, inp)
+        e = oracle.rel_l2(got, fixture(z, t, case))
+        if not e <= TOL[dtype]:
+            bad.append((case, e))
+    assert not bad, bad
