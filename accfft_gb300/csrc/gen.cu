@@ -3,7 +3,7 @@
 // The compiled passes (kernels.cu) fix the line length, radix plan and tile
 // shape at compile time for the lengths of AFG_LENGTHS_*; any other length
 // whose prime factors are at most 31 runs here, from a radix plan chosen at
-// plan creation (gen_factor: radices up to 16, primes 17..31 alone), with
+// plan creation (gen_factor: radices up to 32), with
 // TC lines per CTA held in shared memory and the Stockham stages run
 // between two shared-memory buffers (stage s of radix R reads x[j + r*L/R],
 // multiplies by w_{Ns*R}^{(j%Ns)*r} and writes y[(j/Ns)*Ns*R + j%Ns + r*Ns],
@@ -34,17 +34,20 @@ __device__ __forceinline__ void gen_stage(const typename CT<T>::V* __restrict__ 
                                           int j0, int jstep) {
   typedef typename CT<T>::V V;
   const int nb = L / R;
+  // j / Ns as a high product (exact for j, Ns < 2^16): magic = ceil(2^32 / Ns)
+  const unsigned magic = Ns > 1 ? 0xFFFFFFFFu / unsigned(Ns) + 1u : 0u;
   for (int j = j0; j < nb; j += jstep) {
-    const int k = j % Ns;
+    const int q = Ns > 1 ? int(__umulhi(unsigned(j), magic)) : j;
+    const int k = j - q * Ns;
     V v[R];
 #pragma unroll
     for (int r = 0; r < R; ++r) v[r] = in[(j + r * nb) * tc + c];
 #pragma unroll
     for (int r = 1; r < R; ++r) v[r] = c_mul(v[r], ld_tw(tw + (r - 1) * Ns + k));
     Dft<R, 1>::run(v);
-    const int base = (j / Ns) * Ns * R + k;
+    const int base = q * Ns * R + k;
 #pragma unroll
-    for (int q = 0; q < R; ++q) out[(base + q * Ns) * tc + c] = v[q];
+    for (int o = 0; o < R; ++o) out[(base + o * Ns) * tc + c] = v[o];
   }
 }
 
@@ -63,7 +66,9 @@ __device__ typename CT<T>::V* gen_fft(typename CT<T>::V* a, typename CT<T>::V* b
   case R: gen_stage<T, R>(a, b, t, g.L, Ns, tc, c, j0, jstep); break;
       AFG_GEN_R(2) AFG_GEN_R(3) AFG_GEN_R(4) AFG_GEN_R(5) AFG_GEN_R(6) AFG_GEN_R(7) AFG_GEN_R(8) AFG_GEN_R(9)
       AFG_GEN_R(10) AFG_GEN_R(11) AFG_GEN_R(12) AFG_GEN_R(13) AFG_GEN_R(14) AFG_GEN_R(15) AFG_GEN_R(16)
-      AFG_GEN_R(17) AFG_GEN_R(19) AFG_GEN_R(23) AFG_GEN_R(29) AFG_GEN_R(31)
+      AFG_GEN_R(17) AFG_GEN_R(18) AFG_GEN_R(19) AFG_GEN_R(20) AFG_GEN_R(21) AFG_GEN_R(22) AFG_GEN_R(23)
+      AFG_GEN_R(24) AFG_GEN_R(25) AFG_GEN_R(26) AFG_GEN_R(27) AFG_GEN_R(28) AFG_GEN_R(29) AFG_GEN_R(30)
+      AFG_GEN_R(31) AFG_GEN_R(32)
 #undef AFG_GEN_R
       default: break;   // gen_factor produces no other radix
     }
@@ -173,15 +178,11 @@ template <typename T, typename K>
 bool gen_launch(K kernel, const GenArgs& g, cudaStream_t s) {
   typedef typename CT<T>::V V;
   const size_t smem = 2 * (size_t)g.g.L * g.tc * sizeof(V);
-  static PerDevice prepared;
-  int dev = 0;
-  // the shared-memory opt-in is per kernel and size: set it on every launch
-  // above the default (cheap, and the sizes differ between lengths)
-  if (smem > 48 * 1024 && (cudaGetDevice(&dev) != cudaSuccess ||
-                           cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)) !=
-                               cudaSuccess))
+  // the shared-memory opt-in belongs to the current device and the sizes
+  // differ between lengths: set it on every launch above the default (cheap)
+  if (smem > 48 * 1024 &&
+      cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)) != cudaSuccess)
     return false;
-  (void)prepared;
   GenArgs b = g;
   b.early_trigger = pdl_mode() == 2;
   const long long grid = (g.nlines + g.tc - 1) / g.tc;

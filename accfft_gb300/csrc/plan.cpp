@@ -103,9 +103,10 @@ std::vector<long double> stage_table(int L, int cls, int first_radix = 0) {
 }
 
 // Radix plan of the generic kernels (gen.cu) for a line of L: the prime
-// factors (at most 31) combined greedily into radices of at most 16, primes
-// above 16 alone; false when L has a larger prime factor, exceeds 4096 or
-// needs more than kGenMaxStages stages.  Lengths of one or no stage are fine.
+// factors (at most 31), largest first, each multiplied into the first radix
+// that stays at most 32 (fewer stages: each stage is a shared-memory round
+// trip); false when L has a larger prime factor, exceeds 4096 or needs more
+// than kGenMaxStages stages.  Lengths of one or no stage are fine.
 bool gen_factor(int L, GenPlan* g) {
   if (L < 1 || L > 4096) return false;
   std::vector<int> pf;
@@ -122,9 +123,8 @@ bool gen_factor(int L, GenPlan* g) {
   std::vector<int> rad;
   for (int q : pf) {
     bool merged = false;
-    if (q <= 16)
-      for (int& r : rad)
-        if (r <= 16 && r * q <= 16) {
+    for (int& r : rad)
+      if (r * q <= 32) {
           r *= q;
           merged = true;
           break;
