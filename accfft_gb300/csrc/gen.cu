@@ -89,31 +89,31 @@ __global__ void __launch_bounds__(kGenThreads) k_gen_strided(const GenArgs ga) {
   const int L = ga.g.L, tc = ga.tc;
   V* a = reinterpret_cast<V*>(smraw);
   V* b = a + (size_t)L * tc;
-  const long long g0 = (long long)blockIdx.x * tc;
   const T sg = ga.inverse ? T(-1) : T(1);
-  const V* in = static_cast<const V*>(ga.in);
-  for (int e = threadIdx.x; e < L * tc; e += kGenThreads) {
-    const int p = e / tc, c = e % tc;
-    const long long col = g0 + c;
+  // this thread's column is fixed (the CTA size is a multiple of tc): its
+  // slab and offset are worked out once; it visits rows p0, p0 + pstep, ...
+  const int c = threadIdx.x % tc, p0 = threadIdx.x / tc, pstep = kGenThreads / tc;
+  const long long col = (long long)blockIdx.x * tc + c;
+  const bool valid = col < ga.nlines;
+  const long long slab = valid ? col / ga.cps : 0;
+  const long long cc = valid ? col - slab * ga.cps : 0;
+  const V* in = static_cast<const V*>(ga.in) + slab * ga.in_slab + cc;
+  for (int p = p0; p < L; p += pstep) {
     V x = c_make<V>(T(0), T(0));
-    if (col < ga.nlines) {
-      const long long slab = col / ga.cps;
-      x = in[slab * ga.in_slab + (col - slab * ga.cps) + (long long)p * ga.in_line];
+    if (valid) {
+      x = in[(long long)p * ga.in_line];
       x.y *= sg;
     }
-    a[e] = x;
+    a[p * tc + c] = x;
   }
   __syncthreads();
   const V* res = gen_fft<T>(a, b, ga.g, tc);
-  V* out = static_cast<V*>(ga.out);
-  for (int e = threadIdx.x; e < L * tc; e += kGenThreads) {
-    const int p = e / tc, c = e % tc;
-    const long long col = g0 + c;
-    if (col < ga.nlines) {
-      const long long slab = col / ga.cps;
-      V x = res[e];
+  V* out = static_cast<V*>(ga.out) + slab * ga.out_slab + cc;
+  if (valid) {
+    for (int p = p0; p < L; p += pstep) {
+      V x = res[p * tc + c];
       x.y *= sg;
-      out[slab * ga.out_slab + (col - slab * ga.cps) + (long long)p * ga.out_line] = x;
+      out[(long long)p * ga.out_line] = x;
     }
   }
 }
@@ -130,8 +130,8 @@ __global__ void __launch_bounds__(kGenThreads) k_gen_contig(const GenArgs ga) {
   const long long l0 = (long long)blockIdx.x * tc;
   const T sg = ga.inverse ? T(-1) : T(1);
   // load: entry p of line c (consecutive threads along p)
-  for (int e = threadIdx.x; e < L * tc; e += kGenThreads) {
-    const int c = e / L, p = e % L;
+  for (int c = 0; c < tc; ++c)
+  for (int p = threadIdx.x; p < L; p += kGenThreads) {
     const long long l = l0 + c;
     V x = c_make<V>(T(0), T(0));
     if (l < ga.nlines) {
@@ -158,8 +158,8 @@ __global__ void __launch_bounds__(kGenThreads) k_gen_contig(const GenArgs ga) {
   }
   __syncthreads();
   const V* res = gen_fft<T>(a, b, ga.g, tc);
-  for (int e = threadIdx.x; e < L * tc; e += kGenThreads) {
-    const int c = e / L, p = e % L;
+  for (int c = 0; c < tc; ++c)
+  for (int p = threadIdx.x; p < L; p += kGenThreads) {
     const long long l = l0 + c;
     if (l >= ga.nlines) continue;
     V x = res[p * tc + c];
