@@ -11,12 +11,12 @@
 // engine).  These kernels make every such grid run; they are not tuned.
 //
 // Four kernels:
-//   k_gen_strided  c2c along strided lines (y and x passes)
-//   k_gen_c2c      c2c along contiguous lines (z pass of c2c plans)
-//   k_gen_r2c      real lines of L -> L/2+1 complex (z pass of r2c plans,
-//                  odd L included: the real line as a complex line)
-//   k_gen_c2r      L/2+1 complex -> real lines of L (the Hermitian
-//                  completion, imaginary parts of kz = 0 and L/2 dropped)
+//   k_gen_strided      c2c along strided lines (y and x passes)
+//   k_gen_contig<0>    c2c along contiguous lines (z pass of c2c plans)
+//   k_gen_contig<1>    real lines of L -> L/2+1 complex (z pass of r2c plans,
+//                      odd L included: the real line as a complex line)
+//   k_gen_contig<2>    L/2+1 complex -> real lines of L (the Hermitian
+//                      completion, imaginary parts of kz = 0 and L/2 dropped)
 // Inverse transforms conjugate on the way in and out.
 #include "launch.h"
 #include "passes.cuh"
@@ -28,10 +28,14 @@ namespace {
 
 constexpr int kGenThreads = 256;
 
+// entry p of line c of a shared-memory buffer sits at p*ps + c*cs: strided
+// passes interleave the lines (ps = lines per CTA, cs = 1: the global loads
+// run along the lines' common rows), contiguous passes keep them apart
+// (ps = 1, cs = L: the global loads and the stages run along a line)
 template <typename T, int R>
 __device__ __forceinline__ void gen_stage(const typename CT<T>::V* __restrict__ in, typename CT<T>::V* __restrict__ out,
-                                          const typename CT<T>::V* __restrict__ tw, int L, int Ns, int tc, int c,
-                                          int j0, int jstep) {
+                                          const typename CT<T>::V* __restrict__ tw, int L, int Ns, int ps, int cs,
+                                          int c, int j0, int jstep) {
   typedef typename CT<T>::V V;
   const int nb = L / R;
   // j / Ns as a high product (exact for j, Ns < 2^16): magic = ceil(2^32 / Ns)
@@ -41,29 +45,36 @@ __device__ __forceinline__ void gen_stage(const typename CT<T>::V* __restrict__ 
     const int k = j - q * Ns;
     V v[R];
 #pragma unroll
-    for (int r = 0; r < R; ++r) v[r] = in[(j + r * nb) * tc + c];
+    for (int r = 0; r < R; ++r) v[r] = in[(j + r * nb) * ps + c * cs];
 #pragma unroll
     for (int r = 1; r < R; ++r) v[r] = c_mul(v[r], ld_tw(tw + (r - 1) * Ns + k));
     Dft<R, 1>::run(v);
     const int base = q * Ns * R + k;
 #pragma unroll
-    for (int o = 0; o < R; ++o) out[(base + o * Ns) * tc + c] = v[o];
+    for (int o = 0; o < R; ++o) out[(base + o * Ns) * ps + c * cs] = v[o];
   }
 }
 
-// every stage over the CTA's tc lines, buffer a holding entry p of line c at
-// p*tc + c; returns the buffer holding the result
+// every stage over the CTA's tc lines (layout as gen_stage; interleaved:
+// lines interleaved, thread c = tid % tc; else lines apart, consecutive
+// threads on consecutive butterflies of one line); returns the buffer
+// holding the result
 template <typename T>
-__device__ typename CT<T>::V* gen_fft(typename CT<T>::V* a, typename CT<T>::V* b, const GenPlan& g, int tc) {
+__device__ typename CT<T>::V* gen_fft(typename CT<T>::V* a, typename CT<T>::V* b, const GenPlan& g, int tc,
+                                      bool interleaved) {
   typedef typename CT<T>::V V;
-  const int c = threadIdx.x % tc, j0 = threadIdx.x / tc, jstep = kGenThreads / tc;
+  const int per = kGenThreads / tc;   // threads per line
+  const int c = interleaved ? threadIdx.x % tc : threadIdx.x / per;
+  const int j0 = interleaved ? threadIdx.x / tc : threadIdx.x % per;
+  const int jstep = per;
+  const int ps = interleaved ? tc : 1, cs = interleaved ? 1 : g.L;
   const V* tw = static_cast<const V*>(g.tw);
   int Ns = 1;
   for (int s = 0; s < g.nst; ++s) {
     const V* t = tw + g.off[s];
     switch (g.radix[s]) {
 #define AFG_GEN_R(R) \
-  case R: gen_stage<T, R>(a, b, t, g.L, Ns, tc, c, j0, jstep); break;
+  case R: gen_stage<T, R>(a, b, t, g.L, Ns, ps, cs, c, j0, jstep); break;
       AFG_GEN_R(2) AFG_GEN_R(3) AFG_GEN_R(4) AFG_GEN_R(5) AFG_GEN_R(6) AFG_GEN_R(7) AFG_GEN_R(8) AFG_GEN_R(9)
       AFG_GEN_R(10) AFG_GEN_R(11) AFG_GEN_R(12) AFG_GEN_R(13) AFG_GEN_R(14) AFG_GEN_R(15) AFG_GEN_R(16)
       AFG_GEN_R(17) AFG_GEN_R(18) AFG_GEN_R(19) AFG_GEN_R(20) AFG_GEN_R(21) AFG_GEN_R(22) AFG_GEN_R(23)
@@ -107,7 +118,7 @@ __global__ void __launch_bounds__(kGenThreads) k_gen_strided(const GenArgs ga) {
     a[p * tc + c] = x;
   }
   __syncthreads();
-  const V* res = gen_fft<T>(a, b, ga.g, tc);
+  const V* res = gen_fft<T>(a, b, ga.g, tc, true);
   V* out = static_cast<V*>(ga.out) + slab * ga.out_slab + cc;
   if (valid) {
     for (int p = p0; p < L; p += pstep) {
@@ -129,9 +140,13 @@ __global__ void __launch_bounds__(kGenThreads) k_gen_contig(const GenArgs ga) {
   V* b = a + (size_t)L * tc;
   const long long l0 = (long long)blockIdx.x * tc;
   const T sg = ga.inverse ? T(-1) : T(1);
-  // load: entry p of line c (consecutive threads along p)
-  for (int c = 0; c < tc; ++c)
-  for (int p = threadIdx.x; p < L; p += kGenThreads) {
+  // entry e = c*L + p of the CTA's lines: line c, position p (c = e / L as a
+  // high product, exact for e < 2^16: L*tc is at most 6144; L = 1 is the
+  // real z axis of N2 = 1)
+  const unsigned magic = L > 1 ? 0xFFFFFFFFu / unsigned(L) + 1u : 0u;
+  // load, consecutive threads along p
+  for (int e = threadIdx.x; e < L * tc; e += kGenThreads) {
+    const int c = L > 1 ? int(__umulhi(unsigned(e), magic)) : e, p = e - c * L;
     const long long l = l0 + c;
     V x = c_make<V>(T(0), T(0));
     if (l < ga.nlines) {
@@ -154,15 +169,15 @@ __global__ void __launch_bounds__(kGenThreads) k_gen_contig(const GenArgs ga) {
         x.y = -x.y;
       }
     }
-    a[p * tc + c] = x;
+    a[e] = x;
   }
   __syncthreads();
-  const V* res = gen_fft<T>(a, b, ga.g, tc);
-  for (int c = 0; c < tc; ++c)
-  for (int p = threadIdx.x; p < L; p += kGenThreads) {
+  const V* res = gen_fft<T>(a, b, ga.g, tc, false);
+  for (int e = threadIdx.x; e < L * tc; e += kGenThreads) {
+    const int c = L > 1 ? int(__umulhi(unsigned(e), magic)) : e, p = e - c * L;
     const long long l = l0 + c;
     if (l >= ga.nlines) continue;
-    V x = res[p * tc + c];
+    V x = res[e];
     if constexpr (MODE == 0) {
       x.y *= sg;
       static_cast<V*>(ga.out)[l * ga.out_dist + p] = x;

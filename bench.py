@@ -160,6 +160,18 @@ KERNEL_OF = {"z_r2c": "k_zr2c", "y": "k_strided (y)", "x": "k_strided (x)", "x_i
              "zy_slab": "k_slab_fwd (z+y, cluster)", "yz_slab": "k_slab_inv (y+z, cluster)"}
 
 
+def kernel_of(lib, dom, n):
+    """Kernel of pass `dom` on grid n: axes without compiled kernels run the
+    generic ones (the real z axis when N2 is odd or N2/2 is not compiled)."""
+    axis = {"x": 0, "x_inv": 0, "y": 1, "y_inv": 1, "z_r2c": 2, "z_c2r": 2}.get(dom)
+    if axis is not None:
+        compiled = (n[2] % 2 == 0 and lib.accfft_c_length_supported(n[2] // 2)) if axis == 2 \
+            else lib.accfft_c_length_supported(n[axis])
+        if not compiled:
+            return ("k_gen_contig" if axis == 2 else "k_gen_strided") + f" ({dom})"
+    return KERNEL_OF.get(dom, dom)
+
+
 class Clocks:
     """nvidia-smi sampling during the timed region."""
 
@@ -711,7 +723,7 @@ def ours(args):
         "gpu_launches": int(launches),
         "pdl_mode": ag.set_pdl(None),
         "profiled_ms_per_step": prof_total_ms / args.steps,
-        "roofline": {"bound": "hbm", "kernel": KERNEL_OF.get(dom, dom), "pass": dom, "achieved": achieved,
+        "roofline": {"bound": "hbm", "kernel": kernel_of(ag.lib(), dom, n), "pass": dom, "achieved": achieved,
                      "peak": peak, "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": TRAFFIC.get((n, dt, args.order), {}).get(dom), "bytes_per_launch": dom_bytes,
                      "ms_per_launch": per[dom]},

@@ -13,7 +13,7 @@ pytestmark = pytest.mark.gpu
 
 # every grid has at least one axis outside the compiled lengths
 R2C_GRIDS = [(7, 11, 13), (36, 30, 14), (64, 18, 96), (27, 64, 50), (14, 49, 62), (121, 6, 20), (2048, 3, 6),
-             (5, 9, 7), (12, 8, 2048)]
+             (5, 9, 7), (12, 8, 2048), (6, 7, 1)]
 C2C_GRIDS = [(7, 11, 13), (36, 30, 14), (64, 18, 96), (4, 20, 18), (13, 1, 31)]
 
 
