@@ -14,9 +14,10 @@
 //   k_gen_strided      c2c along strided lines (y and x passes)
 //   k_gen_contig<0>    c2c along contiguous lines (z pass of c2c plans)
 //   k_gen_contig<1>    real lines of L -> L/2+1 complex (z pass of r2c plans,
-//                      odd L included: the real line as a complex line)
+//                      odd L included: two real lines as one complex line)
 //   k_gen_contig<2>    L/2+1 complex -> real lines of L (the Hermitian
-//                      completion, imaginary parts of kz = 0 and L/2 dropped)
+//                      completion, imaginary parts of kz = 0 and L/2 dropped;
+//                      two lines per complex line)
 // Inverse transforms conjugate on the way in and out.
 #include "launch.h"
 #include "passes.cuh"
@@ -27,6 +28,10 @@ namespace afg {
 namespace {
 
 constexpr int kGenThreads = 256;
+// global loads a thread issues before it stores any of them to shared
+// memory: a loop of runtime length that stored each value as it arrived
+// would wait out one memory latency per entry
+constexpr int kGenBatch = 8;
 
 // entry p of line c of a shared-memory buffer sits at p*ps + c*cs: strided
 // passes interleave the lines (ps = lines per CTA, cs = 1: the global loads
@@ -109,13 +114,20 @@ __global__ void __launch_bounds__(kGenThreads) k_gen_strided(const GenArgs ga) {
   const long long slab = valid ? col / ga.cps : 0;
   const long long cc = valid ? col - slab * ga.cps : 0;
   const V* in = static_cast<const V*>(ga.in) + slab * ga.in_slab + cc;
-  for (int p = p0; p < L; p += pstep) {
-    V x = c_make<V>(T(0), T(0));
-    if (valid) {
-      x = in[(long long)p * ga.in_line];
-      x.y *= sg;
+  for (int p = p0; p < L; p += kGenBatch * pstep) {
+    V x[kGenBatch];
+#pragma unroll
+    for (int u = 0; u < kGenBatch; ++u) {
+      const int q = p + u * pstep;
+      x[u] = c_make<V>(T(0), T(0));
+      if (valid && q < L) x[u] = in[(long long)q * ga.in_line];
     }
-    a[p * tc + c] = x;
+#pragma unroll
+    for (int u = 0; u < kGenBatch; ++u) {
+      const int q = p + u * pstep;
+      x[u].y *= sg;
+      if (q < L) a[q * tc + c] = x[u];
+    }
   }
   __syncthreads();
   const V* res = gen_fft<T>(a, b, ga.g, tc, true);
@@ -129,68 +141,113 @@ __global__ void __launch_bounds__(kGenThreads) k_gen_strided(const GenArgs ga) {
   }
 }
 
-// contiguous lines: MODE 0 c2c, 1 r2c, 2 c2r
+// contiguous lines: MODE 0 c2c; MODE 1 r2c and MODE 2 c2r hold two real
+// lines in each complex slot (line 2c as the real part, 2c+1 as the
+// imaginary part: half the line transforms), so a CTA of tc slots covers
+// 2*tc real lines
 template <typename T, int MODE>
 __global__ void __launch_bounds__(kGenThreads) k_gen_contig(const GenArgs ga) {
   typedef typename CT<T>::V V;
   PassScope scope(ga.early_trigger);
   extern __shared__ __align__(16) unsigned char smraw[];
-  const int L = ga.g.L, tc = ga.tc, H = L / 2 + 1;
+  constexpr int LPS = MODE == 0 ? 1 : 2;   // lines per slot
+  const int L = ga.g.L, tc = ga.tc, H = L / 2 + 1, n = L * tc;
   V* a = reinterpret_cast<V*>(smraw);
-  V* b = a + (size_t)L * tc;
-  const long long l0 = (long long)blockIdx.x * tc;
+  V* b = a + (size_t)n;
+  const long long l0 = (long long)blockIdx.x * tc * LPS;
+  const long long d = ga.in_dist;
   const T sg = ga.inverse ? T(-1) : T(1);
-  // entry e = c*L + p of the CTA's lines: line c, position p (c = e / L as a
-  // high product, exact for e < 2^16: L*tc is at most 6144; L = 1 is the
-  // real z axis of N2 = 1)
+  // entry e = c*L + p of the slots: slot c, position p (c = e / L as a high
+  // product, exact for e < 2^16: L*tc is at most 6144; L = 1 is the real z
+  // axis of N2 = 1)
   const unsigned magic = L > 1 ? 0xFFFFFFFFu / unsigned(L) + 1u : 0u;
-  // load, consecutive threads along p
-  for (int e = threadIdx.x; e < L * tc; e += kGenThreads) {
-    const int c = L > 1 ? int(__umulhi(unsigned(e), magic)) : e, p = e - c * L;
-    const long long l = l0 + c;
-    V x = c_make<V>(T(0), T(0));
-    if (l < ga.nlines) {
+  // load, consecutive threads along p, kGenBatch entries (of each line) in
+  // flight a thread
+  for (int e0 = threadIdx.x; e0 < n; e0 += kGenBatch * kGenThreads) {
+    V x0[kGenBatch], x1[kGenBatch];
+#pragma unroll
+    for (int u = 0; u < kGenBatch; ++u) {
+      const int e = e0 + u * kGenThreads;
+      const int c = L > 1 ? int(__umulhi(unsigned(e), magic)) : e, p = e - c * L;
+      const long long l = l0 + (long long)c * LPS;
+      x0[u] = x1[u] = c_make<V>(T(0), T(0));
+      if (e >= n) continue;
       if constexpr (MODE == 0) {
-        x = static_cast<const V*>(ga.in)[l * ga.in_dist + p];
-        x.y *= sg;
+        if (l < ga.nlines) x0[u] = static_cast<const V*>(ga.in)[l * d + p];
       } else if constexpr (MODE == 1) {
-        x.x = static_cast<const T*>(ga.in)[l * ga.in_dist + p];
+        const T* r = static_cast<const T*>(ga.in) + l * d + p;
+        if (l < ga.nlines) x0[u].x = r[0];
+        if (l + 1 < ga.nlines) x1[u].x = r[d];
       } else {
-        // the full spectrum from the half one (Hermitian completion), then
-        // conjugated for the forward engine
-        const V* h = static_cast<const V*>(ga.in) + l * ga.in_dist;
-        if (p < H) {
-          x = h[p];
-          if (p == 0 || 2 * p == L) x.y = T(0);
-        } else {
-          x = h[L - p];
-          x.y = -x.y;
-        }
-        x.y = -x.y;
+        // entry p of each line's full spectrum comes from its half at
+        // min(p, L - p) (the Hermitian completion, below)
+        const V* h = static_cast<const V*>(ga.in) + l * d + (p < H ? p : L - p);
+        if (l < ga.nlines) x0[u] = h[0];
+        if (l + 1 < ga.nlines) x1[u] = h[d];
       }
     }
-    a[e] = x;
+#pragma unroll
+    for (int u = 0; u < kGenBatch; ++u) {
+      const int e = e0 + u * kGenThreads;
+      if (e >= n) break;
+      V x = x0[u];
+      if constexpr (MODE == 0) {
+        x.y *= sg;
+      } else if constexpr (MODE == 1) {
+        x.y = x1[u].x;
+      } else {
+        // spectra A (line 2c) and B (line 2c+1): imaginary parts of DC and
+        // Nyquist dropped, the mirrored half conjugated; the slot holds
+        // conj(A + iB) for the forward engine
+        const int c = L > 1 ? int(__umulhi(unsigned(e), magic)) : e, p = e - c * L;
+        V A = x0[u], B = x1[u];
+        if (p == 0 || 2 * p == L) A.y = B.y = T(0);
+        if (p >= H) {
+          A.y = -A.y;
+          B.y = -B.y;
+        }
+        x = c_make<V>(A.x - B.y, -(A.y + B.x));
+      }
+      a[e] = x;
+    }
   }
   __syncthreads();
   const V* res = gen_fft<T>(a, b, ga.g, tc, false);
-  for (int e = threadIdx.x; e < L * tc; e += kGenThreads) {
-    const int c = L > 1 ? int(__umulhi(unsigned(e), magic)) : e, p = e - c * L;
-    const long long l = l0 + c;
-    if (l >= ga.nlines) continue;
-    V x = res[e];
-    if constexpr (MODE == 0) {
-      x.y *= sg;
-      static_cast<V*>(ga.out)[l * ga.out_dist + p] = x;
-    } else if constexpr (MODE == 1) {
-      if (p < H) static_cast<V*>(ga.out)[l * ga.out_dist + p] = x;
-    } else {
-      static_cast<T*>(ga.out)[l * ga.out_dist + p] = x.x;   // real part of the conjugated result
+  const long long od = ga.out_dist;
+  if constexpr (MODE == 1) {
+    // X = A + iB: A[k] = (X[k] + conj X[L-k]) / 2, B[k] = (X[k] - conj X[L-k]) / 2i
+    const unsigned mh = H > 1 ? 0xFFFFFFFFu / unsigned(H) + 1u : 0u;
+    for (int e = threadIdx.x; e < H * tc; e += kGenThreads) {
+      const int c = H > 1 ? int(__umulhi(unsigned(e), mh)) : e, k = e - c * H;
+      const long long l = l0 + 2LL * c;
+      if (l >= ga.nlines) continue;
+      const V X = res[c * L + k], Y = res[c * L + (k == 0 ? 0 : L - k)];
+      V* o = static_cast<V*>(ga.out) + l * od + k;
+      o[0] = c_make<V>(T(0.5) * (X.x + Y.x), T(0.5) * (X.y - Y.y));
+      if (l + 1 < ga.nlines) o[od] = c_make<V>(T(0.5) * (X.y + Y.y), T(-0.5) * (X.x - Y.x));
+    }
+  } else {
+    for (int e = threadIdx.x; e < n; e += kGenThreads) {
+      const int c = L > 1 ? int(__umulhi(unsigned(e), magic)) : e, p = e - c * L;
+      const long long l = l0 + (long long)c * LPS;
+      if (l >= ga.nlines) continue;
+      V x = res[e];
+      if constexpr (MODE == 0) {
+        x.y *= sg;
+        static_cast<V*>(ga.out)[l * od + p] = x;
+      } else {
+        // the forward engine gave conj(a + ib): line 2c is a, line 2c+1 is b
+        T* o = static_cast<T*>(ga.out) + l * od + p;
+        o[0] = x.x;
+        if (l + 1 < ga.nlines) o[od] = -x.y;
+      }
     }
   }
 }
 
+// lines_per_slot: 2 for the paired real kernels
 template <typename T, typename K>
-bool gen_launch(K kernel, const GenArgs& g, cudaStream_t s) {
+bool gen_launch(K kernel, const GenArgs& g, cudaStream_t s, int lines_per_slot = 1) {
   typedef typename CT<T>::V V;
   const size_t smem = 2 * (size_t)g.g.L * g.tc * sizeof(V);
   // the shared-memory opt-in belongs to the current device and the sizes
@@ -200,7 +257,8 @@ bool gen_launch(K kernel, const GenArgs& g, cudaStream_t s) {
     return false;
   GenArgs b = g;
   b.early_trigger = pdl_mode() == 2;
-  const long long grid = (g.nlines + g.tc - 1) / g.tc;
+  const long long per = (long long)g.tc * lines_per_slot;
+  const long long grid = (g.nlines + per - 1) / per;
   return launch_pass(kernel, unsigned(grid), kGenThreads, smem, s, b) == cudaSuccess;
 }
 
@@ -221,15 +279,15 @@ bool launch_gen(int prec, int mode, const GenArgs& g, cudaStream_t s) {
     switch (mode) {
       case 0: return gen_launch<float>(k_gen_strided<float>, g, s);
       case 1: return gen_launch<float>(k_gen_contig<float, 0>, g, s);
-      case 2: return gen_launch<float>(k_gen_contig<float, 1>, g, s);
-      case 3: return gen_launch<float>(k_gen_contig<float, 2>, g, s);
+      case 2: return gen_launch<float>(k_gen_contig<float, 1>, g, s, 2);
+      case 3: return gen_launch<float>(k_gen_contig<float, 2>, g, s, 2);
     }
   } else if (prec == PREC_F64) {
     switch (mode) {
       case 0: return gen_launch<double>(k_gen_strided<double>, g, s);
       case 1: return gen_launch<double>(k_gen_contig<double, 0>, g, s);
-      case 2: return gen_launch<double>(k_gen_contig<double, 1>, g, s);
-      case 3: return gen_launch<double>(k_gen_contig<double, 2>, g, s);
+      case 2: return gen_launch<double>(k_gen_contig<double, 1>, g, s, 2);
+      case 3: return gen_launch<double>(k_gen_contig<double, 2>, g, s, 2);
     }
   }
   return false;
