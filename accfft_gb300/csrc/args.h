@@ -64,6 +64,8 @@ struct StridedArgs {
   unsigned wait_limit;
   // radix / tile variant of a float MODE 0 pass (variants.cu; 0 = default)
   int variant;
+  // set to 1 when a bounded wait of the pass gave up (variant 4)
+  int* wait_err;
 };
 
 struct ContigArgs {

@@ -100,7 +100,7 @@ bool launch_add_rows(bool dbl, void* out, long long out_row, const void* in, lon
 bool launch_strided_variant_f32(int L, int v, const StridedArgs& a, cudaStream_t s);
 bool launch_contig_variant_f32(bool r2c, int M, int v, const ContigArgs& a, cudaStream_t s);
 void variant_shape(int kind, int L, int v, int* E, int* tile);
-constexpr int kMaxVariant = 3;
+constexpr int kMaxVariant = 4;
 // spec[n0][cols] (complex, float or double) *= the symbol of s at
 // (x, column), for the operators that run as r2c, symbol, c2r
 // (sym_spectrum.cu)

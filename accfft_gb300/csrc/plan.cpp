@@ -583,7 +583,8 @@ int take_wait_error(accfft_c_plan* p, const char* fn) {
               "%s: a device-side wait gave up (%s) in this call or an earlier asynchronous call of the plan; "
               "its results are not valid",
               fn, p->tc ? "a tensor-core stage waiting for its matrix products"
-                        : "the persistent z+y kernel waiting for another item");
+                        : "the persistent z+y kernel waiting for another item, or a pipelined strided pass "
+                          "waiting for its tile loads");
 }
 
 struct Exec {
@@ -697,7 +698,8 @@ struct Exec {
     a.wait_limit = g_wait_limit.load();
     if (!p->tc && !p->recording) a.variant = tw == p->tw_x ? p->var_x : p->var_y;
     if (a.variant == 2) a.tw = tw == p->tw_x ? p->tw_x_alt : p->tw_y_alt;
-    if (p->tc) p->waits_used = true;
+    a.wait_err = p->wait_err;
+    if (p->tc || a.variant == 4) p->waits_used = true;
     if (!timed(tw == p->tw_x ? (inverse ? "x_inv" : "x") : (inverse ? "y_inv" : "y"), p->stream, [&] {
           return p->tc ? launch_strided_tc(p->tc, L, a, p->wait_err, p->stream) : go_strided(L, 0, a, p->stream);
         }))

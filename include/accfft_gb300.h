@@ -173,7 +173,10 @@ int accfft_c_set_pass_order(accfft_c_plan* plan, int order);
  * variants of its y, x, z r2c and z c2r passes on the plan's scratch and a
  * temporary spectrum (variant 0 = default; 1 = half the columns or the other
  * line count per CTA; 2 = the next smaller first radix; 3 = for y and x,
- * the default tile with 16-byte loads and stores) and keeps the
+ * the default tile with 16-byte loads and stores; 4 = for y and x of 512
+ * and 1024, one persistent CTA a SM with three column tiles in flight
+ * through tensor copies, its waits bounded and reported like the
+ * tensor-core ones, see accfft_c_check) and keeps the
  * fastest; the choice is cached per process by grid and pass order, so plans
  * of one grid run the same kernels.  ACCFFT_ESTIMATE keeps the defaults.
  * accfft_c_plan_tuning reports, for y, x, z r2c and z c2r, the variant, its

@@ -26,7 +26,7 @@ def test_every_variant_matches_oracle(cuda, native, oracle, n, order):
     back = empty(torch, n, "float32")
     tried = 0
     for w in range(4):
-        for v in (1, 2, 3):
+        for v in (1, 2, 3, 4):
             vs = [0, 0, 0, 0]
             vs[w] = v
             try:
@@ -49,7 +49,7 @@ def test_measure_tunes_and_caches(cuda, native, oracle):
     t1 = p1.tuning()
     assert t1["tuned"]
     for k in ("y", "x", "z_r2c", "z_c2r"):
-        assert t1[k]["radix"] > 0 and t1[k]["tile"] > 0 and t1[k]["variant"] in (0, 1, 2, 3)
+        assert t1[k]["radix"] > 0 and t1[k]["tile"] > 0 and t1[k]["variant"] in (0, 1, 2, 3, 4)
     p2 = native.PlanR2C(n, "float32", flags=native.ACCFFT_MEASURE)
     assert p2.tuning() == t1                 # one choice per grid in a process
     est = native.PlanR2C(n, "float32")       # ACCFFT_ESTIMATE: the defaults

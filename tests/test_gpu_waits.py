@@ -80,3 +80,30 @@ def test_nonblocking_call_reports_through_check(cuda, native, zero_wait_limit):
     native.set_wait_limit(None)
     plan.r2c(u, out)
     plan.check()
+
+
+def test_pipelined_strided_wait_reports(cuda, native, zero_wait_limit):
+    """The x pass of 1024 in variant 4 waits for its tensor-copy tile loads.
+    With one poll a wait may give up (the call returns ACCFFT_C_ECUDA after
+    the kernel let its issued copies land) or, if a load was already in, the
+    pass completes; a wrong result is never returned as a success."""
+    torch = cuda
+    n = (1024, 64, 512)
+    u = torch.randn(n, device="cuda")
+    ref = native.PlanR2C(n, "float32")
+    a = torch.empty(half(n), device="cuda")
+    plan = native.PlanR2C(n, "float32")
+    plan.set_variants(0, 4, 0, 0)
+    out = torch.empty(half(n), device="cuda")
+    try:
+        plan.r2c(u, out)
+        gave_up = False
+    except native.AccfftError as e:
+        assert e.code == native.ECUDA and "gave up" in str(e)
+        gave_up = True
+    native.set_wait_limit(None)
+    ref.r2c(u, a)
+    if not gave_up:
+        assert ((out - a).norm() / a.norm()).item() < 1e-6
+    plan.r2c(u, out)                      # the default limit: the pass completes
+    assert ((out - a).norm() / a.norm()).item() < 1e-6
