@@ -170,9 +170,10 @@ __device__ __forceinline__ bool pipe_try(uint32_t bar, uint32_t parity) {
       : "memory");
   return done != 0;
 }
-// bounded wait on phase `parity` of mbarrier `bar` (every thread polls)
+// wait on phase `parity` of mbarrier `bar`, at most `limit` polls (every
+// thread polls; a limit of 0 gives up at once)
 __device__ __forceinline__ bool pipe_wait(uint32_t bar, uint32_t parity, unsigned limit) {
-  for (unsigned k = 0; k <= limit; ++k)
+  for (unsigned k = 0; k < limit; ++k)
     if (pipe_try(bar, parity)) return true;
   return false;
 }
