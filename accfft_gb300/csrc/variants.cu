@@ -309,7 +309,9 @@ bool run_strided_pipe(const StridedArgs& a, cudaStream_t s) {
   if (grid < 1) return false;
   StridedArgs b = a;
   b.early_trigger = pdl_mode() == 2;
-  return launch_pass(k, unsigned(grid), SH::threads, SH::smem, s, tm, b) == cudaSuccess;
+  if (launch_pass(k, unsigned(grid), SH::threads, SH::smem, s, tm, b) == cudaSuccess) return true;
+  cudaGetLastError();   // a refused launch: the default kernel runs instead and reports its own errors
+  return false;
 }
 
 template <int L>
