@@ -105,28 +105,40 @@ def c2c_axis(data: np.ndarray, axis: int, sign: int, prec="d", nthreads=0) -> np
 
 def _c2c_axis_inplace(d: np.ndarray, axis: int, sign: int, prec="d", nthreads=0) -> np.ndarray:
     """c2c_axis on an array the caller owns (C-contiguous complex128), in place."""
+    assert d.dtype == np.complex128 and d.flags.c_contiguous and d.ndim == 3
     n0, n1, w = d.shape
     _check(lib().orc_c2c_axis(n0, n1, w, axis, _dp(d), sign, _prec(prec), _threads(nthreads)), "c2c_axis")
     return d
 
 
-def r2c_z(u: np.ndarray, prec="d", nthreads=0) -> np.ndarray:
+c2c_axis_inplace = _c2c_axis_inplace
+
+
+def _out(out, shape, dtype):
+    """`out` when given (C-contiguous, of the shape and type), else a new array."""
+    if out is None:
+        return np.empty(shape, dtype)
+    assert out.shape == shape and out.dtype == dtype and out.flags.c_contiguous
+    return out
+
+
+def r2c_z(u: np.ndarray, prec="d", nthreads=0, out=None) -> np.ndarray:
     """z pass of r2c: [..][N2] real -> [..][N2/2+1] complex (src/accfft_gpu.cpp:170-206)."""
     u = np.ascontiguousarray(u, dtype=np.float64)
     n2 = u.shape[-1]
     rows = u.size // n2
-    out = np.empty(u.shape[:-1] + (n2 // 2 + 1,), np.complex128)
+    out = _out(out, u.shape[:-1] + (n2 // 2 + 1,), np.complex128)
     _check(lib().orc_r2c_z(rows, n2, _dp(u), n2, _dp(out), n2 // 2 + 1, _prec(prec), _threads(nthreads)), "r2c_z")
     return out
 
 
-def c2r_z(s: np.ndarray, n2: int, prec="d", nthreads=0) -> np.ndarray:
+def c2r_z(s: np.ndarray, n2: int, prec="d", nthreads=0, out=None) -> np.ndarray:
     """z pass of c2r: [..][N2/2+1] complex -> [..][N2] real, DC/Nyquist imaginary parts ignored."""
     s = np.ascontiguousarray(s, dtype=np.complex128)
     h = s.shape[-1]
     assert h == n2 // 2 + 1
     rows = s.size // h
-    out = np.empty(s.shape[:-1] + (n2,), np.float64)
+    out = _out(out, s.shape[:-1] + (n2,), np.float64)
     _check(lib().orc_c2r_z(rows, n2, _dp(s), h, _dp(out), n2, _prec(prec), _threads(nthreads)), "c2r_z")
     return out
 

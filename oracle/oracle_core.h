@@ -67,9 +67,18 @@ static inline SFX(cpx) SFX(wexp)(const SFX(cpx) * w, long long N, long long e, i
   if (sign > 0) t.im = -t.im;
   return t;
 }
+/* the same for 0 <= e < N (no reduction) */
+static inline SFX(cpx) SFX(wexp_in)(const SFX(cpx) * w, long long e, int sign) {
+  SFX(cpx) t = w[e];
+  if (sign > 0) t.im = -t.im;
+  return t;
+}
 
 /* Recursive decimation in time.  Sub-transform of length n reads in[j*is]
- * for j < n; w is the table of the top-level length N and wstep = N/n. */
+ * for j < n; w is the table of the top-level length N and wstep = N/n.
+ * The twiddle exponent q*k*wstep stays below p*m*wstep = N.  A last factor
+ * (m == 1) reads its inputs directly: its length-1 sub-transforms are
+ * copies and its twiddles are w^0 = 1. */
 static void SFX(rec)(const SFX(cpx) * in, long long is, SFX(cpx) * out, int n, const int* fac, const SFX(cpx) * w,
                      long long N, long long wstep, int sign, SFX(cpx) * tmp) {
   if (n == 1) {
@@ -77,9 +86,13 @@ static void SFX(rec)(const SFX(cpx) * in, long long is, SFX(cpx) * out, int n, c
     return;
   }
   const int p = fac[0], m = n / p;
-  for (int q = 0; q < p; ++q) SFX(rec)(in + q * is, is * p, out + q * m, m, fac + 1, w, N, wstep * p, sign, tmp);
+  if (m > 1)
+    for (int q = 0; q < p; ++q) SFX(rec)(in + q * is, is * p, out + q * m, m, fac + 1, w, N, wstep * p, sign, tmp);
   for (int k = 0; k < m; ++k) {
-    for (int q = 0; q < p; ++q) tmp[q] = SFX(cmul)(out[q * m + k], SFX(wexp)(w, N, (long long)q * k * wstep, sign));
+    if (m == 1)
+      for (int q = 0; q < p; ++q) tmp[q] = in[q * is];
+    else
+      for (int q = 0; q < p; ++q) tmp[q] = SFX(cmul)(out[q * m + k], SFX(wexp_in)(w, (long long)q * k * wstep, sign));
     if (p == 2) {
       SFX(cpx) a = tmp[0], b = tmp[1];
       out[k].re = a.re + b.re; out[k].im = a.im + b.im;
@@ -142,26 +155,43 @@ typedef struct {
   long long a, b;            /* strided real passes: [a][L][b] */
 } SFX(batch);
 
+/* Lines li of [b0, b1); on a strided axis up to ORC_COLS neighbouring
+ * columns of one slab move together (each line position j is then one
+ * contiguous run of the array), each transformed on its own as before. */
+#define ORC_COLS 8
 static void SFX(axis_worker)(void* ctx, long long b0, long long b1, int tid) {
   (void)tid;
   SFX(batch)* B = (SFX(batch)*)ctx;
   const int L = B->L;
-  SFX(cpx)* buf = (SFX(cpx)*)malloc(sizeof(SFX(cpx)) * (3 * (size_t)L + 8));
-  for (long long li = b0; li < b1; ++li) {
-    long long base = (li / B->nb) * B->bstride + (li % B->nb);
+  const int cols = B->lstride > 1 ? ORC_COLS : 1;
+  SFX(cpx)* io = (SFX(cpx)*)malloc(sizeof(SFX(cpx)) * ((size_t)L * cols + 2 * (size_t)L + 8));
+  SFX(cpx)* buf = io + (size_t)L * cols;
+  for (long long li = b0; li < b1;) {
+    const long long base = (li / B->nb) * B->bstride + (li % B->nb);
+    long long c = B->nb - li % B->nb; /* columns left in this slab */
+    if (c > cols) c = cols;
+    if (c > b1 - li) c = b1 - li;
     for (int j = 0; j < L; ++j) {
       const double* s = B->data + 2 * (base + j * B->lstride);
-      buf[j].re = s[0];
-      buf[j].im = s[1];
+      for (long long t = 0; t < c; ++t) {
+        io[t * L + j].re = s[2 * t];
+        io[t * L + j].im = s[2 * t + 1];
+      }
     }
-    SFX(fft_line)(&B->pl, buf, buf + L, B->sign, buf + 2 * L);
+    for (long long t = 0; t < c; ++t) {
+      SFX(fft_line)(&B->pl, io + t * L, buf, B->sign, buf + L);
+      memcpy(io + t * L, buf, sizeof(SFX(cpx)) * (size_t)L);
+    }
     for (int j = 0; j < L; ++j) {
       double* d = B->data + 2 * (base + j * B->lstride);
-      d[0] = (double)buf[L + j].re;
-      d[1] = (double)buf[L + j].im;
+      for (long long t = 0; t < c; ++t) {
+        d[2 * t] = (double)io[t * L + j].re;
+        d[2 * t + 1] = (double)io[t * L + j].im;
+      }
     }
+    li += c;
   }
-  free(buf);
+  free(io);
 }
 
 static int SFX(c2c_axis)(int n0, int n1, int w, int axis, double* data, int sign, int nthreads) {
