@@ -232,12 +232,33 @@ static void SFX(c2r_line)(SFX(batch) * B, SFX(cpx) * buf) {
   SFX(fft_line)(&B->pl, buf, buf + L, +1, buf + 2 * L);
 }
 
+/* Rows r and r+1 go through one complex transform of x_r + i x_{r+1}:
+ * A[k] = (X[k] + conj X[L-k]) / 2, B[k] = (X[k] - conj X[L-k]) / 2i (both rows
+ * are read before either is written, so in-place rows are fine); an odd last
+ * row runs alone. */
 static void SFX(r2c_z_worker)(void* ctx, long long b0, long long b1, int tid) {
   (void)tid;
   SFX(batch)* B = (SFX(batch)*)ctx;
   const int L = B->L, H = L / 2 + 1;
   SFX(cpx)* buf = (SFX(cpx)*)malloc(sizeof(SFX(cpx)) * (3 * (size_t)L + 8));
-  for (long long r = b0; r < b1; ++r) {
+  long long r = b0;
+  for (; r + 1 < b1; r += 2) {
+    const double* s0 = B->rin + r * B->in_row;
+    const double* s1 = s0 + B->in_row;
+    for (int j = 0; j < L; ++j) { buf[j].re = s0[j]; buf[j].im = s1[j]; }
+    SFX(fft_line)(&B->pl, buf, buf + L, -1, buf + 2 * L);
+    const SFX(cpx)* X = buf + L;
+    double* d0 = B->rout + 2 * r * B->out_row;
+    double* d1 = d0 + 2 * B->out_row;
+    for (int k = 0; k < H; ++k) {
+      const SFX(cpx) x = X[k], y = X[k == 0 ? 0 : L - k];
+      d0[2 * k] = (double)((REAL)0.5 * (x.re + y.re));
+      d0[2 * k + 1] = (double)((REAL)0.5 * (x.im - y.im));
+      d1[2 * k] = (double)((REAL)0.5 * (x.im + y.im));
+      d1[2 * k + 1] = (double)((REAL)-0.5 * (x.re - y.re));
+    }
+  }
+  for (; r < b1; ++r) {
     const double* s = B->rin + r * B->in_row;
     for (int j = 0; j < L; ++j) { buf[j].re = s[j]; buf[j].im = 0; }
     SFX(r2c_line)(B, buf);
@@ -247,12 +268,32 @@ static void SFX(r2c_z_worker)(void* ctx, long long b0, long long b1, int tid) {
   free(buf);
 }
 
+/* Rows r and r+1 go through one backward transform of A + iB (A, B their
+ * Hermitian completions, imaginary parts of k = 0 and L/2 dropped): the
+ * result is a + ib, a and b the two real rows; an odd last row runs alone. */
 static void SFX(c2r_z_worker)(void* ctx, long long b0, long long b1, int tid) {
   (void)tid;
   SFX(batch)* B = (SFX(batch)*)ctx;
   const int L = B->L, H = L / 2 + 1;
   SFX(cpx)* buf = (SFX(cpx)*)malloc(sizeof(SFX(cpx)) * (3 * (size_t)L + 8));
-  for (long long r = b0; r < b1; ++r) {
+  long long r = b0;
+  for (; r + 1 < b1; r += 2) {
+    const double* h0 = B->rin + 2 * r * B->in_row;
+    const double* h1 = h0 + 2 * B->in_row;
+    for (int p = 0; p < L; ++p) {
+      const int q = p < H ? p : L - p;
+      REAL ar = h0[2 * q], ai = h0[2 * q + 1], br = h1[2 * q], bi = h1[2 * q + 1];
+      if (p == 0 || 2 * p == L) ai = bi = 0;
+      if (p >= H) { ai = -ai; bi = -bi; }
+      buf[p].re = ar - bi;
+      buf[p].im = ai + br;
+    }
+    SFX(fft_line)(&B->pl, buf, buf + L, +1, buf + 2 * L);
+    double* d0 = B->rout + r * B->out_row;
+    double* d1 = d0 + B->out_row;
+    for (int j = 0; j < L; ++j) { d0[j] = (double)buf[L + j].re; d1[j] = (double)buf[L + j].im; }
+  }
+  for (; r < b1; ++r) {
     const double* s = B->rin + 2 * r * B->in_row;
     for (int k = 0; k < H; ++k) { buf[k].re = s[2 * k]; buf[k].im = s[2 * k + 1]; }
     SFX(c2r_line)(B, buf);
