@@ -21,8 +21,9 @@
  *   - single-axis real transforms for the x and y derivatives
  *     (src/accfft_gpu.cpp:254-323, 1319-1604)
  *
- * Transforms: recursive mixed-radix decimation in time (any factorisation;
- * prime factors by direct DFT), twiddles from an exactly reduced angle.  Each
+ * Transforms: mixed-radix Stockham stages (any factorisation; radix 2 and 4
+ * butterflies, other prime factors by direct DFT), twiddles from an exactly
+ * reduced angle.  Each
  * entry point computes in double (prec == 0) or long double (prec == 1);
  * arrays are always double (complex = interleaved re, im).
  * Lines are processed by `nthreads` POSIX threads.

@@ -12,7 +12,10 @@ typedef struct {
   int n;
   int nf;
   int fac[ORC_MAX_FACTORS];
-  SFX(cpx) * w; /* w[k] = exp(-2*pi*i*k/n) */
+  SFX(cpx) * w;  /* w[k] = exp(-2*pi*i*k/n) */
+  SFX(cpx) * tw; /* stage s (radix p, Ns = product of the earlier radices) at
+                    tw + toff[s]: w_{Ns*p}^{q*k} at k*(p-1) + q-1, q in [1,p), k < Ns */
+  long long toff[ORC_MAX_FACTORS];
 } SFX(plan1d);
 
 /* exp(-2*pi*i*m/d): integer octant reduction, then cos/sin on [0, pi/4] */
@@ -46,9 +49,25 @@ static int SFX(plan_init)(SFX(plan1d) * p, int n) {
     else f = (f == 2) ? 3 : f + 2;
   }
   if (m != 1) return -1;
-  p->w = (SFX(cpx)*)malloc(sizeof(SFX(cpx)) * (size_t)n);
+  long long ntw = 0, Ns = 1;
+  for (int s = 0; s < p->nf; ++s) {
+    p->toff[s] = ntw;
+    ntw += Ns * (p->fac[s] - 1);
+    Ns *= p->fac[s];
+  }
+  p->w = (SFX(cpx)*)malloc(sizeof(SFX(cpx)) * ((size_t)n + (size_t)ntw + 1));
   if (!p->w) return -1;
+  p->tw = p->w + n;
   for (int k = 0; k < n; ++k) SFX(twid)(k, n, &p->w[k].re, &p->w[k].im);
+  /* w_{Ns*p}^{q*k} = w_n^{q*k*(n/(Ns*p))}, the exponent below n */
+  Ns = 1;
+  for (int s = 0; s < p->nf; ++s) {
+    const int r = p->fac[s];
+    const long long step = n / (Ns * r);
+    for (long long k = 0; k < Ns; ++k)
+      for (int q = 1; q < r; ++q) p->tw[p->toff[s] + k * (r - 1) + q - 1] = p->w[q * k * step];
+    Ns *= r;
+  }
   return 0;
 }
 
@@ -61,71 +80,71 @@ static inline SFX(cpx) SFX(cmul)(SFX(cpx) a, SFX(cpx) b) {
   return r;
 }
 
-/* w_N^e for the transform sign (conjugate table entry for sign > 0) */
-static inline SFX(cpx) SFX(wexp)(const SFX(cpx) * w, long long N, long long e, int sign) {
-  SFX(cpx) t = w[e % N];
-  if (sign > 0) t.im = -t.im;
-  return t;
-}
-/* the same for 0 <= e < N (no reduction) */
-static inline SFX(cpx) SFX(wexp_in)(const SFX(cpx) * w, long long e, int sign) {
-  SFX(cpx) t = w[e];
-  if (sign > 0) t.im = -t.im;
-  return t;
-}
-
-/* Recursive decimation in time.  Sub-transform of length n reads in[j*is]
- * for j < n; w is the table of the top-level length N and wstep = N/n.
- * The twiddle exponent q*k*wstep stays below p*m*wstep = N.  A last factor
- * (m == 1) reads its inputs directly: its length-1 sub-transforms are
- * copies and its twiddles are w^0 = 1. */
-static void SFX(rec)(const SFX(cpx) * in, long long is, SFX(cpx) * out, int n, const int* fac, const SFX(cpx) * w,
-                     long long N, long long wstep, int sign, SFX(cpx) * tmp) {
-  if (n == 1) {
+/* Stockham autosort, one stage per factor: stage s of radix p (Ns = product
+ * of the earlier radices, m = n/p) takes x[j + q*m] for q < p, multiplies
+ * entry q by w_{Ns*p}^{q*(j%Ns)}, runs the p-point DFT and writes output r at
+ * (j/Ns)*Ns*p + j%Ns + r*Ns.  `in` is read by the first stage only; the
+ * stages alternate between `out` and `tmp` so that the last one writes
+ * `out` (both n entries). */
+static void SFX(fft_line)(const SFX(plan1d) * P, const SFX(cpx) * in, SFX(cpx) * out, int sign, SFX(cpx) * tmp) {
+  const int n = P->n, nf = P->nf;
+  if (nf == 0) {
     out[0] = in[0];
     return;
   }
-  const int p = fac[0], m = n / p;
-  if (m > 1)
-    for (int q = 0; q < p; ++q) SFX(rec)(in + q * is, is * p, out + q * m, m, fac + 1, w, N, wstep * p, sign, tmp);
-  for (int k = 0; k < m; ++k) {
-    if (m == 1)
-      for (int q = 0; q < p; ++q) tmp[q] = in[q * is];
-    else
-      for (int q = 0; q < p; ++q) tmp[q] = SFX(cmul)(out[q * m + k], SFX(wexp_in)(w, (long long)q * k * wstep, sign));
-    if (p == 2) {
-      SFX(cpx) a = tmp[0], b = tmp[1];
-      out[k].re = a.re + b.re; out[k].im = a.im + b.im;
-      out[m + k].re = a.re - b.re; out[m + k].im = a.im - b.im;
-    } else if (p == 4) {
-      /* X[r] = sum_q t[q] w_4^{qr}; w_4 = -i (forward) or +i (backward) */
-      SFX(cpx) s02 = {tmp[0].re + tmp[2].re, tmp[0].im + tmp[2].im};
-      SFX(cpx) d02 = {tmp[0].re - tmp[2].re, tmp[0].im - tmp[2].im};
-      SFX(cpx) s13 = {tmp[1].re + tmp[3].re, tmp[1].im + tmp[3].im};
-      SFX(cpx) d13 = {tmp[1].re - tmp[3].re, tmp[1].im - tmp[3].im};
-      SFX(cpx) rd; /* w_4 * d13 */
-      if (sign < 0) { rd.re = d13.im; rd.im = -d13.re; }
-      else { rd.re = -d13.im; rd.im = d13.re; }
-      out[k].re = s02.re + s13.re; out[k].im = s02.im + s13.im;
-      out[m + k].re = d02.re + rd.re; out[m + k].im = d02.im + rd.im;
-      out[2 * m + k].re = s02.re - s13.re; out[2 * m + k].im = s02.im - s13.im;
-      out[3 * m + k].re = d02.re - rd.re; out[3 * m + k].im = d02.im - rd.im;
-    } else {
-      for (int r = 0; r < p; ++r) {
-        SFX(cpx) acc = {0, 0};
-        for (int q = 0; q < p; ++q) {
-          SFX(cpx) t = SFX(cmul)(tmp[q], SFX(wexp)(w, N, (long long)q * r * m * wstep, sign));
-          acc.re += t.re;
-          acc.im += t.im;
+  const SFX(cpx)* src = in;
+  long long Ns = 1;
+  for (int s = 0; s < nf; ++s) {
+    const int p = P->fac[s];
+    const long long m = n / p;
+    SFX(cpx)* dst = ((nf - 1 - s) % 2 == 0) ? out : tmp;
+    const SFX(cpx)* t = P->tw + P->toff[s];
+    for (long long j0 = 0; j0 < m; j0 += Ns) {
+      for (long long k = 0; k < Ns; ++k) {
+        const long long j = j0 + k;
+        SFX(cpx) x[p];
+        x[0] = src[j];
+        for (int q = 1; q < p; ++q) {
+          SFX(cpx) w = t[k * (p - 1) + q - 1];
+          if (sign > 0) w.im = -w.im;
+          x[q] = SFX(cmul)(src[j + q * m], w);
         }
-        out[r * m + k] = acc;
+        SFX(cpx)* y = dst + j0 * p + k;
+        if (p == 2) {
+          y[0].re = x[0].re + x[1].re; y[0].im = x[0].im + x[1].im;
+          y[Ns].re = x[0].re - x[1].re; y[Ns].im = x[0].im - x[1].im;
+        } else if (p == 4) {
+          /* X[r] = sum_q x[q] w_4^{qr}; w_4 = -i (forward) or +i (backward) */
+          const SFX(cpx) s02 = {x[0].re + x[2].re, x[0].im + x[2].im};
+          const SFX(cpx) d02 = {x[0].re - x[2].re, x[0].im - x[2].im};
+          const SFX(cpx) s13 = {x[1].re + x[3].re, x[1].im + x[3].im};
+          const SFX(cpx) d13 = {x[1].re - x[3].re, x[1].im - x[3].im};
+          SFX(cpx) rd; /* w_4 * d13 */
+          if (sign < 0) { rd.re = d13.im; rd.im = -d13.re; }
+          else { rd.re = -d13.im; rd.im = d13.re; }
+          y[0].re = s02.re + s13.re; y[0].im = s02.im + s13.im;
+          y[Ns].re = d02.re + rd.re; y[Ns].im = d02.im + rd.im;
+          y[2 * Ns].re = s02.re - s13.re; y[2 * Ns].im = s02.im - s13.im;
+          y[3 * Ns].re = d02.re - rd.re; y[3 * Ns].im = d02.im - rd.im;
+        } else {
+          /* direct p-point DFT: w_p^e = w_n^{(e mod p) * m} */
+          for (int r = 0; r < p; ++r) {
+            SFX(cpx) acc = x[0];
+            for (int q = 1; q < p; ++q) {
+              SFX(cpx) w = P->w[(long long)((q * r) % p) * m];
+              if (sign > 0) w.im = -w.im;
+              const SFX(cpx) v = SFX(cmul)(x[q], w);
+              acc.re += v.re;
+              acc.im += v.im;
+            }
+            y[r * Ns] = acc;
+          }
+        }
       }
     }
+    src = dst;
+    Ns *= p;
   }
-}
-
-static void SFX(fft_line)(const SFX(plan1d) * p, const SFX(cpx) * in, SFX(cpx) * out, int sign, SFX(cpx) * tmp) {
-  SFX(rec)(in, 1, out, p->n, p->fac, p->w, p->n, 1, sign, tmp);
 }
 
 static int SFX(fft1d)(int n, const double* in, double* out, int sign) {
