@@ -785,6 +785,7 @@ def ours(args):
     }
     if not args.no_baseline and world == 1:
         v, sample, th = cpu_pairs_per_s(n)
+        _CPU_ARRAYS.clear()   # the sample's host arrays (several GB at 512^3) are not needed again
         line["cpu_baseline"] = {"value": v, "unit": "pairs/s", "cores": th, "kind": "port", "sample": sample,
                                 "stand_in": stand_in(n)}
     print(json.dumps(line), flush=True)
