@@ -1,6 +1,6 @@
 """Host logic of bench.py on the CPU: the byte model, the replicas-only
-multi-process timing (world size 2 over gloo) and the reference arm's
-rank-0-only output."""
+multi-process timing (world size 2 over gloo), the reference arm's
+rank-0-only output and the CPU baseline's sampling."""
 import json
 import os
 import socket
@@ -59,3 +59,20 @@ def test_reference_arm_prints_on_rank_zero_only(monkeypatch, capsys):
     monkeypatch.setattr(sys, "argv", ["bench.py", "--impl", "reference", "--steps", "1", "--warmup", "0"])
     bench.main()
     assert capsys.readouterr().out == ""
+
+
+def test_cpu_baseline_sample_is_chosen_once_and_repeats_whole_pairs():
+    """The CPU baseline (oracle, all host threads) picks its sample once per
+    grid and budget; a budget above one pair's time repeats whole pairs."""
+    bench._CPU_FRACTION.clear()
+    bench._CPU_ARRAYS.clear()
+    n = (16, 12, 10)
+    v1, s1, th = bench.cpu_pairs_per_s(n, budget_s=0.05, nthreads=2)
+    v2, s2, _ = bench.cpu_pairs_per_s(n, budget_s=0.05, nthreads=2)
+    assert v1 > 0 and v2 > 0 and th == 2
+    assert s1 == s2 and s1.endswith("double, 2 threads")
+    reps = int(s1.split(" x ")[0])
+    assert reps >= 1 and "1.0000 of one 16x12x10 pair" in s1
+    assert len(bench._CPU_FRACTION) == 1 and len(bench._CPU_ARRAYS) == 1
+    bench._CPU_FRACTION.clear()
+    bench._CPU_ARRAYS.clear()
