@@ -83,61 +83,76 @@ static inline SFX(cpx) SFX(cmul)(SFX(cpx) a, SFX(cpx) b) {
 /* Stockham autosort, one stage per factor: stage s of radix p (Ns = product
  * of the earlier radices, m = n/p) takes x[j + q*m] for q < p, multiplies
  * entry q by w_{Ns*p}^{q*(j%Ns)}, runs the p-point DFT and writes output r at
- * (j/Ns)*Ns*p + j%Ns + r*Ns.  `in` is read by the first stage only; the
- * stages alternate between `out` and `tmp` so that the last one writes
- * `out` (both n entries). */
-static void SFX(fft_line)(const SFX(plan1d) * P, const SFX(cpx) * in, SFX(cpx) * out, int sign, SFX(cpx) * tmp) {
+ * (j/Ns)*Ns*p + j%Ns + r*Ns.  V lines run together, element-major (entry j of
+ * line t at x[j*V + t]), sharing each twiddle.  `in` is read by the first
+ * stage only; the stages alternate between `out` and `tmp` so that the last
+ * one writes `out` (both n*V entries). */
+static void SFX(fft_lines)(const SFX(plan1d) * P, const SFX(cpx) * in, SFX(cpx) * out, int sign, SFX(cpx) * tmp,
+                           int V) {
   const int n = P->n, nf = P->nf;
   if (nf == 0) {
-    out[0] = in[0];
+    for (int t = 0; t < V; ++t) out[t] = in[t];
     return;
   }
+  const REAL sg = sign < 0 ? (REAL)1 : (REAL)-1; /* w_4 * d = (sg * d.im, -sg * d.re) */
   const SFX(cpx)* src = in;
   long long Ns = 1;
   for (int s = 0; s < nf; ++s) {
     const int p = P->fac[s];
-    const long long m = n / p;
+    const long long m = n / p, xs = m * V;
     SFX(cpx)* dst = ((nf - 1 - s) % 2 == 0) ? out : tmp;
-    const SFX(cpx)* t = P->tw + P->toff[s];
+    const SFX(cpx)* tw = P->tw + P->toff[s];
+    const long long ys = Ns * V;
     for (long long j0 = 0; j0 < m; j0 += Ns) {
       for (long long k = 0; k < Ns; ++k) {
-        const long long j = j0 + k;
-        SFX(cpx) x[p];
-        x[0] = src[j];
-        for (int q = 1; q < p; ++q) {
-          SFX(cpx) w = t[k * (p - 1) + q - 1];
-          if (sign > 0) w.im = -w.im;
-          x[q] = SFX(cmul)(src[j + q * m], w);
-        }
-        SFX(cpx)* y = dst + j0 * p + k;
+        const SFX(cpx)* x = src + (j0 + k) * V;
+        SFX(cpx)* y = dst + (j0 * p + k) * V;
         if (p == 2) {
-          y[0].re = x[0].re + x[1].re; y[0].im = x[0].im + x[1].im;
-          y[Ns].re = x[0].re - x[1].re; y[Ns].im = x[0].im - x[1].im;
+          SFX(cpx) w = tw[k];
+          if (sign > 0) w.im = -w.im;
+          for (int t = 0; t < V; ++t) {
+            const SFX(cpx) a = x[t], b = SFX(cmul)(x[xs + t], w);
+            y[t].re = a.re + b.re; y[t].im = a.im + b.im;
+            y[ys + t].re = a.re - b.re; y[ys + t].im = a.im - b.im;
+          }
         } else if (p == 4) {
           /* X[r] = sum_q x[q] w_4^{qr}; w_4 = -i (forward) or +i (backward) */
-          const SFX(cpx) s02 = {x[0].re + x[2].re, x[0].im + x[2].im};
-          const SFX(cpx) d02 = {x[0].re - x[2].re, x[0].im - x[2].im};
-          const SFX(cpx) s13 = {x[1].re + x[3].re, x[1].im + x[3].im};
-          const SFX(cpx) d13 = {x[1].re - x[3].re, x[1].im - x[3].im};
-          SFX(cpx) rd; /* w_4 * d13 */
-          if (sign < 0) { rd.re = d13.im; rd.im = -d13.re; }
-          else { rd.re = -d13.im; rd.im = d13.re; }
-          y[0].re = s02.re + s13.re; y[0].im = s02.im + s13.im;
-          y[Ns].re = d02.re + rd.re; y[Ns].im = d02.im + rd.im;
-          y[2 * Ns].re = s02.re - s13.re; y[2 * Ns].im = s02.im - s13.im;
-          y[3 * Ns].re = d02.re - rd.re; y[3 * Ns].im = d02.im - rd.im;
+          SFX(cpx) w1 = tw[3 * k], w2 = tw[3 * k + 1], w3 = tw[3 * k + 2];
+          if (sign > 0) { w1.im = -w1.im; w2.im = -w2.im; w3.im = -w3.im; }
+          for (int t = 0; t < V; ++t) {
+            const SFX(cpx) a0 = x[t], a1 = SFX(cmul)(x[xs + t], w1), a2 = SFX(cmul)(x[2 * xs + t], w2),
+                           a3 = SFX(cmul)(x[3 * xs + t], w3);
+            const SFX(cpx) s02 = {a0.re + a2.re, a0.im + a2.im};
+            const SFX(cpx) d02 = {a0.re - a2.re, a0.im - a2.im};
+            const SFX(cpx) s13 = {a1.re + a3.re, a1.im + a3.im};
+            const SFX(cpx) d13 = {a1.re - a3.re, a1.im - a3.im};
+            const SFX(cpx) rd = {sg * d13.im, -sg * d13.re};
+            y[t].re = s02.re + s13.re; y[t].im = s02.im + s13.im;
+            y[ys + t].re = d02.re + rd.re; y[ys + t].im = d02.im + rd.im;
+            y[2 * ys + t].re = s02.re - s13.re; y[2 * ys + t].im = s02.im - s13.im;
+            y[3 * ys + t].re = d02.re - rd.re; y[3 * ys + t].im = d02.im - rd.im;
+          }
         } else {
           /* direct p-point DFT: w_p^e = w_n^{(e mod p) * m} */
-          for (int r = 0; r < p; ++r) {
-            SFX(cpx) acc = x[0];
+          SFX(cpx) xq[p];
+          for (int t = 0; t < V; ++t) {
+            xq[0] = x[t];
             for (int q = 1; q < p; ++q) {
-              SFX(cpx) w = P->w[(long long)((q * r) % p) * m];
+              SFX(cpx) w = tw[k * (p - 1) + q - 1];
               if (sign > 0) w.im = -w.im;
-              const SFX(cpx) v = SFX(cmul)(x[q], w);
-              acc.re += v.re;
-              acc.im += v.im;
+              xq[q] = SFX(cmul)(x[q * xs + t], w);
             }
-            y[r * Ns] = acc;
+            for (int r = 0; r < p; ++r) {
+              SFX(cpx) acc = xq[0];
+              for (int q = 1; q < p; ++q) {
+                SFX(cpx) w = P->w[(long long)((q * r) % p) * m];
+                if (sign > 0) w.im = -w.im;
+                const SFX(cpx) v = SFX(cmul)(xq[q], w);
+                acc.re += v.re;
+                acc.im += v.im;
+              }
+              y[r * ys + t] = acc;
+            }
           }
         }
       }
@@ -145,6 +160,11 @@ static void SFX(fft_line)(const SFX(plan1d) * P, const SFX(cpx) * in, SFX(cpx) *
     src = dst;
     Ns *= p;
   }
+}
+
+/* one line (V = 1) */
+static void SFX(fft_line)(const SFX(plan1d) * P, const SFX(cpx) * in, SFX(cpx) * out, int sign, SFX(cpx) * tmp) {
+  SFX(fft_lines)(P, in, out, sign, tmp, 1);
 }
 
 static int SFX(fft1d)(int n, const double* in, double* out, int sign) {
@@ -174,38 +194,44 @@ typedef struct {
   long long a, b;            /* strided real passes: [a][L][b] */
 } SFX(batch);
 
-/* Lines li of [b0, b1); on a strided axis up to ORC_COLS neighbouring
- * columns of one slab move together (each line position j is then one
- * contiguous run of the array), each transformed on its own as before. */
+/* Lines li of [b0, b1), ORC_COLS at a time through fft_lines: on a strided
+ * axis neighbouring columns of one slab (each line position j is one
+ * contiguous run of the array), on the contiguous axis consecutive rows. */
 #define ORC_COLS 8
 static void SFX(axis_worker)(void* ctx, long long b0, long long b1, int tid) {
   (void)tid;
   SFX(batch)* B = (SFX(batch)*)ctx;
   const int L = B->L;
-  const int cols = B->lstride > 1 ? ORC_COLS : 1;
-  SFX(cpx)* io = (SFX(cpx)*)malloc(sizeof(SFX(cpx)) * ((size_t)L * cols + 2 * (size_t)L + 8));
-  SFX(cpx)* buf = io + (size_t)L * cols;
+  const size_t blk = (size_t)L * ORC_COLS;
+  SFX(cpx)* io = (SFX(cpx)*)malloc(sizeof(SFX(cpx)) * (3 * blk + 8));
+  SFX(cpx)* res = io + blk;
+  long long base[ORC_COLS];
   for (long long li = b0; li < b1;) {
-    const long long base = (li / B->nb) * B->bstride + (li % B->nb);
-    long long c = B->nb - li % B->nb; /* columns left in this slab */
-    if (c > cols) c = cols;
+    long long c = B->nb > 1 ? B->nb - li % B->nb : ORC_COLS; /* lines left in this slab */
+    if (c > ORC_COLS) c = ORC_COLS;
     if (c > b1 - li) c = b1 - li;
-    for (int j = 0; j < L; ++j) {
-      const double* s = B->data + 2 * (base + j * B->lstride);
+    for (long long t = 0; t < c; ++t) base[t] = ((li + t) / B->nb) * B->bstride + (li + t) % B->nb;
+    if (B->lstride > 1) { /* strided: row j of the block is one run of c entries */
+      for (int j = 0; j < L; ++j) {
+        const double* s = B->data + 2 * (base[0] + j * B->lstride);
+        for (long long t = 0; t < c; ++t) { io[j * c + t].re = s[2 * t]; io[j * c + t].im = s[2 * t + 1]; }
+      }
+    } else {
       for (long long t = 0; t < c; ++t) {
-        io[t * L + j].re = s[2 * t];
-        io[t * L + j].im = s[2 * t + 1];
+        const double* s = B->data + 2 * base[t];
+        for (int j = 0; j < L; ++j) { io[j * c + t].re = s[2 * j]; io[j * c + t].im = s[2 * j + 1]; }
       }
     }
-    for (long long t = 0; t < c; ++t) {
-      SFX(fft_line)(&B->pl, io + t * L, buf, B->sign, buf + L);
-      memcpy(io + t * L, buf, sizeof(SFX(cpx)) * (size_t)L);
-    }
-    for (int j = 0; j < L; ++j) {
-      double* d = B->data + 2 * (base + j * B->lstride);
+    SFX(fft_lines)(&B->pl, io, res, B->sign, res + blk, (int)c);
+    if (B->lstride > 1) {
+      for (int j = 0; j < L; ++j) {
+        double* d = B->data + 2 * (base[0] + j * B->lstride);
+        for (long long t = 0; t < c; ++t) { d[2 * t] = (double)res[j * c + t].re; d[2 * t + 1] = (double)res[j * c + t].im; }
+      }
+    } else {
       for (long long t = 0; t < c; ++t) {
-        d[2 * t] = (double)io[t * L + j].re;
-        d[2 * t + 1] = (double)io[t * L + j].im;
+        double* d = B->data + 2 * base[t];
+        for (int j = 0; j < L; ++j) { d[2 * j] = (double)res[j * c + t].re; d[2 * j + 1] = (double)res[j * c + t].im; }
       }
     }
     li += c;
@@ -252,74 +278,89 @@ static void SFX(c2r_line)(SFX(batch) * B, SFX(cpx) * buf) {
 }
 
 /* Rows r and r+1 go through one complex transform of x_r + i x_{r+1}:
- * A[k] = (X[k] + conj X[L-k]) / 2, B[k] = (X[k] - conj X[L-k]) / 2i (both rows
- * are read before either is written, so in-place rows are fine); an odd last
- * row runs alone. */
+ * A[k] = (X[k] + conj X[L-k]) / 2, B[k] = (X[k] - conj X[L-k]) / 2i; up to
+ * ORC_COLS such pairs run together through fft_lines.  Every row of a block
+ * is read before any is written, so in-place rows are fine; an odd last row
+ * pairs with zeros. */
 static void SFX(r2c_z_worker)(void* ctx, long long b0, long long b1, int tid) {
   (void)tid;
   SFX(batch)* B = (SFX(batch)*)ctx;
   const int L = B->L, H = L / 2 + 1;
-  SFX(cpx)* buf = (SFX(cpx)*)malloc(sizeof(SFX(cpx)) * (3 * (size_t)L + 8));
-  long long r = b0;
-  for (; r + 1 < b1; r += 2) {
-    const double* s0 = B->rin + r * B->in_row;
-    const double* s1 = s0 + B->in_row;
-    for (int j = 0; j < L; ++j) { buf[j].re = s0[j]; buf[j].im = s1[j]; }
-    SFX(fft_line)(&B->pl, buf, buf + L, -1, buf + 2 * L);
-    const SFX(cpx)* X = buf + L;
-    double* d0 = B->rout + 2 * r * B->out_row;
-    double* d1 = d0 + 2 * B->out_row;
-    for (int k = 0; k < H; ++k) {
-      const SFX(cpx) x = X[k], y = X[k == 0 ? 0 : L - k];
-      d0[2 * k] = (double)((REAL)0.5 * (x.re + y.re));
-      d0[2 * k + 1] = (double)((REAL)0.5 * (x.im - y.im));
-      d1[2 * k] = (double)((REAL)0.5 * (x.im + y.im));
-      d1[2 * k + 1] = (double)((REAL)-0.5 * (x.re - y.re));
+  const size_t blk = (size_t)L * ORC_COLS;
+  SFX(cpx)* io = (SFX(cpx)*)malloc(sizeof(SFX(cpx)) * (3 * blk + 8));
+  SFX(cpx)* X = io + blk;
+  for (long long r = b0; r < b1;) {
+    long long rows = b1 - r;
+    if (rows > 2 * ORC_COLS) rows = 2 * ORC_COLS;
+    const int c = (int)((rows + 1) / 2);
+    for (int t = 0; t < c; ++t) {
+      const double* s0 = B->rin + (r + 2 * t) * B->in_row;
+      const int two = 2 * t + 1 < rows;
+      for (int j = 0; j < L; ++j) {
+        io[j * c + t].re = s0[j];
+        io[j * c + t].im = two ? s0[B->in_row + j] : 0;
+      }
     }
+    SFX(fft_lines)(&B->pl, io, X, -1, X + blk, c);
+    for (int t = 0; t < c; ++t) {
+      double* d0 = B->rout + 2 * (r + 2 * t) * B->out_row;
+      const int two = 2 * t + 1 < rows;
+      for (int k = 0; k < H; ++k) {
+        const SFX(cpx) x = X[k * c + t], y = X[(k == 0 ? 0 : L - k) * c + t];
+        d0[2 * k] = (double)((REAL)0.5 * (x.re + y.re));
+        d0[2 * k + 1] = (double)((REAL)0.5 * (x.im - y.im));
+        if (two) {
+          d0[2 * B->out_row + 2 * k] = (double)((REAL)0.5 * (x.im + y.im));
+          d0[2 * B->out_row + 2 * k + 1] = (double)((REAL)-0.5 * (x.re - y.re));
+        }
+      }
+    }
+    r += rows;
   }
-  for (; r < b1; ++r) {
-    const double* s = B->rin + r * B->in_row;
-    for (int j = 0; j < L; ++j) { buf[j].re = s[j]; buf[j].im = 0; }
-    SFX(r2c_line)(B, buf);
-    double* d = B->rout + 2 * r * B->out_row;
-    for (int k = 0; k < H; ++k) { d[2 * k] = (double)buf[L + k].re; d[2 * k + 1] = (double)buf[L + k].im; }
-  }
-  free(buf);
+  free(io);
 }
 
 /* Rows r and r+1 go through one backward transform of A + iB (A, B their
  * Hermitian completions, imaginary parts of k = 0 and L/2 dropped): the
- * result is a + ib, a and b the two real rows; an odd last row runs alone. */
+ * result is a + ib, a and b the two real rows; up to ORC_COLS pairs run
+ * together, an odd last row pairs with zeros. */
 static void SFX(c2r_z_worker)(void* ctx, long long b0, long long b1, int tid) {
   (void)tid;
   SFX(batch)* B = (SFX(batch)*)ctx;
   const int L = B->L, H = L / 2 + 1;
-  SFX(cpx)* buf = (SFX(cpx)*)malloc(sizeof(SFX(cpx)) * (3 * (size_t)L + 8));
-  long long r = b0;
-  for (; r + 1 < b1; r += 2) {
-    const double* h0 = B->rin + 2 * r * B->in_row;
-    const double* h1 = h0 + 2 * B->in_row;
-    for (int p = 0; p < L; ++p) {
-      const int q = p < H ? p : L - p;
-      REAL ar = h0[2 * q], ai = h0[2 * q + 1], br = h1[2 * q], bi = h1[2 * q + 1];
-      if (p == 0 || 2 * p == L) ai = bi = 0;
-      if (p >= H) { ai = -ai; bi = -bi; }
-      buf[p].re = ar - bi;
-      buf[p].im = ai + br;
+  const size_t blk = (size_t)L * ORC_COLS;
+  SFX(cpx)* io = (SFX(cpx)*)malloc(sizeof(SFX(cpx)) * (3 * blk + 8));
+  SFX(cpx)* Y = io + blk;
+  for (long long r = b0; r < b1;) {
+    long long rows = b1 - r;
+    if (rows > 2 * ORC_COLS) rows = 2 * ORC_COLS;
+    const int c = (int)((rows + 1) / 2);
+    for (int t = 0; t < c; ++t) {
+      const int two = 2 * t + 1 < rows;
+      const double* h0 = B->rin + 2 * (r + 2 * t) * B->in_row;
+      const double* h1 = two ? h0 + 2 * B->in_row : h0;
+      for (int p = 0; p < L; ++p) {
+        const int q = p < H ? p : L - p;
+        REAL ar = h0[2 * q], ai = h0[2 * q + 1], br = 0, bi = 0;
+        if (two) { br = h1[2 * q]; bi = h1[2 * q + 1]; }
+        if (p == 0 || 2 * p == L) ai = bi = 0;
+        if (p >= H) { ai = -ai; bi = -bi; }
+        io[p * c + t].re = ar - bi;
+        io[p * c + t].im = ai + br;
+      }
     }
-    SFX(fft_line)(&B->pl, buf, buf + L, +1, buf + 2 * L);
-    double* d0 = B->rout + r * B->out_row;
-    double* d1 = d0 + B->out_row;
-    for (int j = 0; j < L; ++j) { d0[j] = (double)buf[L + j].re; d1[j] = (double)buf[L + j].im; }
+    SFX(fft_lines)(&B->pl, io, Y, +1, Y + blk, c);
+    for (int t = 0; t < c; ++t) {
+      double* d0 = B->rout + (r + 2 * t) * B->out_row;
+      const int two = 2 * t + 1 < rows;
+      for (int j = 0; j < L; ++j) {
+        d0[j] = (double)Y[j * c + t].re;
+        if (two) d0[B->out_row + j] = (double)Y[j * c + t].im;
+      }
+    }
+    r += rows;
   }
-  for (; r < b1; ++r) {
-    const double* s = B->rin + 2 * r * B->in_row;
-    for (int k = 0; k < H; ++k) { buf[k].re = s[2 * k]; buf[k].im = s[2 * k + 1]; }
-    SFX(c2r_line)(B, buf);
-    double* d = B->rout + r * B->out_row;
-    for (int j = 0; j < L; ++j) d[j] = (double)buf[L + j].re;
-  }
-  free(buf);
+  free(io);
 }
 
 static int SFX(r2c_z)(long long rows, int n2, const double* in, long long in_row, double* out, long long out_row,
